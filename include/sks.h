@@ -1,0 +1,144 @@
+/*
+ * sks.h — C ABI of the GB300 (sm_103a) SEM time-stepping library.
+ *
+ * The reference solver `sem2d_psvsh` (semsyn/src/sem2d_psvsh.c) is a program:
+ * main() parses a getpar par file, meshes the box and fills per-point
+ * materials (discret, :534-828), builds GLL/mass/Stacey tables (:207-330),
+ * opens the receivers and the GRT boundary-trace files (:333-416), and then
+ * runs the time loop (:418-513) that writes seis.u/seis.w/seis.v.  It has no
+ * library interface, uses file-scope globals and exit()s on errors.
+ *
+ * This ABI is that program cut at its two natural seams, handle based and
+ * re-entrant: sks_open_par() is main() up to the time loop, sks_run() is the
+ * time loop, and the boundary traces may come from the par file's files
+ * (sks_load_boundary_files) or from caller memory (sks_set_boundary).
+ * Plain C types only.  Every call returns SKS_OK (0) or a negative status;
+ * sks_last_error() describes the last failure of the calling thread.
+ * The caller owns every host buffer it passes; the library owns device state.
+ * One host thread at a time per handle.
+ */
+#ifndef SKS_H
+#define SKS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (the reference exit()s with -1/-2/-3 or 100 instead:
+ * readmodel.c:15-19, sem2d_psvsh.c:591-594,699-702,831-838, getpar.c:560-568) */
+#define SKS_OK               0
+#define SKS_ERR_ARG         -1   /* bad argument or par value            */
+#define SKS_ERR_IO          -2   /* a named input file cannot be read    */
+#define SKS_ERR_MODEL       -3   /* ray/SEM model malformed or out of range */
+#define SKS_ERR_UNSUPPORTED -4   /* option outside this library's scope  */
+#define SKS_ERR_CUDA        -5   /* CUDA runtime failure                 */
+#define SKS_ERR_NOMEM       -6   /* host or device allocation failed     */
+#define SKS_ERR_BOUNDARY    -7   /* boundary records missing or short    */
+#define SKS_ERR_STATE       -8   /* call out of order                    */
+#define SKS_ERR_NONFINITE   -9   /* the wavefield stopped being finite   */
+
+/* arithmetic forms */
+#define SKS_FP64   0   /* plain FP64 3-level central-difference update      */
+#define SKS_FP32C  1   /* FP32 wavefield, Kahan-compensated leapfrog update,
+                          FP64 precompute and boundary-trace interpolation */
+
+typedef struct sks_solver sks_solver;
+
+typedef struct {
+    int32_t nex, nez, hpn;        /* elements in x and z, GLL degree N    */
+    int32_t nx, nz;               /* grid points: nex*N+1, nez*N+1        */
+    int32_t nst;                  /* time steps of the whole run          */
+    int32_t nt_inject;            /* steps that inject boundary traces    */
+    int32_t ntrace;               /* receivers                            */
+    int32_t mtotal, shtotal;      /* values per P-SV / SH boundary record */
+    int32_t nrec_psv, nrec_sh;    /* boundary records the run consumes    */
+    int32_t nmat;                 /* distinct materials                   */
+    int32_t anisotropic;          /* 1 if any material is not isotropic   */
+    int32_t precision;            /* SKS_FP64 or SKS_FP32C                */
+    int32_t step;                 /* next step sks_run() will take        */
+    double  eh, h, sdt;           /* element size, GLL spacing, time step */
+    int64_t device_bytes;         /* device memory held by the handle     */
+} sks_info_t;
+
+/* Replaces main() of sem2d_psvsh up to its time loop (sem2d_psvsh.c:82-416):
+ * argv holds getpar words ("par=run.par", "nst=2000", ...; argv[0] is the
+ * program name and is ignored).  Reads the ray model, the SEM model and the
+ * receiver file named there and builds the device state on `device`.  The
+ * boundary-trace files are NOT read here (see sks_load_boundary_files).
+ * Options the reference has that this library does not run return
+ * SKS_ERR_UNSUPPORTED: msource=1 (explosive source), atten>0. */
+int sks_open_par(int argc, const char *const *argv, int precision, int device,
+                 sks_solver **out);
+
+/* Reads greenfile/shgreenfile named in the par words (time-major float32
+ * records, interpl.c:16-54) and uploads the records the run needs. */
+int sks_load_boundary_files(sks_solver *s);
+
+/* Same from caller memory: psv holds nrec_psv records of mtotal floats, sh
+ * holds nrec_sh records of shtotal floats (sh may be NULL when the solver was
+ * opened with psv_only=1).  Records are copied to the device. */
+int sks_set_boundary(sks_solver *s, const float *psv, int32_t nrec_psv,
+                     const float *sh, int32_t nrec_sh);
+
+/* Replaces the time loop (sem2d_psvsh.c:418-513) for steps
+ * [step, step+nsteps): each step writes ntrace floats to each of seis_u
+ * (u_x), seis_w (-u_z) and seis_v (u_y), time-major, like kirrecord_zhl
+ * (sem2d_psvsh.c:2116-2160).  Buffers hold nsteps*ntrace floats; any may be
+ * NULL.  Returns the number of steps taken (>= 0) or a negative status. */
+int sks_run(sks_solver *s, int32_t nsteps, float *seis_u, float *seis_v, float *seis_w);
+
+/* Back to step 0 with a zero wavefield (boundary records are kept). */
+int sks_reset(sks_solver *s);
+
+int sks_get_info(const sks_solver *s, sks_info_t *info);
+
+/* ---- host-only set-up (no device needed) ------------------------------
+ * sks_setup_open() runs the set-up half of main() (par words, ray and SEM
+ * models, mesh, materials, GLL tables, mass, Stacey matrix, receivers and the
+ * boundary-record schedule) and keeps it on the host for inspection;
+ * sks_open_setup() turns it into a device solver. */
+typedef struct sks_setup sks_setup;
+
+int sks_setup_open(int argc, const char *const *argv, sks_setup **out);
+int sks_setup_info(const sks_setup *su, sks_info_t *info);
+
+/* Per-point material: nx*nz rows of 16 doubles, the 5x5 block of the Voigt
+ * stiffness on the strains (11, 12, 13, 23, 33) stored upper-triangle row by
+ * row (C11 C16 C15 C14 C13 C66 C56 C46 C36 C55 C45 C35 C44 C34 C33), then
+ * rho: the entries the 2-D stress uses (Stress_ij, sem2d_psvsh.c:1345-1380). */
+int sks_setup_material(const sks_setup *su, double *out16);
+
+/* Lumped mass (nx*nz) and Stacey coefficients (3*nx*nz, zero off the
+ * absorbing edges) as Mass_Matrix / Absorb_Matrix build them
+ * (sem2d_psvsh.c:1042-1128). */
+int sks_setup_mass(const sks_setup *su, double *mass, double *ab3);
+
+/* Receiver offsets iz*nx+ix (ntrace values). */
+int sks_setup_receivers(const sks_setup *su, int64_t *off);
+
+/* Boundary-record schedule of the injecting steps: per step four record
+ * indices (-1: a ring slot never filled) and four FP64 weights for the P-SV
+ * and the SH family (interpl.c:16-91, ring shared as in
+ * sem2d_psvsh.c:430-431).  Arrays hold 4*nt_inject entries. */
+int sks_setup_schedule(const sks_setup *su, int32_t *tap_psv, double *w_psv,
+                       int32_t *tap_sh, double *w_sh);
+
+void sks_setup_close(sks_setup *su);
+
+/* Device solver from a set-up; the set-up is consumed (closed) on success
+ * and on failure. */
+int sks_open_setup(sks_setup *su, int precision, int device, sks_solver **out);
+
+/* Kernel launches issued by sks_run() so far (instrumentation). */
+int64_t sks_kernel_launches(const sks_solver *s);
+
+void sks_destroy(sks_solver *s);
+
+const char *sks_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SKS_H */

@@ -999,7 +999,7 @@ int oracle_material(void *hv, double *out16)
     size_t np = (size_t)h->o.nx * h->o.nz, g;
     for (g = 0; g < np; g++) {
         const Cmat *m = &h->o.mesh[g];
-        static const int vi[5][2] = {{0, 0}, {2, 2}, {1, 2}, {0, 2}, {0, 1}};
+        static const int vi[5][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 2}, {2, 2}};  /* Voigt 11 12 13 23 33 */
         int a, b, k = 0;
         for (a = 0; a < 5; a++)
             for (b = a; b < 5; b++)
@@ -1017,6 +1017,13 @@ int oracle_mass(void *hv, double *mass, double *ab3)
         ab3[3 * g] = (double)h->o.Ab[g].u[0]; ab3[3 * g + 1] = (double)h->o.Ab[g].u[1]; ab3[3 * g + 2] = (double)h->o.Ab[g].u[2];
     }
     return 0;
+}
+int oracle_receivers(void *hv, long long *off)
+{
+    OracleHandle *h = (OracleHandle *)hv;
+    int i;
+    for (i = 0; i < h->o.ntrace; i++) off[i] = h->o.rec_off[i];
+    return h->o.ntrace;
 }
 void oracle_destroy(void *hv)
 {

@@ -1,0 +1,77 @@
+/*
+ * sem2d_psvsh_gb300 — drop-in replacement of the reference program
+ * `sem2d_psvsh par=run.par` (semsyn/src/sem2d_psvsh.c:82-521) on one GB300.
+ *
+ * Same command line (getpar words), same input files, same outputs: with
+ * plot_trace=1 it writes seis.u, seis.w and seis.v in the working directory,
+ * nst records of ntrace float32 each (kirrecord_zhl, :2116-2160).  Two extra
+ * words choose the arithmetic and the device:
+ *   sks_precision=fp64|fp32c   (default fp64)
+ *   sks_device=N               (default 0)
+ * Invoked as `sem2d_gb300` (or with psv_only=1) it behaves as the P-SV solver
+ * semsyn/src/sem2d.c, which reads no SH boundary file.
+ * Errors print a message and exit with status 1 instead of the reference's
+ * exit(-1/-2/-3).
+ */
+#include "sks.h"
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+int main(int argc, char **argv)
+{
+    int precision = SKS_FP64, device = 0, i, rc, chunk = 1000, step = 0;
+    const char **args = (const char **)calloc((size_t)argc + 2, sizeof(char *));
+    int nargs = 0;
+    sks_solver *s = NULL;
+    sks_info_t info;
+    FILE *fu = NULL, *fw = NULL, *fv = NULL;
+    float *su, *sv, *sw;
+    const char *prog = strrchr(argv[0], '/');
+    prog = prog ? prog + 1 : argv[0];
+    args[nargs++] = argv[0];
+    for (i = 1; i < argc; i++) {
+        if (!strncmp(argv[i], "sks_precision=", 14)) {
+            precision = (!strcmp(argv[i] + 14, "fp32c") || !strcmp(argv[i] + 14, "1")) ? SKS_FP32C : SKS_FP64;
+            continue;
+        }
+        if (!strncmp(argv[i], "sks_device=", 11)) { device = atoi(argv[i] + 11); continue; }
+        args[nargs++] = argv[i];
+    }
+    if (!strncmp(prog, "sem2d_gb300", 11)) args[nargs++] = "psv_only=1";
+    rc = sks_open_par(nargs, args, precision, device, &s);
+    if (rc) { fprintf(stderr, "%s: %s\n", prog, sks_last_error()); return 1; }
+    sks_get_info(s, &info);
+    printf("%s: nx=%d nz=%d eh=%.6f h=%.6f nst=%d inject=%d ntrace=%d materials=%d %s %s\n", prog,
+           info.nx, info.nz, info.eh, info.h, info.nst, info.nt_inject, info.ntrace, info.nmat,
+           info.anisotropic ? "anisotropic" : "isotropic", precision == SKS_FP64 ? "fp64" : "fp32c");
+    rc = sks_load_boundary_files(s);
+    if (rc) { fprintf(stderr, "%s: %s\n", prog, sks_last_error()); sks_destroy(s); return 1; }
+    su = (float *)malloc(sizeof(float) * (size_t)chunk * (info.ntrace + 1));
+    sv = (float *)malloc(sizeof(float) * (size_t)chunk * (info.ntrace + 1));
+    sw = (float *)malloc(sizeof(float) * (size_t)chunk * (info.ntrace + 1));
+    if (info.ntrace > 0) {
+        fu = fopen("seis.u", "wb"); fw = fopen("seis.w", "wb"); fv = fopen("seis.v", "wb");
+        if (!fu || !fw || !fv) { fprintf(stderr, "%s: cannot open seis.* for writing\n", prog); return 1; }
+    }
+    while (step < info.nst) {
+        int n = sks_run(s, chunk, su, sv, sw);
+        if (n < 0) { fprintf(stderr, "%s: %s\n", prog, sks_last_error()); sks_destroy(s); return 1; }
+        if (n == 0) break;
+        if (info.ntrace > 0) {
+            int k;
+            for (k = 0; k < n; k++) {   /* per step: u, then w, then v (kirrecord_zhl order) */
+                fwrite(su + (size_t)k * info.ntrace, sizeof(float), info.ntrace, fu);
+                fwrite(sw + (size_t)k * info.ntrace, sizeof(float), info.ntrace, fw);
+                fwrite(sv + (size_t)k * info.ntrace, sizeof(float), info.ntrace, fv);
+            }
+        }
+        step += n;
+    }
+    if (fu) { fclose(fu); fclose(fw); fclose(fv); }
+    printf("%s: SEM calculation finished, %d steps\n", prog, step);
+    free(su); free(sv); free(sw); free(args);
+    sks_destroy(s);
+    return 0;
+}

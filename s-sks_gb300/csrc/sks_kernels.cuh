@@ -1,0 +1,495 @@
+// Device kernels of the SEM time step (sm_103a, CUDA cores).
+//
+// One time step of semsyn's solver (semsyn/src/sem2d_psvsh.c:418-513) is
+//   GRT_Interface4   u^n += incident-trace increment on the interface line
+//   Stiff_Matrix     K = sum over elements of the element internal force
+//   Time_diff_hybrid u^{n+1} = 2u^n - u^{n-1} - dt^2 M^-1 K
+//   Absorbs          centred Stacey form on the left/bottom/right edges
+//   kirrecord_zhl    sample the surface receivers.
+// Here the element force, the assembly and the update are one kernel.
+//
+// Warp tile.  A warp owns TEX=6 consecutive elements in x and a run of HZ
+// element rows in z.  Lane l = 5e + a (e = element 0..5, a = GLL column
+// 0..4) holds the 5 points of column a of its element for the current element
+// row in registers.  d/dz contractions run inside a lane (its own column),
+// d/dx and the x part of the divergence read the other 4 columns of the
+// element with warp shuffles.  The warp walks its element rows bottom-up;
+// the top row of one element row is the bottom row of the next, so its
+// displacement and its partial internal force are carried in registers.
+// Global assembly is gather-style and deterministic: a point's force is the
+// sum of its element contributions in a fixed order -- in-warp by shuffle
+// (left element first, lower element first, the reference's ex-outer/ez-inner
+// order), across warp tiles through a per-tile perimeter buffer that
+// k_seam sums in a fixed tile order.  No atomics, no global force array.
+//
+// Forms.  LF=false: FP64, the reference's 3-level update (two displacement
+// buffers; u^{n+1} overwrites u^{n-1}).  LF=true: FP32 leapfrog on
+// (u, d = u^n - u^{n-1}) with Kahan compensation of u += d; it is the same
+// recurrence as the 3-level form (d^{n+1} = d^n - dt^2 M^-1 K inside,
+// ((M-A) d^n - dt^2 K)/(M+A) on the Stacey edges, injection adds the
+// increment to both u and d).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sks {
+
+constexpr int N = 4;          // GLL degree compiled for
+constexpr int NP = N + 1;     // points per element edge
+constexpr int TEX = 6;        // elements per warp tile in x
+constexpr int TW = TEX * N;   // grid columns per warp tile
+constexpr int MAT_STRIDE = 16;
+
+template <typename T>
+struct Coef {
+    T D[NP * NP];    // D[j*NP+i]  = l'_i(xi_j) * 2/eh         (dlagP_JeI)
+    T DW[NP * NP];   // DW[j*NP+i] = l'_i(xi_j) * w_j          (dlagP_Gllw)
+    T w[NP];         // GLL weights
+    T Je, JeI;       // eh^2/4, 2/eh
+    T dt2_Je;        // sdt^2 / Je   (M^-1 dt^2 = dt2_Je / (rho Wx Wz))
+};
+
+template <typename T>
+struct Geo {
+    int nex, nez, nx, nz;
+    int ntx, ntz, HZ, ntiles;
+    int pstride;                  // perimeter entries per tile
+    int64_t np;                   // nx*nz
+};
+
+template <typename T>
+struct Field {
+    const T* __restrict__ uc;     // u^n, [3][np]
+    T* __restrict__ un;           // FP64: u^{n-1} in, u^{n+1} out; FP32: u^{n+1} out
+    T* __restrict__ dv;           // FP32 form: d = u^n - u^{n-1}, in place
+    T* __restrict__ cc;           // FP32 form: Kahan compensation of u, in place
+    const uint16_t* __restrict__ mid;   // material index per point
+    const T* __restrict__ mat;          // [nmat][16]: 15 stiffness entries, 1/rho
+    const T* __restrict__ wxi;          // 1 / (sum of GLL weights at column ix)
+    const T* __restrict__ wzi;          // 1 / (... at row iz)
+    const T* __restrict__ stc;          // Stacey coefficients [nbnd][3][3]: dt^2/(M+A), 2M/(M+A), (M-A)/(M+A)
+    T* __restrict__ perim;              // [ntiles][pstride][3] partial forces on tile perimeters
+};
+
+__device__ __forceinline__ int64_t stacey_index(int ix, int iz, int nx, int nz)
+{
+    if (ix == 0) return iz;
+    if (iz == 0) return (int64_t)nz + ix;
+    if (ix == nx - 1) return (int64_t)nz + nx + iz;
+    if (iz == nz - 1 && ix >= 1 && ix <= 3 * N) return 2 * (int64_t)nz + nx + ix;
+    return -1;
+}
+
+// material row -> registers
+template <typename T, bool ANISO>
+struct MatRow;
+
+template <>
+struct MatRow<double, true> {
+    double s[MAT_STRIDE];
+    __device__ __forceinline__ void load(const double* __restrict__ m) {
+        const double2* p = reinterpret_cast<const double2*>(m);
+#pragma unroll
+        for (int i = 0; i < 8; i++) { double2 v = __ldg(p + i); s[2 * i] = v.x; s[2 * i + 1] = v.y; }
+    }
+};
+template <>
+struct MatRow<float, true> {
+    float s[MAT_STRIDE];
+    __device__ __forceinline__ void load(const float* __restrict__ m) {
+        const float4* p = reinterpret_cast<const float4*>(m);
+#pragma unroll
+        for (int i = 0; i < 4; i++) { float4 v = __ldg(p + i); s[4 * i] = v.x; s[4 * i + 1] = v.y; s[4 * i + 2] = v.z; s[4 * i + 3] = v.w; }
+    }
+};
+template <typename T>
+struct MatRow<T, false> {
+    T s[MAT_STRIDE];   // only s[0] (C11=C33), s[4] (C13), s[5] (C66=C55=C44), s[15] used
+    __device__ __forceinline__ void load(const T* __restrict__ m) {
+        s[0] = __ldg(m); s[4] = __ldg(m + 4); s[5] = __ldg(m + 5); s[15] = __ldg(m + 15);
+    }
+};
+
+// stress on the strain list (e11, e12=u_y,x, e13=u_z,x+u_x,z, e23=u_y,z, e33):
+// sigma_a = sum_b C[a][b] e_b in b order, as Stress_ij (sem2d_psvsh.c:1345-1380)
+template <typename T, bool ANISO>
+__device__ __forceinline__ void stress(const MatRow<T, ANISO>& M, const T e[5], T s[5])
+{
+    if (ANISO) {
+        const T* c = M.s;   // upper triangle: 0..4 row0, 5..8 row1, 9..11 row2, 12..13 row3, 14 row4
+        s[0] = c[0] * e[0];  s[0] = fma(c[1], e[1], s[0]);  s[0] = fma(c[2], e[2], s[0]);  s[0] = fma(c[3], e[3], s[0]);  s[0] = fma(c[4], e[4], s[0]);
+        s[1] = c[1] * e[0];  s[1] = fma(c[5], e[1], s[1]);  s[1] = fma(c[6], e[2], s[1]);  s[1] = fma(c[7], e[3], s[1]);  s[1] = fma(c[8], e[4], s[1]);
+        s[2] = c[2] * e[0];  s[2] = fma(c[6], e[1], s[2]);  s[2] = fma(c[9], e[2], s[2]);  s[2] = fma(c[10], e[3], s[2]); s[2] = fma(c[11], e[4], s[2]);
+        s[3] = c[3] * e[0];  s[3] = fma(c[7], e[1], s[3]);  s[3] = fma(c[10], e[2], s[3]); s[3] = fma(c[12], e[3], s[3]); s[3] = fma(c[13], e[4], s[3]);
+        s[4] = c[4] * e[0];  s[4] = fma(c[8], e[1], s[4]);  s[4] = fma(c[11], e[2], s[4]); s[4] = fma(c[13], e[3], s[4]); s[4] = fma(c[14], e[4], s[4]);
+    } else {
+        const T l2m = M.s[0], lam = M.s[4], mu = M.s[5];
+        s[0] = fma(lam, e[4], l2m * e[0]);
+        s[1] = mu * e[1];
+        s[2] = mu * e[2];
+        s[3] = mu * e[3];
+        s[4] = fma(l2m, e[4], lam * e[0]);
+    }
+}
+
+// one owned point: FP64 3-level or FP32 compensated leapfrog update
+template <typename T, bool LF>
+__device__ __forceinline__ void update_point(const Field<T>& F, const Geo<T>& G, const Coef<T>& k,
+                                             int ix, int iz, const T u[3], const T K[3], T rinv)
+{
+    const int64_t g = (int64_t)iz * G.nx + ix;
+    const int64_t bi = stacey_index(ix, iz, G.nx, G.nz);
+    if (!LF) {
+        T u0[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) u0[c] = F.un[c * G.np + g];
+        if (bi < 0) {
+            const T mdt2 = k.dt2_Je * rinv * F.wxi[ix] * F.wzi[iz];
+#pragma unroll
+            for (int c = 0; c < 3; c++) F.un[c * G.np + g] = (-mdt2 * K[c] + (T)2 * u[c]) - u0[c];
+        } else {
+            const T* p = F.stc + bi * 9;
+#pragma unroll
+            for (int c = 0; c < 3; c++) F.un[c * G.np + g] = (-p[3 * c] * K[c] + p[3 * c + 1] * u[c]) - p[3 * c + 2] * u0[c];
+        }
+    } else {
+        T d[3], cm[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) { d[c] = F.dv[c * G.np + g]; cm[c] = F.cc[c * G.np + g]; }
+        T dn[3];
+        if (bi < 0) {
+            const T mdt2 = k.dt2_Je * rinv * F.wxi[ix] * F.wzi[iz];
+#pragma unroll
+            for (int c = 0; c < 3; c++) dn[c] = fma(-mdt2, K[c], d[c]);
+        } else {
+            const T* p = F.stc + bi * 9;
+#pragma unroll
+            for (int c = 0; c < 3; c++) dn[c] = p[3 * c + 2] * d[c] - p[3 * c] * K[c];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const T y = dn[c] - cm[c];
+            const T t = u[c] + y;
+            const T cn = (t - u[c]) - y;
+            F.un[c * G.np + g] = t;
+            F.dv[c * G.np + g] = dn[c];
+            F.cc[c * G.np + g] = cn;
+        }
+    }
+}
+
+__device__ __forceinline__ int perim_pos(int col, int row, int W_eff, int R, int R_eff)
+{
+    // left column, right column, bottom row (interior cols), top row (interior cols)
+    if (col == 0) return row;
+    if (col == W_eff) return (R + 1) + row;
+    if (row == 0) return 2 * (R + 1) + (col - 1);
+    (void)R_eff;
+    return 2 * (R + 1) + (TW - 1) + (col - 1);
+}
+
+template <typename T, bool ANISO, bool LF>
+__global__ void __launch_bounds__(128) k_main(Field<T> F, Geo<T> G, Coef<T> k)
+{
+    const int lane = threadIdx.x & 31;
+    const int tile = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (tile >= G.ntiles) return;                 // warp-uniform
+    const unsigned FULL = 0xffffffffu;
+    const int tx = tile % G.ntx, tz = tile / G.ntx;
+    const int e = lane / NP, al = lane - e * NP;  // lanes 30,31: e = 6
+    const int ex = tx * TEX + e;
+    const int nel = min(TEX, G.nex - tx * TEX);   // elements in this tile
+    const bool live = e < nel;
+    const int ix = ex * N + al;
+    const int ez0 = tz * G.HZ, ez1 = min(ez0 + G.HZ, G.nez);
+    const int base = e * NP;
+    const int R = G.HZ * N, R_eff = (ez1 - ez0) * N, W_eff = nel * N;
+
+    // x ownership: columns 0..N-1 of each element, column N of the last one
+    const bool own_x = live && (al < N || e == nel - 1);
+    const bool seam_v = own_x && ((al == 0 && e == 0 && ex > 0) || (al == N && ix < G.nx - 1));
+
+    T Dx[NP], DWc[NP];
+#pragma unroll
+    for (int t = 0; t < NP; t++) { Dx[t] = k.D[al * NP + t]; DWc[t] = k.DW[t * NP + al]; }
+    const T wal = k.w[al];
+
+    T u[NP][3];
+    uint16_t m[NP];
+    T kc[3] = {0, 0, 0};
+
+#pragma unroll
+    for (int b = 0; b < NP; b++) {
+        const int64_t g = (int64_t)(ez0 * N + b) * G.nx + ix;
+#pragma unroll
+        for (int c = 0; c < 3; c++) u[b][c] = live ? F.uc[c * G.np + g] : (T)0;
+        m[b] = live ? F.mid[g] : (uint16_t)0;
+    }
+
+    for (int ez = ez0; ez < ez1; ++ez) {
+        if (ez > ez0) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) u[0][c] = u[N][c];
+            m[0] = m[N];
+#pragma unroll
+            for (int b = 1; b < NP; b++) {
+                const int64_t g = (int64_t)(ez * N + b) * G.nx + ix;
+#pragma unroll
+                for (int c = 0; c < 3; c++) u[b][c] = live ? F.uc[c * G.np + g] : (T)0;
+                m[b] = live ? F.mid[g] : (uint16_t)0;
+            }
+        }
+        T item0[NP][3], F2[NP][3];
+        T rinv[NP];
+#pragma unroll
+        for (int b = 0; b < NP; b++) {
+            T dx[3], dz[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                T s = 0;
+#pragma unroll
+                for (int t = 0; t < NP; t++) s = fma(__shfl_sync(FULL, u[b][c], base + t), Dx[t], s);
+                dx[c] = s;
+                T z = 0;
+#pragma unroll
+                for (int t = 0; t < NP; t++) z = fma(u[t][c], k.D[b * NP + t], z);
+                dz[c] = z;
+            }
+            const T ee[5] = {dx[0], dx[1], dx[2] + dz[0], dz[1], dz[2]};
+            MatRow<T, ANISO> M;
+            M.load(F.mat + (size_t)m[b] * MAT_STRIDE);
+            rinv[b] = M.s[15];
+            T sg[5];
+            stress<T, ANISO>(M, ee, sg);
+            const T f0[3] = {sg[0] * k.JeI, sg[1] * k.JeI, sg[2] * k.JeI};
+            F2[b][0] = sg[2] * k.JeI; F2[b][1] = sg[3] * k.JeI; F2[b][2] = sg[4] * k.JeI;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                T s = 0;
+#pragma unroll
+                for (int a = 0; a < NP; a++) s = fma(__shfl_sync(FULL, f0[c], base + a), DWc[a], s);
+                item0[b][c] = s;
+            }
+        }
+        T kk[NP][3];
+#pragma unroll
+        for (int b = 0; b < NP; b++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                T s = 0;
+#pragma unroll
+                for (int bb = 0; bb < NP; bb++) s = fma(F2[bb][c], k.DW[bb * NP + b], s);
+                kk[b][c] = (item0[b][c] * k.w[b] + s * wal) * k.Je;
+            }
+        if (ez > ez0) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) kk[0][c] = kc[c] + kk[0][c];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) kc[c] = kk[N][c];
+
+#pragma unroll
+        for (int b = 0; b < N; b++) {
+            T kt[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const T left = __shfl_up_sync(FULL, kk[b][c], 1);
+                kt[c] = (al == 0 && e > 0) ? left + kk[b][c] : kk[b][c];
+            }
+            if (own_x) {
+                const int iz = ez * N + b;
+                const bool seam_h = (b == 0 && ez == ez0 && ez0 > 0);
+                if (seam_v || seam_h) {
+                    const int pos = perim_pos(ix - tx * TW, iz - tz * R, W_eff, R, R_eff);
+                    T* p = F.perim + ((int64_t)tile * G.pstride + pos) * 3;
+                    p[0] = kt[0]; p[1] = kt[1]; p[2] = kt[2];
+                } else {
+                    update_point<T, LF>(F, G, k, ix, iz, u[b], kt, rinv[b]);
+                }
+            }
+        }
+        if (ez == ez1 - 1) {
+            // top row of the tile: the domain's top row, or a seam with the tile above
+            T kt[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const T left = __shfl_up_sync(FULL, kc[c], 1);
+                kt[c] = (al == 0 && e > 0) ? left + kc[c] : kc[c];
+            }
+            if (own_x) {
+                const int iz = ez1 * N;
+                if (ez1 < G.nez || seam_v) {
+                    const int pos = perim_pos(ix - tx * TW, iz - tz * R, W_eff, R, R_eff);
+                    T* p = F.perim + ((int64_t)tile * G.pstride + pos) * 3;
+                    p[0] = kt[0]; p[1] = kt[1]; p[2] = kt[2];
+                } else {
+                    update_point<T, LF>(F, G, k, ix, iz, u[N], kt, rinv[N]);
+                }
+            }
+        }
+    }
+}
+
+// points shared by warp tiles: sum the perimeter partials in a fixed order, then update
+struct SeamPt { int32_t ix, iz; int32_t ref[4]; };
+
+template <typename T, bool LF>
+__global__ void __launch_bounds__(256) k_seam(Field<T> F, Geo<T> G, Coef<T> k, const SeamPt* __restrict__ pts, int npts)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npts) return;
+    const SeamPt s = pts[i];
+    T K[3] = {0, 0, 0};
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        if (s.ref[r] < 0) break;
+        const T* p = F.perim + (int64_t)s.ref[r] * 3;
+        K[0] += p[0]; K[1] += p[1]; K[2] += p[2];
+    }
+    const int64_t g = (int64_t)s.iz * G.nx + s.ix;
+    T u[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) u[c] = F.uc[c * G.np + g];
+    const T rinv = __ldg(F.mat + (size_t)F.mid[g] * MAT_STRIDE + 15);
+    update_point<T, LF>(F, G, k, s.ix, s.iz, u, K, rinv);
+}
+
+// Boundary-trace interpolation for a chunk of steps (interpl.c:16-54): row r of
+// Gout (r = 1..S) is step s0+r-1; four taps of FP32 records with FP64 weights,
+// then the |g| >= 10 guard of sem2d_psvsh.c:432-444 (sequential, ends read 0).
+__global__ void __launch_bounds__(256) k_interp(double* __restrict__ Gout, int L, int s0, int nsteps,
+                                                const float* __restrict__ rpsv, int mtotal,
+                                                const float* __restrict__ rsh, int shtotal,
+                                                const int32_t* __restrict__ tap_psv, const double* __restrict__ w_psv,
+                                                const int32_t* __restrict__ tap_sh, const double* __restrict__ w_sh)
+{
+    const int r = blockIdx.x;
+    if (r >= nsteps) return;
+    const int it = s0 + r;
+    double* out = Gout + (int64_t)(r + 1) * L;
+    __shared__ int bad[2];
+    if (threadIdx.x < 2) bad[threadIdx.x] = 0;
+    __syncthreads();
+    for (int fam = 0; fam < 2; fam++) {
+        const int n = fam ? shtotal : mtotal;
+        const float* rec = fam ? rsh : rpsv;
+        const int32_t* tp = (fam ? tap_sh : tap_psv) + 4 * it;
+        const double* wp = (fam ? w_sh : w_psv) + 4 * it;
+        double* o = out + (fam ? mtotal : 0);
+        int t[4]; double w[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) { t[j] = tp[j]; w[j] = wp[j]; }
+        int anybad = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if (t[j] >= 0) s = fma(w[j], (double)rec[(int64_t)t[j] * n + i], s);
+            o[i] = s;
+            if (!(s < 10.0 && s > -10.0)) anybad = 1;
+        }
+        if (anybad) bad[fam] = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int fam = 0; fam < 2; fam++) {
+            if (!bad[fam]) continue;
+            const int n = fam ? shtotal : mtotal;
+            double* o = out + (fam ? mtotal : 0);
+            for (int i = 0; i < n; i++)
+                if (!(o[i] < 10.0 && o[i] > -10.0)) {
+                    const double l = i > 0 ? o[i - 1] : 0.0, rr = i + 1 < n ? o[i + 1] : 0.0;
+                    o[i] = (l + rr) / 2;
+                }
+        }
+    }
+}
+
+// GRT_Interface4 (sem2d_psvsh.c:2076-2111): u^n += g(it) - g(it-1) on row nbl
+// (ix >= nbl) and column nbl (iz > nbl); the vertical component changes sign.
+template <typename T, bool LF>
+__global__ void __launch_bounds__(256) k_inject(T* __restrict__ u, T* __restrict__ dv, T* __restrict__ cc, int64_t np,
+                                                int nx, int nz, int nbl, const double* __restrict__ Gcur,
+                                                const double* __restrict__ Gprev, int mtotal)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nrow = nx - nbl, ncol = nz - nbl - 1;
+    if (i >= nrow + ncol) return;
+    const double *V = Gcur + mtotal, *V0 = Gprev + mtotal;
+    int64_t g;
+    double du, dvv, dw;
+    if (i < nrow) {
+        const int ix = nbl + i;
+        g = (int64_t)nbl * nx + ix;
+        du = -Gprev[ix] + Gcur[ix];
+        dvv = -V0[ix] + V[ix];
+        dw = Gprev[nx + ix] - Gcur[nx + ix];
+    } else {
+        const int iz = nbl + 1 + (i - nrow);
+        g = (int64_t)iz * nx + nbl;
+        du = -Gprev[2 * nx + iz] + Gcur[2 * nx + iz];
+        dvv = -V0[nx + iz] + V[nx + iz];
+        dw = Gprev[2 * nx + nz + iz] - Gcur[2 * nx + nz + iz];
+    }
+    const double dd[3] = {du, dvv, dw};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        if (!LF) {
+            u[c * np + g] += (T)dd[c];
+        } else {
+            const T add = (T)dd[c];
+            const T uu = u[c * np + g], cm = cc[c * np + g];
+            const T y = add - cm;
+            const T t = uu + y;
+            cc[c * np + g] = (t - uu) - y;
+            u[c * np + g] = t;
+            dv[c * np + g] += add;
+        }
+    }
+}
+
+// GRT_Interface (sem2d_psvsh.c:1953-2005) at step 0: set the line to g(0);
+// the column pass wins at the corner (nbl, nbl).  u^{-1} = 0, so d = u.
+template <typename T, bool LF>
+__global__ void __launch_bounds__(256) k_init_line(T* __restrict__ u, T* __restrict__ dv, int64_t np,
+                                                   int nx, int nz, int nbl, const double* __restrict__ G0, int mtotal)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nrow = nx - nbl - 1, ncol = nz - nbl;
+    if (i >= nrow + ncol) return;
+    const double* V = G0 + mtotal;
+    int64_t g;
+    double v3[3];
+    if (i < nrow) {
+        const int ix = nbl + 1 + i;
+        g = (int64_t)nbl * nx + ix;
+        v3[0] = G0[ix]; v3[1] = V[ix]; v3[2] = -G0[nx + ix];
+    } else {
+        const int iz = nbl + (i - nrow);
+        g = (int64_t)iz * nx + nbl;
+        v3[0] = G0[2 * nx + iz]; v3[1] = V[nx + iz]; v3[2] = -G0[2 * nx + nz + iz];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        u[c * np + g] = (T)v3[c];
+        if (LF) dv[c * np + g] = (T)v3[c];
+    }
+}
+
+// kirrecord_zhl (sem2d_psvsh.c:2116-2160): u_x, u_y, -u_z at the receivers;
+// offset np addresses the reference's never-written extra point (reads 0)
+template <typename T>
+__global__ void __launch_bounds__(128) k_record(const T* __restrict__ u, int64_t np, const int64_t* __restrict__ off,
+                                                int ntrace, float* __restrict__ out)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= ntrace) return;
+    const int64_t g = off[r];
+    float vx = 0.f, vy = 0.f, vz = 0.f;
+    if (g < np) { vx = (float)u[g]; vy = (float)u[np + g]; vz = (float)(-u[2 * np + g]); }
+    out[r] = vx;
+    out[ntrace + r] = vy;
+    out[2 * ntrace + r] = vz;
+}
+
+}  // namespace sks

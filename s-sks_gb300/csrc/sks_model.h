@@ -1,0 +1,87 @@
+/*
+ * Host-side model of one SEM solve: everything the reference's main()
+ * computes before its time loop (semsyn/src/sem2d_psvsh.c:82-416), in FP64,
+ * laid out for the device.  Internal to the library.
+ */
+#ifndef SKS_MODEL_H
+#define SKS_MODEL_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SKS_MAX_N 6
+#define SKS_MAT_STRIDE 16   /* 15 stiffness entries + rho per material */
+
+typedef struct {
+    /* par words (sem2d_psvsh.c:154-205) */
+    int flat, nt, nex, nst, nfil, hpn, absorb, readpars, neh, atten, xtrace;
+    int get_rec, plot_trace, idxplot, msource, semmodel_full, psv_only;
+    double dp, eh_par, sdt, xbeg, zbeg;
+    float dp_f, eh_par_f, sdt_f, xbeg_f, zbeg_f;
+    char greenfile[512], shgreenfile[512], raymodel[512], semmodel[512], rec_file[512];
+
+    /* mesh (discret, sem2d_psvsh.c:534-606) */
+    int nez, nx, nz;
+    double eh, h;            /* FP64 element size / GLL spacing          */
+    float eh_f, h_f;         /* the reference's float values (decisions) */
+
+    /* materials: table of distinct materials + per-point index.
+     * Row layout (16 doubles): the symmetric 5x5 block of the Voigt
+     * stiffness on the strain list (e11, e12, e13, e23, e33) stored upper
+     * triangle row by row: C11 C16 C15 C14 C13 | C66 C56 C46 C36 | C55 C45
+     * C35 | C44 C34 | C33, then rho.  These are the only entries the 2-D
+     * stress (d/dy = 0) touches (Stress_ij, sem2d_psvsh.c:1345-1380). */
+    int nmat, mat_cap;
+    double *mat;
+    uint16_t *mat_id;        /* nx*nz, row-major, iz = 0 at the bottom   */
+    int anisotropic;
+
+    /* GLL tables (lagrange.c) and uniform Jacobian (sem2d_psvsh.c:279-300) */
+    double gllp[SKS_MAX_N + 1], gllw[SKS_MAX_N + 1];
+    double dlagP[(SKS_MAX_N + 1) * (SKS_MAX_N + 1)];  /* [j*(N+1)+i] = l'_i(xi_j) */
+    double Je, JeI, Jb;
+
+    /* lumped mass and Stacey matrix, per point, reference summation order */
+    double *mass;            /* nx*nz */
+    double *ab;              /* 3*nx*nz, zero off the absorbing edges */
+
+    /* receivers: flat offsets iz*nx+ix (nx*nz addresses a point that
+     * stays zero, as the reference's extra array element does) */
+    int ntrace;
+    int64_t *rec_off;
+
+    /* boundary-trace schedule (interpl.c:16-91 with the shared ring of
+     * sem2d_psvsh.c:430-431): for steps [0, nt_sem) four taps per family,
+     * a record index (-1: a slot never filled, reads 0) and an FP64 weight */
+    int nt_sem, mtotal, shtotal;
+    int nrec_psv, nrec_sh;
+    int32_t *tap_psv, *tap_sh;
+    double *w_psv, *w_sh;
+} sks_model;
+
+/* status codes match include/sks.h; internal to the library */
+__attribute__((visibility("hidden")))
+int  sks_model_from_par(sks_model *m, int argc, const char *const *argv, char *err, size_t errlen);
+__attribute__((visibility("hidden")))
+void sks_model_free(sks_model *m);
+
+/* Stacey boundary-point index (-1 off the absorbing edges): left column,
+ * bottom row, right column, then top-row points 1..3N (sem2d_psvsh.c:1834-1892) */
+static inline int64_t sks_stacey_index(int ix, int iz, int nx, int nz, int N)
+{
+    if (ix == 0) return iz;
+    if (iz == 0) return (int64_t)nz + ix;
+    if (ix == nx - 1) return (int64_t)nz + nx + iz;
+    if (iz == nz - 1 && ix >= 1 && ix <= 3 * N) return 2 * (int64_t)nz + nx + ix;
+    return -1;
+}
+static inline int64_t sks_stacey_count(int nx, int nz, int N) { return 2 * (int64_t)nz + nx + 3 * N + 1; }
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,654 @@
+// C ABI of the GB300 SEM time-stepping library (include/sks.h): device state,
+// step scheduling, and the entry points that replace main() and the time loop
+// of semsyn/src/sem2d_psvsh.c.
+#include "sks.h"
+#include "sks_model.h"
+#include "sks_kernels.cuh"
+
+#include <cuda_runtime.h>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+
+using namespace sks;
+
+static thread_local char g_err[1024];
+
+static int set_err(int code, const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return set_err(SKS_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                           __FILE__, __LINE__);                                               \
+    } while (0)
+
+extern "C" const char* sks_last_error(void) { return g_err; }
+
+struct sks_solver {
+    sks_model m;
+    int precision, device;
+    int step;                  // next step to take
+    int64_t launches;
+    cudaStream_t stream;
+    // geometry
+    int ntx, ntz, HZ, ntiles, pstride;
+    int nseam;
+    int nbl;
+    // device buffers
+    void* U[2];                // displacement buffers, [3][np] each
+    void* Dv;                  // FP32 form: increment d
+    void* Cc;                  // FP32 form: Kahan compensation
+    uint16_t* mid;
+    void* mat;                 // [nmat][16] in the form's type
+    void* wxi;
+    void* wzi;
+    void* stc;                 // Stacey coefficients
+    void* perim;
+    SeamPt* seams;
+    int64_t* rec_off;
+    float* seis;               // [chunk][3][ntrace]
+    double* G;                 // [(chunk+1)][mtotal+shtotal]
+    float* rec_psv;            // boundary records
+    float* rec_sh;
+    int32_t* tap_psv;
+    int32_t* tap_sh;
+    double* w_psv;
+    double* w_sh;
+    int nrec_psv_loaded, nrec_sh_loaded;
+    int cur;                   // index of the buffer holding u^n
+    int g_last;                // row of G holding the last interpolated step
+    int chunk;
+    int64_t device_bytes;
+    bool boundary_ready;
+};
+
+struct sks_setup {
+    sks_model m;
+};
+
+static void fill_info(const sks_model& m, sks_info_t* info)
+{
+    memset(info, 0, sizeof *info);
+    info->nex = m.nex; info->nez = m.nez; info->hpn = m.hpn;
+    info->nx = m.nx; info->nz = m.nz; info->nst = m.nst; info->nt_inject = m.nt_sem;
+    info->ntrace = m.ntrace; info->mtotal = m.mtotal; info->shtotal = m.shtotal;
+    info->nrec_psv = m.nrec_psv; info->nrec_sh = m.nrec_sh; info->nmat = m.nmat;
+    info->anisotropic = m.anisotropic;
+    info->eh = m.eh; info->h = m.h; info->sdt = m.sdt;
+}
+
+extern "C" int sks_setup_open(int argc, const char* const* argv, sks_setup** out)
+{
+    if (!out) return set_err(SKS_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    sks_setup* su = new (std::nothrow) sks_setup();
+    if (!su) return set_err(SKS_ERR_NOMEM, "cannot allocate the set-up");
+    char err[512] = {0};
+    int rc = sks_model_from_par(&su->m, argc, argv, err, sizeof err);
+    if (rc) { delete su; return set_err(rc, "%s", err); }
+    *out = su;
+    return SKS_OK;
+}
+
+extern "C" int sks_setup_info(const sks_setup* su, sks_info_t* info)
+{
+    if (!su || !info) return set_err(SKS_ERR_ARG, "NULL argument");
+    fill_info(su->m, info);
+    return SKS_OK;
+}
+
+extern "C" int sks_setup_material(const sks_setup* su, double* out16)
+{
+    if (!su || !out16) return set_err(SKS_ERR_ARG, "NULL argument");
+    const sks_model& m = su->m;
+    const size_t np = (size_t)m.nx * m.nz;
+    for (size_t g = 0; g < np; g++)
+        memcpy(out16 + g * 16, m.mat + (size_t)m.mat_id[g] * SKS_MAT_STRIDE, 16 * sizeof(double));
+    return SKS_OK;
+}
+
+extern "C" int sks_setup_mass(const sks_setup* su, double* mass, double* ab3)
+{
+    if (!su) return set_err(SKS_ERR_ARG, "NULL argument");
+    const sks_model& m = su->m;
+    const size_t np = (size_t)m.nx * m.nz;
+    if (mass) memcpy(mass, m.mass, np * sizeof(double));
+    if (ab3) memcpy(ab3, m.ab, 3 * np * sizeof(double));
+    return SKS_OK;
+}
+
+extern "C" int sks_setup_receivers(const sks_setup* su, int64_t* off)
+{
+    if (!su || (!off && su->m.ntrace > 0)) return set_err(SKS_ERR_ARG, "NULL argument");
+    if (su->m.ntrace > 0) memcpy(off, su->m.rec_off, sizeof(int64_t) * su->m.ntrace);
+    return SKS_OK;
+}
+
+extern "C" int sks_setup_schedule(const sks_setup* su, int32_t* tap_psv, double* w_psv, int32_t* tap_sh, double* w_sh)
+{
+    if (!su) return set_err(SKS_ERR_ARG, "NULL argument");
+    const sks_model& m = su->m;
+    const size_t n = 4 * (size_t)m.nt_sem;
+    if (n == 0) return SKS_OK;
+    if (tap_psv) memcpy(tap_psv, m.tap_psv, n * sizeof(int32_t));
+    if (w_psv) memcpy(w_psv, m.w_psv, n * sizeof(double));
+    if (tap_sh) memcpy(tap_sh, m.tap_sh, n * sizeof(int32_t));
+    if (w_sh) memcpy(w_sh, m.w_sh, n * sizeof(double));
+    return SKS_OK;
+}
+
+extern "C" void sks_setup_close(sks_setup* su)
+{
+    if (!su) return;
+    sks_model_free(&su->m);
+    delete su;
+}
+
+namespace {
+
+template <typename T>
+int dmalloc(sks_solver* s, T** p, size_t n)
+{
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) return set_err(SKS_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e));
+    s->device_bytes += (int64_t)(n * sizeof(T));
+    return SKS_OK;
+}
+
+void free_device(sks_solver* s)
+{
+    void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->wxi, s->wzi, s->stc, s->perim,
+                  s->seams, s->rec_off, s->seis, s->G, s->rec_psv, s->rec_sh, s->tap_psv, s->tap_sh,
+                  s->w_psv, s->w_sh};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->wxi = s->wzi = s->stc = s->perim = nullptr;
+    s->mid = nullptr; s->seams = nullptr; s->rec_off = nullptr; s->seis = nullptr; s->G = nullptr;
+    s->rec_psv = s->rec_sh = nullptr; s->tap_psv = s->tap_sh = nullptr; s->w_psv = s->w_sh = nullptr;
+}
+
+int pick_hz(const sks_model& m, int sm_count)
+{
+    // enough warp tiles to give every SM >= 16 warps, and runs as long as possible
+    const int ntx = (m.nex + TEX - 1) / TEX;
+    const int target = sm_count * 16;
+    const int cands[] = {32, 24, 16, 12, 10, 8, 6, 5, 4, 3, 2, 1};
+    for (int hz : cands) {
+        const int ntz = (m.nez + hz - 1) / hz;
+        if ((int64_t)ntx * ntz >= target) return std::min(hz, m.nez);
+    }
+    return 1;
+}
+
+// perimeter position of local (col,row) in a tile, same rule as perim_pos()
+int host_perim_pos(int col, int row, int W_eff, int R)
+{
+    if (col == 0) return row;
+    if (col == W_eff) return (R + 1) + row;
+    if (row == 0) return 2 * (R + 1) + (col - 1);
+    return 2 * (R + 1) + (TW - 1) + (col - 1);
+}
+
+void build_seams(const sks_solver* s, std::vector<SeamPt>& out)
+{
+    const sks_model& m = s->m;
+    const int R = s->HZ * N;
+    out.clear();
+    auto tile_W = [&](int tx) { return std::min(TEX, m.nex - tx * TEX) * N; };
+    for (int iz = 0; iz < m.nz; iz++) {
+        const bool hs = (iz % R == 0) && iz > 0 && iz < m.nz - 1;
+        for (int ix = 0; ix < m.nx; ix++) {
+            const bool vs = (ix % TW == 0) && ix > 0 && ix < m.nx - 1;
+            if (!vs && !hs) continue;
+            SeamPt p;
+            p.ix = ix; p.iz = iz;
+            int nref = 0;
+            // tiles containing the point, in order (tx-1,tz-1) (tx-1,tz) (tx,tz-1) (tx,tz)
+            int txs[2], ntxs = 0, tzs[2], ntzs = 0;
+            if (vs) { txs[ntxs++] = ix / TW - 1; txs[ntxs++] = ix / TW; }
+            else { int tx = ix / TW; if (tx >= s->ntx) tx = s->ntx - 1; txs[ntxs++] = tx; }
+            if (hs) { tzs[ntzs++] = iz / R - 1; tzs[ntzs++] = iz / R; }
+            else { int tz = iz / R; if (tz >= s->ntz) tz = s->ntz - 1; tzs[ntzs++] = tz; }
+            for (int a = 0; a < ntxs; a++)
+                for (int b = 0; b < ntzs; b++) {
+                    const int tx = txs[a], tz = tzs[b];
+                    const int tile = tz * s->ntx + tx;
+                    const int col = ix - tx * TW, row = iz - tz * R;
+                    p.ref[nref++] = tile * s->pstride + host_perim_pos(col, row, tile_W(tx), R);
+                }
+            for (int r = nref; r < 4; r++) p.ref[r] = -1;
+            out.push_back(p);
+        }
+    }
+}
+
+template <typename T>
+int upload_tables(sks_solver* s)
+{
+    const sks_model& m = s->m;
+    const int N1 = m.hpn + 1;
+    // material table: 15 stiffness entries + 1/rho
+    std::vector<T> mat((size_t)m.nmat * MAT_STRIDE);
+    for (int i = 0; i < m.nmat; i++) {
+        for (int k = 0; k < 15; k++) mat[(size_t)i * MAT_STRIDE + k] = (T)m.mat[(size_t)i * SKS_MAT_STRIDE + k];
+        mat[(size_t)i * MAT_STRIDE + 15] = (T)(1.0 / m.mat[(size_t)i * SKS_MAT_STRIDE + 15]);
+    }
+    // column / row sums of GLL weights over the elements holding a point
+    std::vector<T> wxi(m.nx), wzi(m.nz);
+    for (int pass = 0; pass < 2; pass++) {
+        const int n = pass ? m.nz : m.nx, ne = pass ? m.nez : m.nex;
+        for (int i = 0; i < n; i++) {
+            double w = 0;
+            const int a = i % m.hpn;
+            if (a != 0) w = m.gllw[a];
+            else {
+                if (i / m.hpn < ne) w += m.gllw[0];          // element to the right/above
+                if (i > 0) w += m.gllw[m.hpn];              // element to the left/below
+            }
+            (pass ? wzi : wxi)[i] = (T)(1.0 / w);
+        }
+    }
+    // Stacey coefficients per boundary point and component
+    const int64_t nb = sks_stacey_count(m.nx, m.nz, m.hpn);
+    std::vector<T> stc((size_t)nb * 9, (T)0);
+    const double dt2 = m.sdt * m.sdt;
+    for (int iz = 0; iz < m.nz; iz++)
+        for (int ix = 0; ix < m.nx; ix++) {
+            const int64_t bi = sks_stacey_index(ix, iz, m.nx, m.nz, m.hpn);
+            if (bi < 0) continue;
+            const size_t g = (size_t)iz * m.nx + ix;
+            const double M = m.mass[g];
+            for (int c = 0; c < 3; c++) {
+                const double A = m.ab[3 * g + c];
+                stc[(size_t)bi * 9 + 3 * c + 0] = (T)(dt2 / (M + A));
+                stc[(size_t)bi * 9 + 3 * c + 1] = (T)(2.0 * M / (M + A));
+                stc[(size_t)bi * 9 + 3 * c + 2] = (T)((M - A) / (M + A));
+            }
+        }
+    (void)N1;
+    T *dmat, *dwx, *dwz, *dstc;
+    int rc;
+    if ((rc = dmalloc(s, &dmat, mat.size()))) return rc;
+    s->mat = dmat;
+    if ((rc = dmalloc(s, &dwx, wxi.size()))) return rc;
+    s->wxi = dwx;
+    if ((rc = dmalloc(s, &dwz, wzi.size()))) return rc;
+    s->wzi = dwz;
+    if ((rc = dmalloc(s, &dstc, stc.size()))) return rc;
+    s->stc = dstc;
+    CK(cudaMemcpy(dmat, mat.data(), mat.size() * sizeof(T), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dwx, wxi.data(), wxi.size() * sizeof(T), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dwz, wzi.data(), wzi.size() * sizeof(T), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dstc, stc.data(), stc.size() * sizeof(T), cudaMemcpyHostToDevice));
+    // wavefield
+    const size_t np = (size_t)m.nx * m.nz;
+    T* u0; T* u1;
+    if ((rc = dmalloc(s, &u0, 3 * np))) return rc;
+    s->U[0] = u0;
+    if ((rc = dmalloc(s, &u1, 3 * np))) return rc;
+    s->U[1] = u1;
+    if (s->precision == SKS_FP32C) {
+        T *dv, *cc;
+        if ((rc = dmalloc(s, &dv, 3 * np))) return rc;
+        s->Dv = dv;
+        if ((rc = dmalloc(s, &cc, 3 * np))) return rc;
+        s->Cc = cc;
+    }
+    T* pr;
+    if ((rc = dmalloc(s, &pr, (size_t)s->ntiles * s->pstride * 3))) return rc;
+    s->perim = pr;
+    return SKS_OK;
+}
+
+template <typename T>
+Coef<T> make_coef(const sks_model& m)
+{
+    Coef<T> k;
+    for (int j = 0; j < NP; j++)
+        for (int i = 0; i < NP; i++) {
+            k.D[j * NP + i] = (T)(m.dlagP[j * NP + i] * m.JeI);
+            k.DW[j * NP + i] = (T)(m.dlagP[j * NP + i] * m.gllw[j]);
+        }
+    for (int i = 0; i < NP; i++) k.w[i] = (T)m.gllw[i];
+    k.Je = (T)m.Je;
+    k.JeI = (T)m.JeI;
+    k.dt2_Je = (T)(m.sdt * m.sdt / m.Je);
+    return k;
+}
+
+template <typename T>
+Field<T> make_field(sks_solver* s)
+{
+    Field<T> F;
+    F.uc = (const T*)s->U[s->cur];
+    F.un = (T*)s->U[1 - s->cur];
+    F.dv = (T*)s->Dv;
+    F.cc = (T*)s->Cc;
+    F.mid = s->mid;
+    F.mat = (const T*)s->mat;
+    F.wxi = (const T*)s->wxi;
+    F.wzi = (const T*)s->wzi;
+    F.stc = (const T*)s->stc;
+    F.perim = (T*)s->perim;
+    return F;
+}
+
+template <typename T>
+Geo<T> make_geo(const sks_solver* s)
+{
+    Geo<T> G;
+    G.nex = s->m.nex; G.nez = s->m.nez; G.nx = s->m.nx; G.nz = s->m.nz;
+    G.ntx = s->ntx; G.ntz = s->ntz; G.HZ = s->HZ; G.ntiles = s->ntiles;
+    G.pstride = s->pstride;
+    G.np = (int64_t)s->m.nx * s->m.nz;
+    return G;
+}
+
+// one time step it >= 1 (injection, fused element/update kernel, seams, record)
+template <typename T, bool LF>
+int step_impl(sks_solver* s, int it, const double* Gcur, const double* Gprev, float* seis_row)
+{
+    const sks_model& m = s->m;
+    const int64_t np = (int64_t)m.nx * m.nz;
+    cudaStream_t st = s->stream;
+    if (it < m.nt_sem) {
+        const int n = (m.nx - s->nbl) + (m.nz - s->nbl - 1);
+        k_inject<T, LF><<<(n + 255) / 256, 256, 0, st>>>((T*)s->U[s->cur], (T*)s->Dv, (T*)s->Cc, np, m.nx, m.nz,
+                                                         s->nbl, Gcur, Gprev, m.mtotal);
+        s->launches++;
+    }
+    Field<T> F = make_field<T>(s);
+    Geo<T> G = make_geo<T>(s);
+    static thread_local Coef<T> k;
+    k = make_coef<T>(m);
+    const int blocks = (s->ntiles + 3) / 4;
+    if (m.anisotropic) k_main<T, true, LF><<<blocks, 128, 0, st>>>(F, G, k);
+    else k_main<T, false, LF><<<blocks, 128, 0, st>>>(F, G, k);
+    s->launches++;
+    if (s->nseam > 0) {
+        k_seam<T, LF><<<(s->nseam + 255) / 256, 256, 0, st>>>(F, G, k, s->seams, s->nseam);
+        s->launches++;
+    }
+    s->cur = 1 - s->cur;
+    if (m.ntrace > 0) {
+        k_record<T><<<(m.ntrace + 127) / 128, 128, 0, st>>>((const T*)s->U[s->cur], np, s->rec_off, m.ntrace, seis_row);
+        s->launches++;
+    }
+    return SKS_OK;
+}
+
+template <typename T, bool LF>
+int step0_impl(sks_solver* s, const double* G0, float* seis_row)
+{
+    const sks_model& m = s->m;
+    const int64_t np = (int64_t)m.nx * m.nz;
+    cudaStream_t st = s->stream;
+    s->cur = 0;
+    CK(cudaMemsetAsync(s->U[0], 0, 3 * np * sizeof(T), st));
+    CK(cudaMemsetAsync(s->U[1], 0, 3 * np * sizeof(T), st));
+    if (LF) {
+        CK(cudaMemsetAsync(s->Dv, 0, 3 * np * sizeof(T), st));
+        CK(cudaMemsetAsync(s->Cc, 0, 3 * np * sizeof(T), st));
+    }
+    if (m.nt_sem > 0) {
+        const int n = (m.nx - s->nbl - 1) + (m.nz - s->nbl);
+        k_init_line<T, LF><<<(n + 255) / 256, 256, 0, st>>>((T*)s->U[0], (T*)s->Dv, np, m.nx, m.nz, s->nbl, G0, m.mtotal);
+        s->launches++;
+    }
+    if (m.ntrace > 0) {
+        k_record<T><<<(m.ntrace + 127) / 128, 128, 0, st>>>((const T*)s->U[0], np, s->rec_off, m.ntrace, seis_row);
+        s->launches++;
+    }
+    return SKS_OK;
+}
+
+int run_chunk(sks_solver* s, int it0, int n)
+{
+    const sks_model& m = s->m;
+    const int L = m.mtotal + m.shtotal;
+    cudaStream_t st = s->stream;
+    // interpolated boundary traces for the injecting steps of this chunk
+    const int ni = std::max(0, std::min(it0 + n, m.nt_sem) - it0);
+    if (ni > 0) {
+        if (it0 > 0 && s->g_last > 0)
+            CK(cudaMemcpyAsync(s->G, s->G + (size_t)s->g_last * L, sizeof(double) * L, cudaMemcpyDeviceToDevice, st));
+        k_interp<<<ni, 256, 0, st>>>(s->G, L, it0, ni, s->rec_psv, m.mtotal, s->rec_sh, m.shtotal,
+                                     s->tap_psv, s->w_psv, s->tap_sh, s->w_sh);
+        s->launches++;
+        s->g_last = ni;
+    }
+    for (int i = 0; i < n; i++) {
+        const int it = it0 + i;
+        const double* Gcur = s->G + (size_t)(i + 1) * L;
+        const double* Gprev = s->G + (size_t)i * L;
+        float* row = s->seis + (size_t)i * 3 * m.ntrace;
+        int rc;
+        if (s->precision == SKS_FP64) {
+            rc = it == 0 ? step0_impl<double, false>(s, Gcur, row) : step_impl<double, false>(s, it, Gcur, Gprev, row);
+        } else {
+            rc = it == 0 ? step0_impl<float, true>(s, Gcur, row) : step_impl<float, true>(s, it, Gcur, Gprev, row);
+        }
+        if (rc) return rc;
+    }
+    CK(cudaGetLastError());
+    return SKS_OK;
+}
+
+}  // namespace
+
+extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solver** out)
+{
+    if (!su) return set_err(SKS_ERR_ARG, "set-up is NULL");
+    if (!out) { sks_setup_close(su); return set_err(SKS_ERR_ARG, "out is NULL"); }
+    *out = nullptr;
+    if (precision != SKS_FP64 && precision != SKS_FP32C) { sks_setup_close(su); return set_err(SKS_ERR_ARG, "unknown precision %d", precision); }
+    sks_solver* s = new (std::nothrow) sks_solver();
+    if (!s) { sks_setup_close(su); return set_err(SKS_ERR_NOMEM, "cannot allocate the solver"); }
+    s->m = su->m;                 // take ownership of the host model
+    memset(&su->m, 0, sizeof su->m);
+    delete su;
+    int rc = SKS_OK;
+    const sks_model& m = s->m;
+    if (m.hpn != N) { sks_model_free(&s->m); delete s; return set_err(SKS_ERR_UNSUPPORTED, "hpn=%d: the kernels are built for GLL degree %d", m.hpn, N); }
+    s->precision = precision;
+    s->device = device;
+    s->nbl = m.neh * m.hpn;
+    cudaError_t ce = cudaSetDevice(device);
+    if (ce != cudaSuccess) { sks_model_free(&s->m); delete s; return set_err(SKS_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(ce)); }
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    ce = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) { sks_model_free(&s->m); delete s; return set_err(SKS_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(ce)); }
+    s->HZ = pick_hz(m, sms);
+    s->ntx = (m.nex + TEX - 1) / TEX;
+    s->ntz = (m.nez + s->HZ - 1) / s->HZ;
+    s->ntiles = s->ntx * s->ntz;
+    s->pstride = 2 * (s->HZ * N + 1) + 2 * (TW - 1);
+    s->chunk = 64;
+    const size_t np = (size_t)m.nx * m.nz;
+    rc = precision == SKS_FP64 ? upload_tables<double>(s) : upload_tables<float>(s);
+    if (!rc) rc = dmalloc(s, &s->mid, np);
+    if (!rc) {
+        ce = cudaMemcpy(s->mid, m.mat_id, np * sizeof(uint16_t), cudaMemcpyHostToDevice);
+        if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "upload of material indices: %s", cudaGetErrorString(ce));
+    }
+    std::vector<SeamPt> seams;
+    if (!rc) {
+        build_seams(s, seams);
+        s->nseam = (int)seams.size();
+        rc = dmalloc(s, &s->seams, seams.size());
+        if (!rc && !seams.empty()) {
+            ce = cudaMemcpy(s->seams, seams.data(), seams.size() * sizeof(SeamPt), cudaMemcpyHostToDevice);
+            if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "upload of seam list: %s", cudaGetErrorString(ce));
+        }
+    }
+    if (!rc) rc = dmalloc(s, &s->rec_off, std::max(1, m.ntrace));
+    if (!rc && m.ntrace > 0) {
+        ce = cudaMemcpy(s->rec_off, m.rec_off, sizeof(int64_t) * m.ntrace, cudaMemcpyHostToDevice);
+        if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "upload of receivers: %s", cudaGetErrorString(ce));
+    }
+    if (!rc) rc = dmalloc(s, &s->seis, (size_t)s->chunk * 3 * std::max(1, m.ntrace));
+    if (!rc) rc = dmalloc(s, &s->G, (size_t)(s->chunk + 1) * (m.mtotal + m.shtotal));
+    if (!rc && m.nt_sem > 0) {
+        rc = dmalloc(s, &s->tap_psv, 4 * (size_t)m.nt_sem);
+        if (!rc) rc = dmalloc(s, &s->tap_sh, 4 * (size_t)m.nt_sem);
+        if (!rc) rc = dmalloc(s, &s->w_psv, 4 * (size_t)m.nt_sem);
+        if (!rc) rc = dmalloc(s, &s->w_sh, 4 * (size_t)m.nt_sem);
+        if (!rc) {
+            cudaMemcpy(s->tap_psv, m.tap_psv, 16 * (size_t)m.nt_sem, cudaMemcpyHostToDevice);
+            cudaMemcpy(s->tap_sh, m.tap_sh, 16 * (size_t)m.nt_sem, cudaMemcpyHostToDevice);
+            cudaMemcpy(s->w_psv, m.w_psv, 32 * (size_t)m.nt_sem, cudaMemcpyHostToDevice);
+            ce = cudaMemcpy(s->w_sh, m.w_sh, 32 * (size_t)m.nt_sem, cudaMemcpyHostToDevice);
+            if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "upload of the boundary schedule: %s", cudaGetErrorString(ce));
+        }
+    }
+    if (rc) { free_device(s); cudaStreamDestroy(s->stream); sks_model_free(&s->m); delete s; return rc; }
+    s->boundary_ready = (m.nt_sem == 0);
+    *out = s;
+    return SKS_OK;
+}
+
+extern "C" int sks_open_par(int argc, const char* const* argv, int precision, int device, sks_solver** out)
+{
+    sks_setup* su = nullptr;
+    int rc = sks_setup_open(argc, argv, &su);
+    if (rc) return rc;
+    return sks_open_setup(su, precision, device, out);
+}
+
+extern "C" int sks_set_boundary(sks_solver* s, const float* psv, int32_t nrec_psv, const float* sh, int32_t nrec_sh)
+{
+    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    const sks_model& m = s->m;
+    if (nrec_psv < m.nrec_psv) return set_err(SKS_ERR_BOUNDARY, "the run reads %d P-SV records, %d given", m.nrec_psv, nrec_psv);
+    if (!m.psv_only && nrec_sh < m.nrec_sh) return set_err(SKS_ERR_BOUNDARY, "the run reads %d SH records, %d given", m.nrec_sh, nrec_sh);
+    if (m.nrec_psv > 0 && !psv) return set_err(SKS_ERR_ARG, "psv records are NULL");
+    if (!m.psv_only && m.nrec_sh > 0 && !sh) return set_err(SKS_ERR_ARG, "sh records are NULL");
+    cudaSetDevice(s->device);
+    const size_t npsv = (size_t)m.nrec_psv * m.mtotal, nsh = (size_t)m.nrec_sh * m.shtotal;
+    if (s->nrec_psv_loaded < m.nrec_psv || !s->rec_psv) {
+        if (s->rec_psv) { cudaFree(s->rec_psv); s->device_bytes -= (int64_t)(sizeof(float) * (size_t)s->nrec_psv_loaded * m.mtotal); s->rec_psv = nullptr; }
+        int rc = dmalloc(s, &s->rec_psv, npsv);
+        if (rc) return rc;
+        s->nrec_psv_loaded = m.nrec_psv;
+    }
+    if (s->nrec_sh_loaded < m.nrec_sh || !s->rec_sh) {
+        if (s->rec_sh) { cudaFree(s->rec_sh); s->device_bytes -= (int64_t)(sizeof(float) * (size_t)s->nrec_sh_loaded * m.shtotal); s->rec_sh = nullptr; }
+        int rc = dmalloc(s, &s->rec_sh, nsh);
+        if (rc) return rc;
+        s->nrec_sh_loaded = m.nrec_sh;
+    }
+    if (npsv) CK(cudaMemcpyAsync(s->rec_psv, psv, npsv * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    if (nsh) {
+        if (m.psv_only || !sh) CK(cudaMemsetAsync(s->rec_sh, 0, nsh * sizeof(float), s->stream));
+        else CK(cudaMemcpyAsync(s->rec_sh, sh, nsh * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    s->boundary_ready = true;
+    return SKS_OK;
+}
+
+extern "C" int sks_load_boundary_files(sks_solver* s)
+{
+    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    const sks_model& m = s->m;
+    std::vector<float> psv((size_t)m.nrec_psv * m.mtotal), sh;
+    FILE* f = fopen(m.greenfile, "rb");
+    if (!f) return set_err(SKS_ERR_IO, "cannot open P-SV boundary file %s", m.greenfile);
+    size_t got = psv.empty() ? 0 : fread(psv.data(), sizeof(float), psv.size(), f);
+    fclose(f);
+    if (got != psv.size())
+        return set_err(SKS_ERR_BOUNDARY, "%s holds %zu of the %d records of %d values the run reads", m.greenfile,
+                       got / (size_t)m.mtotal, m.nrec_psv, m.mtotal);
+    if (!m.psv_only) {
+        sh.resize((size_t)m.nrec_sh * m.shtotal);
+        f = fopen(m.shgreenfile, "rb");
+        if (!f) return set_err(SKS_ERR_IO, "cannot open SH boundary file %s", m.shgreenfile);
+        got = sh.empty() ? 0 : fread(sh.data(), sizeof(float), sh.size(), f);
+        fclose(f);
+        if (got != sh.size())
+            return set_err(SKS_ERR_BOUNDARY, "%s holds %zu of the %d records of %d values the run reads", m.shgreenfile,
+                           got / (size_t)m.shtotal, m.nrec_sh, m.shtotal);
+    }
+    return sks_set_boundary(s, psv.data(), m.nrec_psv, m.psv_only ? nullptr : sh.data(), m.nrec_sh);
+}
+
+extern "C" int sks_run(sks_solver* s, int32_t nsteps, float* su, float* sv, float* sw)
+{
+    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    if (nsteps < 0) return set_err(SKS_ERR_ARG, "nsteps=%d", nsteps);
+    const sks_model& m = s->m;
+    if (s->step < m.nt_sem && !s->boundary_ready)
+        return set_err(SKS_ERR_STATE, "boundary records not set: call sks_load_boundary_files or sks_set_boundary");
+    cudaSetDevice(s->device);
+    const int end = std::min(m.nst, s->step + nsteps);
+    const int total = end - s->step;
+    std::vector<float> host((size_t)s->chunk * 3 * std::max(1, m.ntrace));
+    int done = 0;
+    while (s->step < end) {
+        const int n = std::min(s->chunk, end - s->step);
+        int rc = run_chunk(s, s->step, n);
+        if (rc) return rc;
+        if (m.ntrace > 0 && (su || sv || sw)) {
+            CK(cudaMemcpyAsync(host.data(), s->seis, sizeof(float) * (size_t)n * 3 * m.ntrace, cudaMemcpyDeviceToHost, s->stream));
+            CK(cudaStreamSynchronize(s->stream));
+            for (int i = 0; i < n; i++) {
+                const float* r = host.data() + (size_t)i * 3 * m.ntrace;
+                const size_t o = (size_t)(done + i) * m.ntrace;
+                if (su) memcpy(su + o, r, sizeof(float) * m.ntrace);
+                if (sv) memcpy(sv + o, r + m.ntrace, sizeof(float) * m.ntrace);
+                if (sw) memcpy(sw + o, r + 2 * m.ntrace, sizeof(float) * m.ntrace);
+            }
+        }
+        s->step += n;
+        done += n;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return total;
+}
+
+extern "C" int sks_reset(sks_solver* s)
+{
+    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    s->step = 0;
+    s->cur = 0;
+    s->g_last = 0;
+    return SKS_OK;
+}
+
+extern "C" int sks_get_info(const sks_solver* s, sks_info_t* info)
+{
+    if (!s || !info) return set_err(SKS_ERR_ARG, "NULL argument");
+    fill_info(s->m, info);
+    info->precision = s->precision;
+    info->step = s->step;
+    info->device_bytes = s->device_bytes;
+    return SKS_OK;
+}
+
+extern "C" int64_t sks_kernel_launches(const sks_solver* s) { return s ? s->launches : -1; }
+
+extern "C" void sks_destroy(sks_solver* s)
+{
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    free_device(s);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    sks_model_free(&s->m);
+    delete s;
+}

@@ -1,0 +1,219 @@
+"""Python binding of the C ABI in include/sks.h (ctypes, no torch types).
+
+    import sks
+    with sks.Setup(["par=run.par"]) as su:          # host-only set-up
+        info = su.info()
+    s = sks.Solver(["par=run.par"], precision=sks.FP32C)
+    s.load_boundary_files()
+    u, v, w = s.run(s.info()["nst"])               # seismograms [nst, ntrace]
+
+The library is the in-tree build s-sks_gb300/_build/libsks_gb300.so; there is
+no fallback: a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+FP64 = 0
+FP32C = 1
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_build", "libsks_gb300.so")
+
+ERRORS = {0: "OK", -1: "ERR_ARG", -2: "ERR_IO", -3: "ERR_MODEL", -4: "ERR_UNSUPPORTED", -5: "ERR_CUDA",
+          -6: "ERR_NOMEM", -7: "ERR_BOUNDARY", -8: "ERR_STATE", -9: "ERR_NONFINITE"}
+
+EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_run", "sks_reset",
+           "sks_get_info", "sks_setup_open", "sks_setup_info", "sks_setup_material", "sks_setup_mass",
+           "sks_setup_receivers", "sks_setup_schedule", "sks_setup_close", "sks_open_setup",
+           "sks_kernel_launches", "sks_destroy", "sks_last_error"]
+
+
+class SksError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Info(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("nex", "nez", "hpn", "nx", "nz", "nst", "nt_inject", "ntrace",
+                                         "mtotal", "shtotal", "nrec_psv", "nrec_sh", "nmat", "anisotropic",
+                                         "precision", "step")] + \
+               [("eh", C.c_double), ("h", C.c_double), ("sdt", C.c_double), ("device_bytes", C.c_int64)]
+
+    def asdict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"{LIB_PATH} is not built; run s-sks_gb300/sks_build.py")
+        L = C.CDLL(LIB_PATH)
+        vp, ip, dp, fp = C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_float)
+        argv_t = C.POINTER(C.c_char_p)
+        L.sks_open_par.argtypes = [C.c_int, argv_t, C.c_int, C.c_int, C.POINTER(vp)]
+        L.sks_load_boundary_files.argtypes = [vp]
+        L.sks_set_boundary.argtypes = [vp, fp, C.c_int32, fp, C.c_int32]
+        L.sks_run.argtypes = [vp, C.c_int32, fp, fp, fp]
+        L.sks_reset.argtypes = [vp]
+        L.sks_get_info.argtypes = [vp, C.POINTER(Info)]
+        L.sks_setup_open.argtypes = [C.c_int, argv_t, C.POINTER(vp)]
+        L.sks_setup_info.argtypes = [vp, C.POINTER(Info)]
+        L.sks_setup_material.argtypes = [vp, dp]
+        L.sks_setup_mass.argtypes = [vp, dp, dp]
+        L.sks_setup_receivers.argtypes = [vp, C.POINTER(C.c_int64)]
+        L.sks_setup_schedule.argtypes = [vp, ip, dp, ip, dp]
+        L.sks_setup_close.argtypes = [vp]
+        L.sks_setup_close.restype = None
+        L.sks_open_setup.argtypes = [vp, C.c_int, C.c_int, C.POINTER(vp)]
+        L.sks_kernel_launches.argtypes = [vp]
+        L.sks_kernel_launches.restype = C.c_int64
+        L.sks_destroy.argtypes = [vp]
+        L.sks_destroy.restype = None
+        L.sks_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def _check(rc: int) -> int:
+    if rc < 0:
+        raise SksError(rc, lib().sks_last_error().decode())
+    return rc
+
+
+def _argv(words) -> tuple:
+    words = ["sks"] + [str(w) for w in words]
+    arr = (C.c_char_p * len(words))(*[w.encode() for w in words])
+    return len(words), arr
+
+
+def _f32(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None else None
+
+
+class Setup:
+    """Host-only set-up of a par file (mesh, materials, mass, receivers, schedule)."""
+
+    def __init__(self, words):
+        self.h = C.c_void_p()
+        n, arr = _argv(words)
+        _check(lib().sks_setup_open(n, arr, C.byref(self.h)))
+
+    def info(self) -> dict:
+        i = Info()
+        _check(lib().sks_setup_info(self.h, C.byref(i)))
+        return i.asdict()
+
+    def material(self) -> np.ndarray:
+        i = self.info()
+        out = np.zeros((i["nx"] * i["nz"], 16))
+        _check(lib().sks_setup_material(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def mass(self):
+        i = self.info()
+        np_ = i["nx"] * i["nz"]
+        m = np.zeros(np_)
+        ab = np.zeros(3 * np_)
+        _check(lib().sks_setup_mass(self.h, m.ctypes.data_as(C.POINTER(C.c_double)),
+                                    ab.ctypes.data_as(C.POINTER(C.c_double))))
+        return m, ab.reshape(np_, 3)
+
+    def receivers(self) -> np.ndarray:
+        off = np.zeros(max(1, self.info()["ntrace"]), dtype=np.int64)
+        _check(lib().sks_setup_receivers(self.h, off.ctypes.data_as(C.POINTER(C.c_int64))))
+        return off[: self.info()["ntrace"]]
+
+    def schedule(self):
+        n = self.info()["nt_inject"]
+        tp, ts = np.zeros(4 * n + 1, np.int32), np.zeros(4 * n + 1, np.int32)
+        wp, ws = np.zeros(4 * n + 1), np.zeros(4 * n + 1)
+        ip, dp = C.POINTER(C.c_int32), C.POINTER(C.c_double)
+        _check(lib().sks_setup_schedule(self.h, tp.ctypes.data_as(ip), wp.ctypes.data_as(dp),
+                                        ts.ctypes.data_as(ip), ws.ctypes.data_as(dp)))
+        return (tp[:4 * n].reshape(n, 4), wp[:4 * n].reshape(n, 4),
+                ts[:4 * n].reshape(n, 4), ws[:4 * n].reshape(n, 4))
+
+    def close(self):
+        if self.h:
+            lib().sks_setup_close(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver:
+    """Device solver of one par file (sks_open_par)."""
+
+    def __init__(self, words, precision: int = FP64, device: int = 0):
+        self.h = C.c_void_p()
+        n, arr = _argv(words)
+        _check(lib().sks_open_par(n, arr, precision, device, C.byref(self.h)))
+
+    def info(self) -> dict:
+        i = Info()
+        _check(lib().sks_get_info(self.h, C.byref(i)))
+        return i.asdict()
+
+    def load_boundary_files(self):
+        _check(lib().sks_load_boundary_files(self.h))
+
+    def set_boundary(self, psv: np.ndarray, sh: np.ndarray | None):
+        psv = np.ascontiguousarray(psv, dtype=np.float32)
+        i = self.info()
+        nps = psv.size // max(1, i["mtotal"])
+        if sh is not None:
+            sh = np.ascontiguousarray(sh, dtype=np.float32)
+            nsh = sh.size // max(1, i["shtotal"])
+        else:
+            nsh = 0
+        _check(lib().sks_set_boundary(self.h, _f32(psv), nps, _f32(sh), nsh))
+
+    def run(self, nsteps: int, out=None):
+        nt = self.info()["ntrace"]
+        if out is None:
+            out = tuple(np.zeros((nsteps, max(nt, 0)), np.float32) for _ in range(3))
+        u, v, w = out
+        n = _check(lib().sks_run(self.h, nsteps, _f32(u), _f32(v), _f32(w)))
+        return u[:n], v[:n], w[:n]
+
+    def reset(self):
+        _check(lib().sks_reset(self.h))
+
+    def launches(self) -> int:
+        return lib().sks_kernel_launches(self.h)
+
+    def close(self):
+        if self.h:
+            lib().sks_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,33 @@
+"""Test configuration: paths, the `gpu` marker, and a session build of the
+library and the oracle (nvcc cross-compiles for sm_103a without a GPU)."""
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "s-sks_gb300")
+for p in (PKG, ROOT, os.path.join(ROOT, "tests")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built():
+    import sks_build
+    from oracle import oracle as orc
+    sks_build.build()
+    orc.build(None)
+    yield
+
+
+def have_gpu() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False

@@ -1,0 +1,184 @@
+"""GPU parity: the CUDA solver through the C ABI against the FP64 oracle.
+
+Bars: the plain FP64 form within relative L2 1e-10 of the FP64 oracle on every
+seismogram component; the FP32-compensated form within 1e-4.  Cases cover the
+isotropic and anisotropic stress kernels, P-SV+SH and P-SV-only injection,
+Stacey on/off, a GRT record step different from the SEM step with injection
+ending inside the run, Earth flattening, both receiver layouts, many warp-tile
+seams, runs split across calls, determinism and the drop-in CLI.
+"""
+import glob
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import sks
+import synth
+from oracle.oracle import Oracle
+from golden.make_golden import extract
+from util import chdir, seis_err
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+FP32C_TOL = 1e-4
+
+
+def _aniso_layers(H, tilt=20.0):
+    return [synth.SemLayer(H - 6, synth.iso_cij(8.1, 4.5, 3.4), 3.4),
+            synth.SemLayer(H - 3, synth.hexagonal_cij(8.1, 4.5, 3.4, 0.06, 30.0, tilt), 3.4),
+            synth.SemLayer(H + 1, synth.iso_cij(6.4, 3.6, 2.8), 2.8)]
+
+
+CASES = {
+    "aniso_full_sh": lambda: synth.Case(nex=16, nez=10, eh=2.0, sdt=0.01, nst=800, layers=_aniso_layers(20.0),
+                                        p=0.05, f0=1.0, sv_amp=1.0, sh_amp=0.5, ntrace=7, rec_x0=1.0,
+                                        rec_dx=4.0, semmodel_full=True),
+    "aniso_13_sh": lambda: synth.Case(nex=18, nez=9, eh=2.0, sdt=0.01, nst=760,
+                                      layers=_aniso_layers(18.0, tilt=0.0), p=0.05, f0=1.0, sv_amp=1.0,
+                                      sh_amp=0.7, ntrace=9, rec_x0=0.5, rec_dx=3.7),
+    "iso_psv": lambda: synth.Case(nex=30, nez=10, eh=2.0, sdt=0.01, nst=800, layers=synth.layered_two(20.0, 6.0),
+                                  p=0.045, f0=1.0, ntrace=15, rec_dx=4.0),
+    "seams_many": lambda: synth.Case(nex=40, nez=24, eh=1.0, sdt=0.005, nst=1400, layers=_aniso_layers(24.0),
+                                     p=0.045, f0=1.5, sv_amp=1.0, sh_amp=0.3, ntrace=21, rec_dx=1.9,
+                                     semmodel_full=True),
+    "rdt_half_short_grt": lambda: synth.Case(nex=16, nez=10, eh=2.0, sdt=0.005, dp=0.01, nt=300, nst=1500,
+                                             layers=_aniso_layers(20.0), p=0.05, f0=1.0, sh_amp=0.5,
+                                             ntrace=7, rec_dx=4.0, semmodel_full=True),
+    "psv_only_no_absorb": lambda: synth.Case(nex=16, nez=10, eh=2.0, sdt=0.01, nst=800, layers=_aniso_layers(20.0),
+                                             p=0.05, f0=1.0, ntrace=7, rec_dx=4.0, psv_only=True, absorb=0,
+                                             semmodel_full=True),
+    "flat0_raymodel_xbeg": lambda: synth.Case(nex=20, nez=8, eh=2.0, sdt=0.01, nst=700,
+                                              layers=synth.layered_two(16.0, 5.0), p=0.04, f0=1.0, flat=0,
+                                              readpars=0, get_rec=0, ntrace=6, sh_amp=0.4,
+                                              extra={"xbeg": "0.0", "idxplot": 13}),
+}
+
+
+@pytest.fixture(scope="module")
+def casedirs(tmp_path_factory):
+    out = {}
+    for name, mk in CASES.items():
+        d = str(tmp_path_factory.mktemp(name))
+        c = mk()
+        synth.write_case(c, d)
+        with chdir(d):
+            o = Oracle(["par=run.par"], fp64=True)
+            ref = o.run(c.nst)
+            o.close()
+        out[name] = (d, c, ref)
+    return out
+
+
+def _gpu_run(d, prec, nsteps, pieces=None):
+    with chdir(d), sks.Solver(["par=run.par"], precision=prec, device=0) as s:
+        s.load_boundary_files()
+        if not pieces:
+            return s.run(nsteps), s.info()
+        parts = []
+        done = 0
+        for p in pieces:
+            parts.append(s.run(p))
+            done += len(parts[-1][0])
+        rest = nsteps - done
+        if rest > 0:
+            parts.append(s.run(rest))
+        return tuple(np.concatenate([q[i] for q in parts]) for i in range(3)), s.info()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_fp64_matches_oracle(casedirs, name):
+    d, c, ref = casedirs[name]
+    out, info = _gpu_run(d, sks.FP64, c.nst)
+    assert out[0].shape == ref[0].shape
+    err = seis_err(out, ref)
+    assert np.isfinite(err) and err <= FP64_TOL, f"{name}: FP64 rel L2 {err:.3e}"
+    assert max(np.abs(r).max() for r in ref) > 0.5, "case produced no signal"
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_fp32c_matches_oracle(casedirs, name):
+    d, c, ref = casedirs[name]
+    out, _ = _gpu_run(d, sks.FP32C, c.nst)
+    err = seis_err(out, ref)
+    assert np.isfinite(err) and err <= FP32C_TOL, f"{name}: FP32C rel L2 {err:.3e}"
+
+
+@pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])
+def test_split_runs_equal_one_run(casedirs, prec):
+    d, c, _ = casedirs["seams_many"]
+    whole, _ = _gpu_run(d, prec, c.nst)
+    split, _ = _gpu_run(d, prec, c.nst, pieces=[1, 63, 64, 5, 70])
+    for i in range(3):
+        assert np.array_equal(whole[i], split[i])
+
+
+@pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])
+def test_deterministic(casedirs, prec):
+    d, c, _ = casedirs["aniso_full_sh"]
+    a, _ = _gpu_run(d, prec, c.nst)
+    b, _ = _gpu_run(d, prec, c.nst)
+    for i in range(3):
+        assert np.array_equal(a[i], b[i])
+
+
+def test_reset_replays(casedirs):
+    d, c, _ = casedirs["aniso_13_sh"]
+    with chdir(d), sks.Solver(["par=run.par"], precision=sks.FP64) as s:
+        s.load_boundary_files()
+        a = s.run(c.nst)
+        s.reset()
+        b = s.run(c.nst)
+    for i in range(3):
+        assert np.array_equal(a[i], b[i])
+
+
+def test_set_boundary_from_memory_equals_files(casedirs):
+    d, c, _ = casedirs["aniso_full_sh"]
+    with chdir(d):
+        with sks.Solver(["par=run.par"], precision=sks.FP64) as s:
+            info = s.info()
+            psv = np.fromfile("greenfile", np.float32)[: info["nrec_psv"] * info["mtotal"]]
+            sh = np.fromfile("shgreenfile", np.float32)[: info["nrec_sh"] * info["shtotal"]]
+            s.set_boundary(psv, sh)
+            a = s.run(c.nst)
+        b, _ = _gpu_run(d, sks.FP64, c.nst)
+    for i in range(3):
+        assert np.array_equal(a[i], b[i])
+
+
+def test_cli_drop_in_writes_reference_files(casedirs):
+    d, c, ref = casedirs["aniso_13_sh"]
+    cli = os.path.join(os.path.dirname(sks.LIB_PATH), "sem2d_psvsh_gb300")
+    r = subprocess.run([cli, "par=run.par"], cwd=d, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    nt = c.ntrace
+    got = [np.fromfile(os.path.join(d, f"seis.{x}"), np.float32).reshape(-1, nt) for x in "uvw"]
+    assert got[0].shape[0] == c.nst
+    assert seis_err(got, ref) <= FP64_TOL
+
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_golden_inputs_fp64_vs_oracle_and_reference(path, tmp_path):
+    """On the reference-generated fixtures: FP64 GPU within 1e-10 of the FP64
+    oracle, and within the reference's own FP32 rounding of its seismograms."""
+    d = str(tmp_path)
+    z = extract(path, d)
+    nt, nst = int(z["ntrace"]), int(z["nst"])
+    words = ["par=run.par"] + (["psv_only=1"] if str(z["prog"]) == "sem2d" else [])
+    gold = [z["seis_" + x].reshape(nst, nt) for x in "uvw"]
+    with chdir(d):
+        o = Oracle(words, fp64=True)
+        ref = o.run(nst)
+        o.close()
+        for prec, tol in ((sks.FP64, FP64_TOL), (sks.FP32C, FP32C_TOL)):
+            with sks.Solver(words, precision=prec) as s:
+                s.load_boundary_files()
+                out = s.run(nst)
+            assert seis_err(out, ref) <= tol
+            assert seis_err(out, gold) <= 5e-5
