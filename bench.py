@@ -1,0 +1,370 @@
+"""Benchmark of the SEM time step on one GB300 (and N replicas under torchrun).
+
+Workload: the anisotropic 3-component SKS case -- an 800 x 300 km box of
+800 x 300 elements of 1 km, GLL degree 4 (3201 x 1201 = 3,844,401 points), a
+35 km crust over a 100 km layer of 4 % hexagonal anisotropy (fast axis at
+azimuth 45 deg, tilt 20 deg: full c_ij) over the mantle, an SV plane wave with
+ray parameter 0.042 s/km and a 0.5 Hz Ricker pulse, dt = 5 ms, 201 surface
+receivers.  Inputs are synthetic (the generator in s-sks_gb300/synth.py).
+
+A step is one SEM time step over the whole mesh.  `value` is GLL-point
+updates per second of the FP32-compensated form, device resident, timed with
+CUDA events on the solver's stream; `e2e` is the same metric through the C ABI
+with host buffers (boundary records uploaded from pinned memory and the
+seismograms read back inside the timed region).  The FP64 form is measured
+the same way and reported beside it.  The per-step working set (~190 MB) is
+larger than the 129 MB L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "s-sks_gb300")
+for _p in (PKG, ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+NEX, NEZ = 800, 300
+FULL_STEPS = 24000
+BYTES_PER_POINT = {"fp32c": 74, "fp64": 74}   # see the roofline note in main()
+WORKLOAD = ("anisotropic 3-component SKS solve: 800x300 elements of 1 km, GLL degree 4, "
+            "3,844,401 points, 100 km hexagonal layer (4 %, azimuth 45, tilt 20), dt 5 ms, 201 receivers")
+
+
+def _peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_case(d: str, nst: int) -> None:
+    import synth
+    c = synth.config_aniso_3c(nst=nst)
+    synth.write_case(c, d)
+
+
+class Clocks:
+    """nvidia-smi clock/throttle sampling while the timed region runs."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    smax.append(float(f[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        except OSError:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.remove(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _pinned(n: int):
+    import torch
+    return torch.empty(n, dtype=torch.float32, pin_memory=True)
+
+
+def run_form(d: str, precision: int, steps: int, warmup: int, gpu: int, clocks: bool = False) -> dict:
+    """Device-resident timing of one form: W warm-up steps, then K timed."""
+    import sks
+    cwd = os.getcwd()
+    os.chdir(d)
+    try:
+        s = sks.Solver(["par=run.par"], precision=precision, device=gpu)
+        s.load_boundary_files()
+        info = s.info()
+        lib_run_noout(s, warmup)
+        s.enable_kernel_timing(True)
+        l0 = s.launches()
+        ck = Clocks(gpu) if clocks else None
+        if ck:
+            ck.__enter__()
+        n = lib_run_noout(s, steps)
+        if ck:
+            ck.__exit__(None, None, None)
+        ms = s.last_run_ms()
+        launches = s.launches() - l0
+        kt = s.kernel_timing()
+        s.close()
+    finally:
+        os.chdir(cwd)
+    npts = info["nx"] * info["nz"]
+    res = {"steps": n, "ms": ms, "ms_per_step": ms / n, "points": npts,
+           "updates_per_s": npts * n / (ms / 1e3), "launches": launches, "kernels": kt, "info": info}
+    if ck:
+        res["clocks"] = ck.summary()
+    return res
+
+
+def lib_run_noout(s, steps: int) -> int:
+    """sks_run with no seismogram buffers: nothing is copied back, no host sync per chunk."""
+    import sks
+    n = sks.lib().sks_run(s.h, steps, None, None, None)
+    if n < 0:
+        raise sks.SksError(n, sks.lib().sks_last_error().decode())
+    return n
+
+
+def run_e2e(d: str, precision: int, steps: int, warmup: int, gpu: int) -> dict:
+    """Through the C ABI with host buffers: upload the run's boundary records from
+    pinned memory, run, read the seismograms back; wall-clock timed."""
+    import ctypes as C
+    import sks
+    cwd = os.getcwd()
+    os.chdir(d)
+    try:
+        s = sks.Solver(["par=run.par", f"nst={steps}"], precision=precision, device=gpu)
+        info = s.info()
+        npsv, nsh = info["nrec_psv"] * info["mtotal"], info["nrec_sh"] * info["shtotal"]
+        psv, sh = _pinned(npsv), _pinned(nsh)
+        psv.numpy()[:] = np.fromfile("greenfile", np.float32, count=npsv)
+        sh.numpy()[:] = np.fromfile("shgreenfile", np.float32, count=nsh)
+        nt = info["ntrace"]
+        outs = [_pinned(steps * nt) for _ in range(3)]
+        fp = C.POINTER(C.c_float)
+        ptr = lambda t: C.cast(t.data_ptr(), fp)
+        # warm-up pass (same calls), then the timed pass
+        for timed in (False, True):
+            s.reset()
+            t0 = time.perf_counter()
+            rc = sks.lib().sks_set_boundary(s.h, ptr(psv), info["nrec_psv"], ptr(sh), info["nrec_sh"])
+            if rc < 0:
+                raise sks.SksError(rc, sks.lib().sks_last_error().decode())
+            n = sks.lib().sks_run(s.h, steps, ptr(outs[0]), ptr(outs[1]), ptr(outs[2]))
+            if n < 0:
+                raise sks.SksError(n, sks.lib().sks_last_error().decode())
+            wall = time.perf_counter() - t0
+        s.close()
+    finally:
+        os.chdir(cwd)
+    npts = info["nx"] * info["nz"]
+    return {"value": npts * n / wall, "wall_s": wall, "h2d_bytes_per_step": (npsv + nsh) * 4 // max(1, n),
+            "d2h_bytes_per_step": 3 * nt * 4, "steps": n}
+
+
+# ---------------------------------------------------------------- CPU side
+def _cpu_worker(args):
+    d, nsteps, fp64 = args
+    sys.path.insert(0, ROOT)
+    from oracle.oracle import Oracle
+    os.chdir(d)
+    o = Oracle(["par=run.par"], fp64=fp64)
+    o.run(1)                      # step 0 (initialisation only)
+    t0 = time.perf_counter()
+    o.run(nsteps)
+    dt = time.perf_counter() - t0
+    pts = o.nx * o.nz
+    o.close()
+    return pts * nsteps, dt
+
+
+def cpu_rate(d: str, nsteps: int, procs: int) -> dict:
+    """The oracle's float build (the reference's arithmetic restated) on the host
+    cores: `procs` independent single-threaded solves at once."""
+    from oracle import oracle as orc
+    orc.build(None)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(_cpu_worker, [(d, nsteps, False)] * procs)
+        wall = time.perf_counter() - t0
+    pts = sum(r[0] for r in res)
+    per_proc = [r[0] / r[1] for r in res]
+    return {"value": sum(per_proc), "per_process": statistics.median(per_proc), "wall_s": wall, "procs": procs,
+            "pts": pts}
+
+
+# ---------------------------------------------------------------- main
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        return dist, int(os.environ["RANK"]), ws, int(os.environ.get("LOCAL_RANK", "0"))
+    return None, 0, 1, 0
+
+
+def _max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=30)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    a = ap.parse_args()
+    a.warmup = max(3, a.warmup)
+    dist, rank, world, local = _dist()
+
+    if a.impl == "reference":
+        # the reference's CPU path (float restatement, bit-exact to the
+        # reference binary) on every host core, rank 0 only
+        if rank != 0:
+            return
+        ncpu = os.cpu_count() or 1
+        d = tempfile.mkdtemp(prefix="sks_ref_")
+        try:
+            make_case(d, 8)
+            nsteps = max(1, min(a.cpu_steps, 3))
+            r = cpu_rate(d, nsteps, ncpu)
+        finally:
+            shutil.rmtree(d, ignore_errors=True)
+        v = r["value"]
+        npts = 3201 * 1201
+        line = {"impl": "reference", "metric": "GLL-pt updates/s", "value": v, "unit": "GLL-pt updates/s",
+                "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": npts / v * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": {"workload": WORKLOAD, "form": "reference float arithmetic"},
+                "cpu_baseline": {"value": v, "unit": "GLL-pt updates/s", "cores": ncpu, "kind": "port",
+                                 "sample": f"{nsteps} time steps of the full mesh in each of {ncpu} "
+                                           "independent single-threaded processes (oracle float build, "
+                                           "bit-exact to the reference binary)"},
+                "e2e": {"value": v, "unit": "GLL-pt updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    gpu = local if world > 1 else 0
+    torch.cuda.set_device(gpu)
+    d = tempfile.mkdtemp(prefix="sks_bench_")
+    try:
+        nst = a.warmup + a.steps + 8
+        make_case(d, nst)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        r32 = run_form(d, 1, a.steps, a.warmup, gpu, clocks=True)
+        r64 = run_form(d, 0, min(a.steps, 1000), a.warmup, gpu)
+        e2e = run_e2e(d, 1, a.steps, a.warmup, gpu)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        ms32 = _max_over_ranks(dist, r32["ms"])
+        ms64 = _max_over_ranks(dist, r64["ms"])
+        e2e_wall = _max_over_ranks(dist, e2e["wall_s"])
+        cpu = None
+        if rank == 0 and world == 1 and not a.no_cpu:
+            cpu = cpu_rate(d, a.cpu_steps, 1)
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    if rank != 0:
+        return
+    npts = r32["points"]
+    value = world * npts * r32["steps"] / (ms32 / 1e3)
+    v64 = world * npts * r64["steps"] / (ms64 / 1e3)
+    peak, peak_kind = _peaks()
+    # roofline of the dominant kernel (fused element/update): algorithmic bytes
+    # per launch = points it updates x 74 B (u, d, Kahan c: 3 x 4 B read + write
+    # each, 2 B material index) over its mean event-timed duration
+    km, kc = r32["kernels"]["element"]
+    main_pts = npts - r32["info"]["seam_points"]
+    t_launch = km / max(1, kc) / 1e3
+    achieved = main_pts * BYTES_PER_POINT["fp32c"] / t_launch / 1e9
+    traffic = _traffic_per_launch(main_pts)
+    total_k = sum(v[0] for v in r32["kernels"].values())
+    line = {
+        "metric": "GLL-pt updates/s", "value": value, "unit": "GLL-pt updates/s", "n_gpus": world,
+        "steps": r32["steps"], "warmup": a.warmup, "ms_per_step": ms32 / r32["steps"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": "FP32 wavefield, Kahan-compensated leapfrog",
+                   "points": npts, "l2": "working set > L2 (no flush)", "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "k_main (fused element force + assembly + update)",
+                     "kernel_ms_per_launch": t_launch * 1e3, "kernel_share": km / max(total_k, 1e-12)},
+        "e2e": {"value": world * npts * e2e["steps"] / e2e_wall, "unit": "GLL-pt updates/s",
+                "h2d_bytes_per_step": e2e["h2d_bytes_per_step"], "d2h_bytes_per_step": e2e["d2h_bytes_per_step"]},
+        "gpu_launches": r32["launches"],
+        "clocks": r32.get("clocks"),
+        "fp64": {"value": v64, "unit": "GLL-pt updates/s", "ms_per_step": ms64 / r64["steps"],
+                 "steps": r64["steps"]},
+        "solves_per_hour": {"fp32c": 3600.0 / (FULL_STEPS * ms32 / r32["steps"] / 1e3) * world,
+                            "fp64": 3600.0 / (FULL_STEPS * ms64 / r64["steps"] / 1e3) * world,
+                            "solve_steps": FULL_STEPS},
+        "kernel_ms": {k: v[0] for k, v in r32["kernels"].items()},
+    }
+    if cpu:
+        line["cpu_baseline"] = {"value": cpu["value"], "unit": "GLL-pt updates/s", "cores": 1, "kind": "port",
+                                "sample": f"{a.cpu_steps} time steps of the same mesh, one thread, oracle float "
+                                          "build (bit-exact to the reference binary)"}
+    print(json.dumps(line))
+
+
+def _traffic_per_launch(points: int):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        t = json.load(f)
+    bpp = t.get("fp32c_bytes_per_point")
+    return None if bpp is None else bpp * points
+
+
+if __name__ == "__main__":
+    main()

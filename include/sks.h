@@ -60,6 +60,9 @@ typedef struct {
     int32_t step;                 /* next step sks_run() will take        */
     double  eh, h, sdt;           /* element size, GLL spacing, time step */
     int64_t device_bytes;         /* device memory held by the handle     */
+    int64_t seam_points;          /* points shared by warp tiles          */
+    int32_t tile_rows;            /* element rows per warp tile           */
+    int32_t reserved;
 } sks_info_t;
 
 /* Replaces main() of sem2d_psvsh up to its time loop (sem2d_psvsh.c:82-416):
@@ -131,8 +134,24 @@ void sks_setup_close(sks_setup *su);
  * and on failure. */
 int sks_open_setup(sks_setup *su, int precision, int device, sks_solver **out);
 
-/* Kernel launches issued by sks_run() so far (instrumentation). */
+/* ---- instrumentation --------------------------------------------------
+ * Kernel launches issued by sks_run() so far. */
 int64_t sks_kernel_launches(const sks_solver *s);
+
+/* Device time in ms of the last sks_run(): CUDA events recorded on the
+ * solver's stream before its first and after its last launch. */
+double sks_last_run_ms(const sks_solver *s);
+
+/* Per-kernel-class device time: with timing on, every launch is bracketed by
+ * CUDA events on the solver's stream and its time added to its class. */
+#define SKS_KC_ELEMENT  0   /* fused element force + assembly + update      */
+#define SKS_KC_SEAM     1   /* points shared by warp tiles                  */
+#define SKS_KC_INJECT   2   /* GRT boundary injection (and step-0 set line) */
+#define SKS_KC_RECORD   3   /* receiver sampling                            */
+#define SKS_KC_INTERP   4   /* boundary-trace interpolation                 */
+#define SKS_KERNEL_CLASSES 5
+int sks_enable_kernel_timing(sks_solver *s, int on);   /* also clears the sums */
+int sks_kernel_timing(const sks_solver *s, double *ms, int64_t *count);  /* arrays of SKS_KERNEL_CLASSES */
 
 void sks_destroy(sks_solver *s);
 

@@ -72,6 +72,15 @@ struct sks_solver {
     int chunk;
     int64_t device_bytes;
     bool boundary_ready;
+    // instrumentation: whole-run events, per-kernel-class event pairs
+    cudaEvent_t run_ev[2];
+    double last_run_ms;
+    int timing;
+    std::vector<cudaEvent_t> kev;     // pool of event pairs for one chunk
+    std::vector<int> kcls;            // class of each recorded pair
+    int kused;
+    double kms[SKS_KERNEL_CLASSES];
+    int64_t kcount[SKS_KERNEL_CLASSES];
 };
 
 struct sks_setup {
@@ -179,6 +188,43 @@ void free_device(sks_solver* s)
     s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->wxi = s->wzi = s->stc = s->perim = nullptr;
     s->mid = nullptr; s->seams = nullptr; s->rec_off = nullptr; s->seis = nullptr; s->G = nullptr;
     s->rec_psv = s->rec_sh = nullptr; s->tap_psv = s->tap_sh = nullptr; s->w_psv = s->w_sh = nullptr;
+}
+
+// per-kernel-class timing: an event pair around each launch when enabled
+struct KTimer {
+    sks_solver* s;
+    int cls;
+    int idx;
+    KTimer(sks_solver* sv, int c) : s(sv), cls(c), idx(-1) {
+        if (!s->timing) return;
+        if ((size_t)(2 * s->kused + 2) > s->kev.size()) {
+            const size_t old = s->kev.size();
+            s->kev.resize(old + 64);
+            for (size_t i = old; i < s->kev.size(); i++) cudaEventCreate(&s->kev[i]);
+            s->kcls.resize(s->kev.size() / 2);
+        }
+        idx = s->kused++;
+        s->kcls[idx] = cls;
+        cudaEventRecord(s->kev[2 * idx], s->stream);
+    }
+    ~KTimer() {
+        if (idx >= 0) cudaEventRecord(s->kev[2 * idx + 1], s->stream);
+        s->launches++;
+    }
+};
+
+int collect_timing(sks_solver* s)
+{
+    if (!s->timing || s->kused == 0) return SKS_OK;
+    CK(cudaEventSynchronize(s->kev[2 * s->kused - 1]));
+    for (int i = 0; i < s->kused; i++) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, s->kev[2 * i], s->kev[2 * i + 1]));
+        s->kms[s->kcls[i]] += ms;
+        s->kcount[s->kcls[i]]++;
+    }
+    s->kused = 0;
+    return SKS_OK;
 }
 
 int pick_hz(const sks_model& m, int sm_count)
@@ -367,26 +413,28 @@ int step_impl(sks_solver* s, int it, const double* Gcur, const double* Gprev, fl
     cudaStream_t st = s->stream;
     if (it < m.nt_sem) {
         const int n = (m.nx - s->nbl) + (m.nz - s->nbl - 1);
+        KTimer t(s, SKS_KC_INJECT);
         k_inject<T, LF><<<(n + 255) / 256, 256, 0, st>>>((T*)s->U[s->cur], (T*)s->Dv, (T*)s->Cc, np, m.nx, m.nz,
                                                          s->nbl, Gcur, Gprev, m.mtotal);
-        s->launches++;
     }
     Field<T> F = make_field<T>(s);
     Geo<T> G = make_geo<T>(s);
     static thread_local Coef<T> k;
     k = make_coef<T>(m);
     const int blocks = (s->ntiles + 3) / 4;
-    if (m.anisotropic) k_main<T, true, LF><<<blocks, 128, 0, st>>>(F, G, k);
-    else k_main<T, false, LF><<<blocks, 128, 0, st>>>(F, G, k);
-    s->launches++;
+    {
+        KTimer t(s, SKS_KC_ELEMENT);
+        if (m.anisotropic) k_main<T, true, LF><<<blocks, 128, 0, st>>>(F, G, k);
+        else k_main<T, false, LF><<<blocks, 128, 0, st>>>(F, G, k);
+    }
     if (s->nseam > 0) {
+        KTimer t(s, SKS_KC_SEAM);
         k_seam<T, LF><<<(s->nseam + 255) / 256, 256, 0, st>>>(F, G, k, s->seams, s->nseam);
-        s->launches++;
     }
     s->cur = 1 - s->cur;
     if (m.ntrace > 0) {
+        KTimer t(s, SKS_KC_RECORD);
         k_record<T><<<(m.ntrace + 127) / 128, 128, 0, st>>>((const T*)s->U[s->cur], np, s->rec_off, m.ntrace, seis_row);
-        s->launches++;
     }
     return SKS_OK;
 }
@@ -406,12 +454,12 @@ int step0_impl(sks_solver* s, const double* G0, float* seis_row)
     }
     if (m.nt_sem > 0) {
         const int n = (m.nx - s->nbl - 1) + (m.nz - s->nbl);
+        KTimer t(s, SKS_KC_INJECT);
         k_init_line<T, LF><<<(n + 255) / 256, 256, 0, st>>>((T*)s->U[0], (T*)s->Dv, np, m.nx, m.nz, s->nbl, G0, m.mtotal);
-        s->launches++;
     }
     if (m.ntrace > 0) {
+        KTimer t(s, SKS_KC_RECORD);
         k_record<T><<<(m.ntrace + 127) / 128, 128, 0, st>>>((const T*)s->U[0], np, s->rec_off, m.ntrace, seis_row);
-        s->launches++;
     }
     return SKS_OK;
 }
@@ -426,9 +474,11 @@ int run_chunk(sks_solver* s, int it0, int n)
     if (ni > 0) {
         if (it0 > 0 && s->g_last > 0)
             CK(cudaMemcpyAsync(s->G, s->G + (size_t)s->g_last * L, sizeof(double) * L, cudaMemcpyDeviceToDevice, st));
-        k_interp<<<ni, 256, 0, st>>>(s->G, L, it0, ni, s->rec_psv, m.mtotal, s->rec_sh, m.shtotal,
-                                     s->tap_psv, s->w_psv, s->tap_sh, s->w_sh);
-        s->launches++;
+        {
+            KTimer t(s, SKS_KC_INTERP);
+            k_interp<<<ni, 256, 0, st>>>(s->G, L, it0, ni, s->rec_psv, m.mtotal, s->rec_sh, m.shtotal,
+                                         s->tap_psv, s->w_psv, s->tap_sh, s->w_sh);
+        }
         s->g_last = ni;
     }
     for (int i = 0; i < n; i++) {
@@ -599,9 +649,16 @@ extern "C" int sks_run(sks_solver* s, int32_t nsteps, float* su, float* sv, floa
     const int total = end - s->step;
     std::vector<float> host((size_t)s->chunk * 3 * std::max(1, m.ntrace));
     int done = 0;
+    if (!s->run_ev[0]) {
+        CK(cudaEventCreate(&s->run_ev[0]));
+        CK(cudaEventCreate(&s->run_ev[1]));
+    }
+    CK(cudaEventRecord(s->run_ev[0], s->stream));
     while (s->step < end) {
         const int n = std::min(s->chunk, end - s->step);
         int rc = run_chunk(s, s->step, n);
+        if (rc) return rc;
+        rc = collect_timing(s);
         if (rc) return rc;
         if (m.ntrace > 0 && (su || sv || sw)) {
             CK(cudaMemcpyAsync(host.data(), s->seis, sizeof(float) * (size_t)n * 3 * m.ntrace, cudaMemcpyDeviceToHost, s->stream));
@@ -617,7 +674,13 @@ extern "C" int sks_run(sks_solver* s, int32_t nsteps, float* su, float* sv, floa
         s->step += n;
         done += n;
     }
+    CK(cudaEventRecord(s->run_ev[1], s->stream));
     CK(cudaStreamSynchronize(s->stream));
+    {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, s->run_ev[0], s->run_ev[1]));
+        s->last_run_ms = ms;
+    }
     return total;
 }
 
@@ -637,6 +700,8 @@ extern "C" int sks_get_info(const sks_solver* s, sks_info_t* info)
     info->precision = s->precision;
     info->step = s->step;
     info->device_bytes = s->device_bytes;
+    info->seam_points = s->nseam;
+    info->tile_rows = s->HZ;
     return SKS_OK;
 }
 
@@ -648,7 +713,30 @@ extern "C" void sks_destroy(sks_solver* s)
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_device(s);
+    for (cudaEvent_t e : s->kev) cudaEventDestroy(e);
+    if (s->run_ev[0]) { cudaEventDestroy(s->run_ev[0]); cudaEventDestroy(s->run_ev[1]); }
     if (s->stream) cudaStreamDestroy(s->stream);
     sks_model_free(&s->m);
     delete s;
+}
+
+extern "C" double sks_last_run_ms(const sks_solver* s) { return s ? s->last_run_ms : -1.0; }
+
+extern "C" int sks_enable_kernel_timing(sks_solver* s, int on)
+{
+    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    s->timing = on ? 1 : 0;
+    for (int i = 0; i < SKS_KERNEL_CLASSES; i++) { s->kms[i] = 0; s->kcount[i] = 0; }
+    s->kused = 0;
+    return SKS_OK;
+}
+
+extern "C" int sks_kernel_timing(const sks_solver* s, double* ms, int64_t* count)
+{
+    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    for (int i = 0; i < SKS_KERNEL_CLASSES; i++) {
+        if (ms) ms[i] = s->kms[i];
+        if (count) count[i] = s->kcount[i];
+    }
+    return SKS_OK;
 }

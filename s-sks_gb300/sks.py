@@ -29,7 +29,10 @@ ERRORS = {0: "OK", -1: "ERR_ARG", -2: "ERR_IO", -3: "ERR_MODEL", -4: "ERR_UNSUPP
 EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_run", "sks_reset",
            "sks_get_info", "sks_setup_open", "sks_setup_info", "sks_setup_material", "sks_setup_mass",
            "sks_setup_receivers", "sks_setup_schedule", "sks_setup_close", "sks_open_setup",
-           "sks_kernel_launches", "sks_destroy", "sks_last_error"]
+           "sks_kernel_launches", "sks_last_run_ms", "sks_enable_kernel_timing", "sks_kernel_timing",
+           "sks_destroy", "sks_last_error"]
+
+KERNEL_CLASSES = ["element", "seam", "inject", "record", "interp"]
 
 
 class SksError(RuntimeError):
@@ -42,7 +45,8 @@ class Info(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("nex", "nez", "hpn", "nx", "nz", "nst", "nt_inject", "ntrace",
                                          "mtotal", "shtotal", "nrec_psv", "nrec_sh", "nmat", "anisotropic",
                                          "precision", "step")] + \
-               [("eh", C.c_double), ("h", C.c_double), ("sdt", C.c_double), ("device_bytes", C.c_int64)]
+               [("eh", C.c_double), ("h", C.c_double), ("sdt", C.c_double), ("device_bytes", C.c_int64),
+                ("seam_points", C.c_int64), ("tile_rows", C.c_int32), ("reserved", C.c_int32)]
 
     def asdict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -76,6 +80,10 @@ def lib() -> C.CDLL:
         L.sks_open_setup.argtypes = [vp, C.c_int, C.c_int, C.POINTER(vp)]
         L.sks_kernel_launches.argtypes = [vp]
         L.sks_kernel_launches.restype = C.c_int64
+        L.sks_last_run_ms.argtypes = [vp]
+        L.sks_last_run_ms.restype = C.c_double
+        L.sks_enable_kernel_timing.argtypes = [vp, C.c_int]
+        L.sks_kernel_timing.argtypes = [vp, dp, C.POINTER(C.c_int64)]
         L.sks_destroy.argtypes = [vp]
         L.sks_destroy.restype = None
         L.sks_last_error.restype = C.c_char_p
@@ -200,6 +208,18 @@ class Solver:
 
     def launches(self) -> int:
         return lib().sks_kernel_launches(self.h)
+
+    def last_run_ms(self) -> float:
+        return lib().sks_last_run_ms(self.h)
+
+    def enable_kernel_timing(self, on: bool = True):
+        _check(lib().sks_enable_kernel_timing(self.h, 1 if on else 0))
+
+    def kernel_timing(self) -> dict:
+        ms = (C.c_double * 5)()
+        cnt = (C.c_int64 * 5)()
+        _check(lib().sks_kernel_timing(self.h, ms, cnt))
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(KERNEL_CLASSES)}
 
     def close(self):
         if self.h:
