@@ -8,19 +8,21 @@
 //   kirrecord_zhl    sample the surface receivers.
 // Here the element force, the assembly and the update are one kernel.
 //
-// Warp tile.  A warp owns TEX=6 consecutive elements in x and a run of HZ
-// element rows in z.  Lane l = 5e + a (e = element 0..5, a = GLL column
-// 0..4) holds the 5 points of column a of its element for the current element
-// row in registers.  d/dz contractions run inside a lane (its own column),
-// d/dx and the x part of the divergence read the other 4 columns of the
-// element with warp shuffles.  The warp walks its element rows bottom-up;
-// the top row of one element row is the bottom row of the next, so its
-// displacement and its partial internal force are carried in registers.
-// Global assembly is gather-style and deterministic: a point's force is the
-// sum of its element contributions in a fixed order -- in-warp by shuffle
-// (left element first, lower element first, the reference's ex-outer/ez-inner
-// order), across warp tiles through a per-tile perimeter buffer that
-// k_seam sums in a fixed tile order.  No atomics, no global force array.
+// Tiling.  A warp covers TEX=6 consecutive elements in x: lane l = 5e + a
+// (e = element 0..5, a = GLL column 0..4) holds the 5 points of column a of
+// its element for the current element row in registers.  d/dz contractions
+// run inside a lane (its own column), d/dx and the x part of the divergence
+// read the other 4 columns of the element with warp shuffles.  A CTA puts NW
+// warps side by side and walks a band of HZ element rows bottom-up; the top
+// row of one element row is the bottom row of the next, so its displacement
+// and its partial force are carried in registers.  Each CTA recomputes one
+// element column to its left and one element row below its band (halos), so
+// every point it owns receives all of its element contributions inside the
+// CTA: the force of a point is gathered in a fixed order (left element
+// first, lower element first; in-warp by shuffle, warp to warp through shared
+// memory), with no atomics, no global force array and no second pass.  The
+// update, the receiver sampling and the next step's boundary injection are
+// applied where the point's force is complete.
 //
 // Forms.  LF=false: FP64, the reference's 3-level update (two displacement
 // buffers; u^{n+1} overwrites u^{n-1}).  LF=true: FP32 leapfrog on
@@ -52,8 +54,8 @@ struct Coef {
 template <typename T>
 struct Geo {
     int nex, nez, nx, nz;
-    int ntx, ntz, HZ, ntiles;
-    int pstride;                  // perimeter entries per tile
+    int ncx, ncz, HZ, nblocks;    // CTA grid: ncx columns x ncz row bands of HZ element rows
+    int nbl;                      // GRT interface line: row nbl (ix >= nbl), column nbl (iz > nbl)
     int64_t np;                   // nx*nz
 };
 
@@ -68,7 +70,17 @@ struct Field {
     const T* __restrict__ wxi;          // 1 / (sum of GLL weights at column ix)
     const T* __restrict__ wzi;          // 1 / (... at row iz)
     const T* __restrict__ stc;          // Stacey coefficients [nbnd][3][3]: dt^2/(M+A), 2M/(M+A), (M-A)/(M+A)
-    T* __restrict__ perim;              // [ntiles][pstride][3] partial forces on tile perimeters
+    // next step's boundary injection, fused into this step's write (FP64 traces)
+    const double* __restrict__ gnow;    // g(it)
+    const double* __restrict__ gnext;   // g(it+1)
+    int mtotal;
+    int inject_next;                    // it+1 < number of injecting steps
+    // receivers, fused: a bitmap over points, then the sorted offsets
+    const uint32_t* __restrict__ recbits;
+    const int64_t* __restrict__ rec_off;     // sorted
+    const int32_t* __restrict__ rec_idx;     // trace index of each sorted offset
+    int nrec, ntrace;
+    float* __restrict__ seis_row;            // [3][ntrace] of this step
 };
 
 __device__ __forceinline__ int64_t stacey_index(int ix, int iz, int nx, int nz)
@@ -104,7 +116,7 @@ struct MatRow<float, true> {
 };
 template <typename T>
 struct MatRow<T, false> {
-    T s[MAT_STRIDE];   // only s[0] (C11=C33), s[4] (C13), s[5] (C66=C55=C44), s[15] used
+    T s[MAT_STRIDE];   // only s[0] (C11=C33), s[4] (C13), s[5] (C66=C55=C44), s[15] (1/rho) used
     __device__ __forceinline__ void load(const T* __restrict__ m) {
         s[0] = __ldg(m); s[4] = __ldg(m + 4); s[5] = __ldg(m + 5); s[15] = __ldg(m + 15);
     }
@@ -132,82 +144,135 @@ __device__ __forceinline__ void stress(const MatRow<T, ANISO>& M, const T e[5], 
     }
 }
 
-// one owned point: FP64 3-level or FP32 compensated leapfrog update
+// The state a lane needs to update one owned point, loaded at the start of
+// the element row so its latency overlaps the element force.
 template <typename T, bool LF>
-__device__ __forceinline__ void update_point(const Field<T>& F, const Geo<T>& G, const Coef<T>& k,
-                                             int ix, int iz, const T u[3], const T K[3], T rinv)
+struct Aux {
+    T a[3];            // FP64: u^{n-1};  FP32: d
+    T b[LF ? 3 : 1];   // FP32: Kahan compensation
+};
+
+template <typename T, bool LF>
+__device__ __forceinline__ void load_aux(const Field<T>& F, int64_t np, int64_t g, Aux<T, LF>& x)
 {
-    const int64_t g = (int64_t)iz * G.nx + ix;
-    const int64_t bi = stacey_index(ix, iz, G.nx, G.nz);
-    if (!LF) {
-        T u0[3];
 #pragma unroll
-        for (int c = 0; c < 3; c++) u0[c] = F.un[c * G.np + g];
-        if (bi < 0) {
-            const T mdt2 = k.dt2_Je * rinv * F.wxi[ix] * F.wzi[iz];
-#pragma unroll
-            for (int c = 0; c < 3; c++) F.un[c * G.np + g] = (-mdt2 * K[c] + (T)2 * u[c]) - u0[c];
-        } else {
-            const T* p = F.stc + bi * 9;
-#pragma unroll
-            for (int c = 0; c < 3; c++) F.un[c * G.np + g] = (-p[3 * c] * K[c] + p[3 * c + 1] * u[c]) - p[3 * c + 2] * u0[c];
-        }
-    } else {
-        T d[3], cm[3];
-#pragma unroll
-        for (int c = 0; c < 3; c++) { d[c] = F.dv[c * G.np + g]; cm[c] = F.cc[c * G.np + g]; }
-        T dn[3];
-        if (bi < 0) {
-            const T mdt2 = k.dt2_Je * rinv * F.wxi[ix] * F.wzi[iz];
-#pragma unroll
-            for (int c = 0; c < 3; c++) dn[c] = fma(-mdt2, K[c], d[c]);
-        } else {
-            const T* p = F.stc + bi * 9;
-#pragma unroll
-            for (int c = 0; c < 3; c++) dn[c] = p[3 * c + 2] * d[c] - p[3 * c] * K[c];
-        }
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const T y = dn[c] - cm[c];
-            const T t = u[c] + y;
-            const T cn = (t - u[c]) - y;
-            F.un[c * G.np + g] = t;
-            F.dv[c * G.np + g] = dn[c];
-            F.cc[c * G.np + g] = cn;
-        }
+    for (int c = 0; c < 3; c++) {
+        if (!LF) x.a[c] = F.un[c * np + g];
+        else { x.a[c] = F.dv[c * np + g]; x.b[c] = F.cc[c * np + g]; }
     }
 }
 
-__device__ __forceinline__ int perim_pos(int col, int row, int W_eff, int R, int R_eff)
+// update one owned point, sample it if it is a receiver, then add the next
+// step's boundary increment if it lies on the interface line
+template <typename T, bool LF>
+__device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G, const Coef<T>& k,
+                                             int ix, int iz, const T u[3], const T K[3], T rinv,
+                                             const Aux<T, LF>& x)
 {
-    // left column, right column, bottom row (interior cols), top row (interior cols)
-    if (col == 0) return row;
-    if (col == W_eff) return (R + 1) + row;
-    if (row == 0) return 2 * (R + 1) + (col - 1);
-    (void)R_eff;
-    return 2 * (R + 1) + (TW - 1) + (col - 1);
+    const int64_t g = (int64_t)iz * G.nx + ix;
+    const int64_t bi = stacey_index(ix, iz, G.nx, G.nz);
+    T un[3], dn[3], cn[3];
+    if (!LF) {
+        if (bi < 0) {
+            const T mdt2 = k.dt2_Je * rinv * F.wxi[ix] * F.wzi[iz];
+#pragma unroll
+            for (int c = 0; c < 3; c++) un[c] = (-mdt2 * K[c] + (T)2 * u[c]) - x.a[c];
+        } else {
+            const T* p = F.stc + bi * 9;
+#pragma unroll
+            for (int c = 0; c < 3; c++) un[c] = (-p[3 * c] * K[c] + p[3 * c + 1] * u[c]) - p[3 * c + 2] * x.a[c];
+        }
+    } else {
+        if (bi < 0) {
+            const T mdt2 = k.dt2_Je * rinv * F.wxi[ix] * F.wzi[iz];
+#pragma unroll
+            for (int c = 0; c < 3; c++) dn[c] = fma(-mdt2, K[c], x.a[c]);
+        } else {
+            const T* p = F.stc + bi * 9;
+#pragma unroll
+            for (int c = 0; c < 3; c++) dn[c] = p[3 * c + 2] * x.a[c] - p[3 * c] * K[c];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const T y = dn[c] - x.b[c];
+            const T t = u[c] + y;
+            cn[c] = (t - u[c]) - y;
+            un[c] = t;
+        }
+    }
+    // kirrecord_zhl: the field after the update, before the next injection
+    if (F.nrec > 0 && ((__ldg(F.recbits + (g >> 5)) >> (g & 31)) & 1u)) {
+        int lo = 0, hi = F.nrec;
+        while (lo < hi) { const int mdl = (lo + hi) >> 1; if (F.rec_off[mdl] < g) lo = mdl + 1; else hi = mdl; }
+        for (int r = lo; r < F.nrec && F.rec_off[r] == g; r++) {
+            const int t = F.rec_idx[r];
+            F.seis_row[t] = (float)un[0];
+            F.seis_row[F.ntrace + t] = (float)un[1];
+            F.seis_row[2 * F.ntrace + t] = (float)(-un[2]);
+        }
+    }
+    // GRT_Interface4 of the next step (sem2d_psvsh.c:2076-2111)
+    if (F.inject_next && ((iz == G.nbl && ix >= G.nbl) || (ix == G.nbl && iz > G.nbl))) {
+        const double* g1 = F.gnext;
+        const double* g0 = F.gnow;
+        const double* v1 = g1 + F.mtotal;
+        const double* v0 = g0 + F.mtotal;
+        double d3[3];
+        if (iz == G.nbl) {
+            d3[0] = -g0[ix] + g1[ix];
+            d3[1] = -v0[ix] + v1[ix];
+            d3[2] = g0[G.nx + ix] - g1[G.nx + ix];
+        } else {
+            d3[0] = -g0[2 * G.nx + iz] + g1[2 * G.nx + iz];
+            d3[1] = -v0[G.nx + iz] + v1[G.nx + iz];
+            d3[2] = g0[2 * G.nx + G.nz + iz] - g1[2 * G.nx + G.nz + iz];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            if (!LF) {
+                un[c] += (T)d3[c];
+            } else {
+                const T add = (T)d3[c];
+                const T y = add - cn[c];
+                const T t = un[c] + y;
+                cn[c] = (t - un[c]) - y;
+                un[c] = t;
+                dn[c] += add;
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        F.un[c * G.np + g] = un[c];
+        if (LF) { F.dv[c * G.np + g] = dn[c]; F.cc[c * G.np + g] = cn[c]; }
+    }
 }
 
-template <typename T, bool ANISO, bool LF>
-__global__ void __launch_bounds__(128) k_main(Field<T> F, Geo<T> G, Coef<T> k)
+// The SEM step.  CTA = NW warps side by side in x: 6*NW elements, the first
+// one a halo (recomputed, owned by the CTA to the left), so every owned point
+// receives all its element contributions inside the CTA; a band of HZ element
+// rows, plus one halo element row below it whose top-row force is carried
+// into the first owned row.  Warps hand the force of their last column to the
+// next warp through shared memory, once per element row.
+template <typename T, bool ANISO, bool LF, int NW>
+__global__ void __launch_bounds__(NW * 32) k_step(Field<T> F, Geo<T> G, Coef<T> k)
 {
-    const int lane = threadIdx.x & 31;
-    const int tile = blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (tile >= G.ntiles) return;                 // warp-uniform
+    __shared__ T xch[2][NW][N][3];
+    __shared__ T xtop[NW][3];
     const unsigned FULL = 0xffffffffu;
-    const int tx = tile % G.ntx, tz = tile / G.ntx;
-    const int e = lane / NP, al = lane - e * NP;  // lanes 30,31: e = 6
-    const int ex = tx * TEX + e;
-    const int nel = min(TEX, G.nex - tx * TEX);   // elements in this tile
-    const bool live = e < nel;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int cx = blockIdx.x % G.ncx, cz = blockIdx.x / G.ncx;
+    constexpr int S = TEX * NW - 1;                // owned elements per CTA
+    const int e = lane / NP, al = lane - e * NP;   // lanes 30,31: e = 6
+    const int q = TEX * w + e;                     // element within the CTA
+    const int ex = cx * S - 1 + q;
+    const bool live = lane < 30 && ex >= 0 && ex < G.nex;
     const int ix = ex * N + al;
-    const int ez0 = tz * G.HZ, ez1 = min(ez0 + G.HZ, G.nez);
+    const bool own_x = live && q >= 1 && (al < N || ex == G.nex - 1);
+    const int ez0 = cz * G.HZ, ez1 = min(ez0 + G.HZ, G.nez);
+    const int ezs = ez0 > 0 ? ez0 - 1 : 0;
     const int base = e * NP;
-    const int R = G.HZ * N, R_eff = (ez1 - ez0) * N, W_eff = nel * N;
-
-    // x ownership: columns 0..N-1 of each element, column N of the last one
-    const bool own_x = live && (al < N || e == nel - 1);
-    const bool seam_v = own_x && ((al == 0 && e == 0 && ex > 0) || (al == N && ix < G.nx - 1));
+    const bool add_left = al == 0 && (e > 0 || w > 0);
 
     T Dx[NP], DWc[NP];
 #pragma unroll
@@ -217,17 +282,19 @@ __global__ void __launch_bounds__(128) k_main(Field<T> F, Geo<T> G, Coef<T> k)
     T u[NP][3];
     uint16_t m[NP];
     T kc[3] = {0, 0, 0};
+    T rinvN = 0;
 
 #pragma unroll
     for (int b = 0; b < NP; b++) {
-        const int64_t g = (int64_t)(ez0 * N + b) * G.nx + ix;
+        const int64_t g = (int64_t)(ezs * N + b) * G.nx + ix;
 #pragma unroll
         for (int c = 0; c < 3; c++) u[b][c] = live ? F.uc[c * G.np + g] : (T)0;
         m[b] = live ? F.mid[g] : (uint16_t)0;
     }
-
-    for (int ez = ez0; ez < ez1; ++ez) {
-        if (ez > ez0) {
+    int par = 0;
+    for (int ez = ezs; ez < ez1; ++ez) {
+        const bool halo = ez < ez0;
+        if (ez > ezs) {
 #pragma unroll
             for (int c = 0; c < 3; c++) u[0][c] = u[N][c];
             m[0] = m[N];
@@ -238,6 +305,11 @@ __global__ void __launch_bounds__(128) k_main(Field<T> F, Geo<T> G, Coef<T> k)
                 for (int c = 0; c < 3; c++) u[b][c] = live ? F.uc[c * G.np + g] : (T)0;
                 m[b] = live ? F.mid[g] : (uint16_t)0;
             }
+        }
+        Aux<T, LF> aux[N];
+        if (!halo && own_x) {
+#pragma unroll
+            for (int b = 0; b < N; b++) load_aux<T, LF>(F, G.np, (int64_t)(ez * N + b) * G.nx + ix, aux[b]);
         }
         T item0[NP][3], F2[NP][3];
         T rinv[NP];
@@ -279,79 +351,59 @@ __global__ void __launch_bounds__(128) k_main(Field<T> F, Geo<T> G, Coef<T> k)
                 T s = 0;
 #pragma unroll
                 for (int bb = 0; bb < NP; bb++) s = fma(F2[bb][c], k.DW[bb * NP + b], s);
-                kk[b][c] = (item0[b][c] * k.w[b] + s * wal) * k.Je;
+                kk[b][c] = live ? (item0[b][c] * k.w[b] + s * wal) * k.Je : (T)0;
             }
-        if (ez > ez0) {
+        if (ez > ezs) {
 #pragma unroll
             for (int c = 0; c < 3; c++) kk[0][c] = kc[c] + kk[0][c];
         }
 #pragma unroll
         for (int c = 0; c < 3; c++) kc[c] = kk[N][c];
-
+        rinvN = rinv[N];
+        if (!halo) {
+            // the last column of each warp goes to the next warp
+            if (lane == 29) {
 #pragma unroll
-        for (int b = 0; b < N; b++) {
-            T kt[3];
+                for (int b = 0; b < N; b++)
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-                const T left = __shfl_up_sync(FULL, kk[b][c], 1);
-                kt[c] = (al == 0 && e > 0) ? left + kk[b][c] : kk[b][c];
+                    for (int c = 0; c < 3; c++) xch[par][w][b][c] = kk[b][c];
             }
-            if (own_x) {
-                const int iz = ez * N + b;
-                const bool seam_h = (b == 0 && ez == ez0 && ez0 > 0);
-                if (seam_v || seam_h) {
-                    const int pos = perim_pos(ix - tx * TW, iz - tz * R, W_eff, R, R_eff);
-                    T* p = F.perim + ((int64_t)tile * G.pstride + pos) * 3;
-                    p[0] = kt[0]; p[1] = kt[1]; p[2] = kt[2];
-                } else {
-                    update_point<T, LF>(F, G, k, ix, iz, u[b], kt, rinv[b]);
+            __syncthreads();
+#pragma unroll
+            for (int b = 0; b < N; b++) {
+                T kt[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    T left = __shfl_up_sync(FULL, kk[b][c], 1);
+                    if (e == 0) left = w > 0 ? xch[par][w > 0 ? w - 1 : 0][b][c] : (T)0;
+                    kt[c] = add_left ? left + kk[b][c] : kk[b][c];
                 }
+                if (own_x) finish_point<T, LF>(F, G, k, ix, ez * N + b, u[b], kt, rinv[b], aux[b]);
             }
-        }
-        if (ez == ez1 - 1) {
-            // top row of the tile: the domain's top row, or a seam with the tile above
-            T kt[3];
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                const T left = __shfl_up_sync(FULL, kc[c], 1);
-                kt[c] = (al == 0 && e > 0) ? left + kc[c] : kc[c];
-            }
-            if (own_x) {
-                const int iz = ez1 * N;
-                if (ez1 < G.nez || seam_v) {
-                    const int pos = perim_pos(ix - tx * TW, iz - tz * R, W_eff, R, R_eff);
-                    T* p = F.perim + ((int64_t)tile * G.pstride + pos) * 3;
-                    p[0] = kt[0]; p[1] = kt[1]; p[2] = kt[2];
-                } else {
-                    update_point<T, LF>(F, G, k, ix, iz, u[N], kt, rinv[N]);
-                }
-            }
+            par ^= 1;
         }
     }
-}
-
-// points shared by warp tiles: sum the perimeter partials in a fixed order, then update
-struct SeamPt { int32_t ix, iz; int32_t ref[4]; };
-
-template <typename T, bool LF>
-__global__ void __launch_bounds__(256) k_seam(Field<T> F, Geo<T> G, Coef<T> k, const SeamPt* __restrict__ pts, int npts)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= npts) return;
-    const SeamPt s = pts[i];
-    T K[3] = {0, 0, 0};
+    if (ez1 == G.nez) {
+        // the domain's top row: no element above, complete now
+        if (lane == 29) {
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
-        if (s.ref[r] < 0) break;
-        const T* p = F.perim + (int64_t)s.ref[r] * 3;
-        K[0] += p[0]; K[1] += p[1]; K[2] += p[2];
+            for (int c = 0; c < 3; c++) xtop[w][c] = kc[c];
+        }
+        __syncthreads();
+        T kt[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            T left = __shfl_up_sync(FULL, kc[c], 1);
+            if (e == 0) left = w > 0 ? xtop[w > 0 ? w - 1 : 0][c] : (T)0;
+            kt[c] = add_left ? left + kc[c] : kc[c];
+        }
+        if (own_x) {
+            const int iz = G.nz - 1;
+            Aux<T, LF> x;
+            load_aux<T, LF>(F, G.np, (int64_t)iz * G.nx + ix, x);
+            finish_point<T, LF>(F, G, k, ix, iz, u[N], kt, rinvN, x);
+        }
     }
-    const int64_t g = (int64_t)s.iz * G.nx + s.ix;
-    T u[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) u[c] = F.uc[c * G.np + g];
-    const T rinv = __ldg(F.mat + (size_t)F.mid[g] * MAT_STRIDE + 15);
-    update_point<T, LF>(F, G, k, s.ix, s.iz, u, K, rinv);
 }
 
 // Boundary-trace interpolation for a chunk of steps (interpl.c:16-54): row r of

@@ -42,9 +42,8 @@ struct sks_solver {
     int step;                  // next step to take
     int64_t launches;
     cudaStream_t stream;
-    // geometry
-    int ntx, ntz, HZ, ntiles, pstride;
-    int nseam;
+    // geometry: CTA grid of the step kernel
+    int NW, ncx, ncz, HZ, nblocks;
     int nbl;
     // device buffers
     void* U[2];                // displacement buffers, [3][np] each
@@ -55,9 +54,11 @@ struct sks_solver {
     void* wxi;
     void* wzi;
     void* stc;                 // Stacey coefficients
-    void* perim;
-    SeamPt* seams;
-    int64_t* rec_off;
+    int64_t* rec_off;          // per trace (step-0 recording)
+    uint32_t* recbits;         // receiver bitmap over points
+    int64_t* rec_sorted;       // receiver offsets, sorted
+    int32_t* rec_idx;          // trace index of each sorted offset
+    int nrec_in;               // receivers inside the mesh (offset < np)
     float* seis;               // [chunk][3][ntrace]
     double* G;                 // [(chunk+1)][mtotal+shtotal]
     float* rec_psv;            // boundary records
@@ -180,13 +181,14 @@ int dmalloc(sks_solver* s, T** p, size_t n)
 
 void free_device(sks_solver* s)
 {
-    void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->wxi, s->wzi, s->stc, s->perim,
-                  s->seams, s->rec_off, s->seis, s->G, s->rec_psv, s->rec_sh, s->tap_psv, s->tap_sh,
-                  s->w_psv, s->w_sh};
+    void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->wxi, s->wzi, s->stc,
+                  s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seis, s->G, s->rec_psv, s->rec_sh,
+                  s->tap_psv, s->tap_sh, s->w_psv, s->w_sh};
     for (void* p : ps)
         if (p) cudaFree(p);
-    s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->wxi = s->wzi = s->stc = s->perim = nullptr;
-    s->mid = nullptr; s->seams = nullptr; s->rec_off = nullptr; s->seis = nullptr; s->G = nullptr;
+    s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->wxi = s->wzi = s->stc = nullptr;
+    s->mid = nullptr; s->rec_off = nullptr; s->recbits = nullptr; s->rec_sorted = nullptr; s->rec_idx = nullptr;
+    s->seis = nullptr; s->G = nullptr;
     s->rec_psv = s->rec_sh = nullptr; s->tap_psv = s->tap_sh = nullptr; s->w_psv = s->w_sh = nullptr;
 }
 
@@ -227,59 +229,19 @@ int collect_timing(sks_solver* s)
     return SKS_OK;
 }
 
-int pick_hz(const sks_model& m, int sm_count)
+// CTA band height: at least ~4 resident CTAs' worth of work per SM for the
+// grid, and bands as tall as that allows (each band recomputes one element
+// row below it)
+int pick_band(const sks_model& m, int ncx, int sm_count)
 {
-    // enough warp tiles to give every SM >= 16 warps, and runs as long as possible
-    const int ntx = (m.nex + TEX - 1) / TEX;
-    const int target = sm_count * 16;
-    const int cands[] = {32, 24, 16, 12, 10, 8, 6, 5, 4, 3, 2, 1};
+    const int64_t target = (int64_t)sm_count * 4;
+    const int cands[] = {32, 24, 16, 12, 10, 8, 6, 4, 3, 2};
     for (int hz : cands) {
-        const int ntz = (m.nez + hz - 1) / hz;
-        if ((int64_t)ntx * ntz >= target) return std::min(hz, m.nez);
+        if (hz > m.nez) continue;
+        const int ncz = (m.nez + hz - 1) / hz;
+        if ((int64_t)ncx * ncz >= target) return hz;
     }
-    return 1;
-}
-
-// perimeter position of local (col,row) in a tile, same rule as perim_pos()
-int host_perim_pos(int col, int row, int W_eff, int R)
-{
-    if (col == 0) return row;
-    if (col == W_eff) return (R + 1) + row;
-    if (row == 0) return 2 * (R + 1) + (col - 1);
-    return 2 * (R + 1) + (TW - 1) + (col - 1);
-}
-
-void build_seams(const sks_solver* s, std::vector<SeamPt>& out)
-{
-    const sks_model& m = s->m;
-    const int R = s->HZ * N;
-    out.clear();
-    auto tile_W = [&](int tx) { return std::min(TEX, m.nex - tx * TEX) * N; };
-    for (int iz = 0; iz < m.nz; iz++) {
-        const bool hs = (iz % R == 0) && iz > 0 && iz < m.nz - 1;
-        for (int ix = 0; ix < m.nx; ix++) {
-            const bool vs = (ix % TW == 0) && ix > 0 && ix < m.nx - 1;
-            if (!vs && !hs) continue;
-            SeamPt p;
-            p.ix = ix; p.iz = iz;
-            int nref = 0;
-            // tiles containing the point, in order (tx-1,tz-1) (tx-1,tz) (tx,tz-1) (tx,tz)
-            int txs[2], ntxs = 0, tzs[2], ntzs = 0;
-            if (vs) { txs[ntxs++] = ix / TW - 1; txs[ntxs++] = ix / TW; }
-            else { int tx = ix / TW; if (tx >= s->ntx) tx = s->ntx - 1; txs[ntxs++] = tx; }
-            if (hs) { tzs[ntzs++] = iz / R - 1; tzs[ntzs++] = iz / R; }
-            else { int tz = iz / R; if (tz >= s->ntz) tz = s->ntz - 1; tzs[ntzs++] = tz; }
-            for (int a = 0; a < ntxs; a++)
-                for (int b = 0; b < ntzs; b++) {
-                    const int tx = txs[a], tz = tzs[b];
-                    const int tile = tz * s->ntx + tx;
-                    const int col = ix - tx * TW, row = iz - tz * R;
-                    p.ref[nref++] = tile * s->pstride + host_perim_pos(col, row, tile_W(tx), R);
-                }
-            for (int r = nref; r < 4; r++) p.ref[r] = -1;
-            out.push_back(p);
-        }
-    }
+    return std::max(1, std::min(2, m.nez));
 }
 
 template <typename T>
@@ -354,9 +316,6 @@ int upload_tables(sks_solver* s)
         if ((rc = dmalloc(s, &cc, 3 * np))) return rc;
         s->Cc = cc;
     }
-    T* pr;
-    if ((rc = dmalloc(s, &pr, (size_t)s->ntiles * s->pstride * 3))) return rc;
-    s->perim = pr;
     return SKS_OK;
 }
 
@@ -380,6 +339,7 @@ template <typename T>
 Field<T> make_field(sks_solver* s)
 {
     Field<T> F;
+    memset(&F, 0, sizeof F);
     F.uc = (const T*)s->U[s->cur];
     F.un = (T*)s->U[1 - s->cur];
     F.dv = (T*)s->Dv;
@@ -389,7 +349,12 @@ Field<T> make_field(sks_solver* s)
     F.wxi = (const T*)s->wxi;
     F.wzi = (const T*)s->wzi;
     F.stc = (const T*)s->stc;
-    F.perim = (T*)s->perim;
+    F.mtotal = s->m.mtotal;
+    F.recbits = s->recbits;
+    F.rec_off = s->rec_sorted;
+    F.rec_idx = s->rec_idx;
+    F.nrec = s->nrec_in;
+    F.ntrace = s->m.ntrace;
     return F;
 }
 
@@ -398,49 +363,47 @@ Geo<T> make_geo(const sks_solver* s)
 {
     Geo<T> G;
     G.nex = s->m.nex; G.nez = s->m.nez; G.nx = s->m.nx; G.nz = s->m.nz;
-    G.ntx = s->ntx; G.ntz = s->ntz; G.HZ = s->HZ; G.ntiles = s->ntiles;
-    G.pstride = s->pstride;
+    G.ncx = s->ncx; G.ncz = s->ncz; G.HZ = s->HZ; G.nblocks = s->nblocks;
+    G.nbl = s->nbl;
     G.np = (int64_t)s->m.nx * s->m.nz;
     return G;
 }
 
-// one time step it >= 1 (injection, fused element/update kernel, seams, record)
+template <typename T, bool ANISO, bool LF>
+void launch_step(sks_solver* s, const Field<T>& F, const Geo<T>& G, const Coef<T>& k)
+{
+    switch (s->NW) {
+    case 2: k_step<T, ANISO, LF, 2><<<s->nblocks, 64, 0, s->stream>>>(F, G, k); break;
+    case 8: k_step<T, ANISO, LF, 8><<<s->nblocks, 256, 0, s->stream>>>(F, G, k); break;
+    default: k_step<T, ANISO, LF, 4><<<s->nblocks, 128, 0, s->stream>>>(F, G, k); break;
+    }
+}
+
+// one time step it >= 1: a single fused kernel (force, assembly, update,
+// receivers, and the boundary increment of step it+1)
 template <typename T, bool LF>
-int step_impl(sks_solver* s, int it, const double* Gcur, const double* Gprev, float* seis_row)
+int step_impl(sks_solver* s, int it, const double* Gcur, const double* Gnext, float* seis_row)
 {
     const sks_model& m = s->m;
-    const int64_t np = (int64_t)m.nx * m.nz;
-    cudaStream_t st = s->stream;
-    if (it < m.nt_sem) {
-        const int n = (m.nx - s->nbl) + (m.nz - s->nbl - 1);
-        KTimer t(s, SKS_KC_INJECT);
-        k_inject<T, LF><<<(n + 255) / 256, 256, 0, st>>>((T*)s->U[s->cur], (T*)s->Dv, (T*)s->Cc, np, m.nx, m.nz,
-                                                         s->nbl, Gcur, Gprev, m.mtotal);
-    }
     Field<T> F = make_field<T>(s);
+    F.gnow = Gcur;
+    F.gnext = Gnext;
+    F.inject_next = (it + 1 < m.nt_sem) ? 1 : 0;
+    F.seis_row = seis_row;
     Geo<T> G = make_geo<T>(s);
     static thread_local Coef<T> k;
     k = make_coef<T>(m);
-    const int blocks = (s->ntiles + 3) / 4;
     {
         KTimer t(s, SKS_KC_ELEMENT);
-        if (m.anisotropic) k_main<T, true, LF><<<blocks, 128, 0, st>>>(F, G, k);
-        else k_main<T, false, LF><<<blocks, 128, 0, st>>>(F, G, k);
-    }
-    if (s->nseam > 0) {
-        KTimer t(s, SKS_KC_SEAM);
-        k_seam<T, LF><<<(s->nseam + 255) / 256, 256, 0, st>>>(F, G, k, s->seams, s->nseam);
+        if (m.anisotropic) launch_step<T, true, LF>(s, F, G, k);
+        else launch_step<T, false, LF>(s, F, G, k);
     }
     s->cur = 1 - s->cur;
-    if (m.ntrace > 0) {
-        KTimer t(s, SKS_KC_RECORD);
-        k_record<T><<<(m.ntrace + 127) / 128, 128, 0, st>>>((const T*)s->U[s->cur], np, s->rec_off, m.ntrace, seis_row);
-    }
     return SKS_OK;
 }
 
 template <typename T, bool LF>
-int step0_impl(sks_solver* s, const double* G0, float* seis_row)
+int step0_impl(sks_solver* s, const double* G0, const double* G1, float* seis_row)
 {
     const sks_model& m = s->m;
     const int64_t np = (int64_t)m.nx * m.nz;
@@ -461,6 +424,12 @@ int step0_impl(sks_solver* s, const double* G0, float* seis_row)
         KTimer t(s, SKS_KC_RECORD);
         k_record<T><<<(m.ntrace + 127) / 128, 128, 0, st>>>((const T*)s->U[0], np, s->rec_off, m.ntrace, seis_row);
     }
+    if (m.nt_sem > 1) {   // step 1's GRT_Interface4, applied to the step-0 field
+        const int n = (m.nx - s->nbl) + (m.nz - s->nbl - 1);
+        KTimer t(s, SKS_KC_INJECT);
+        k_inject<T, LF><<<(n + 255) / 256, 256, 0, st>>>((T*)s->U[0], (T*)s->Dv, (T*)s->Cc, np, m.nx, m.nz,
+                                                         s->nbl, G1, G0, m.mtotal);
+    }
     return SKS_OK;
 }
 
@@ -469,8 +438,9 @@ int run_chunk(sks_solver* s, int it0, int n)
     const sks_model& m = s->m;
     const int L = m.mtotal + m.shtotal;
     cudaStream_t st = s->stream;
-    // interpolated boundary traces for the injecting steps of this chunk
-    const int ni = std::max(0, std::min(it0 + n, m.nt_sem) - it0);
+    // G row r holds the interpolated traces of step it0-1+r; a step it needs
+    // rows of it and it+1, so the chunk interpolates steps [it0, it0+n]
+    const int ni = std::max(0, std::min(it0 + n + 1, m.nt_sem) - it0);
     if (ni > 0) {
         if (it0 > 0 && s->g_last > 0)
             CK(cudaMemcpyAsync(s->G, s->G + (size_t)s->g_last * L, sizeof(double) * L, cudaMemcpyDeviceToDevice, st));
@@ -479,18 +449,19 @@ int run_chunk(sks_solver* s, int it0, int n)
             k_interp<<<ni, 256, 0, st>>>(s->G, L, it0, ni, s->rec_psv, m.mtotal, s->rec_sh, m.shtotal,
                                          s->tap_psv, s->w_psv, s->tap_sh, s->w_sh);
         }
-        s->g_last = ni;
+        s->g_last = n;     // row of step it0+n-1: the previous step of the next chunk
     }
+    if (m.ntrace > 0) CK(cudaMemsetAsync(s->seis, 0, sizeof(float) * (size_t)n * 3 * m.ntrace, st));
     for (int i = 0; i < n; i++) {
         const int it = it0 + i;
         const double* Gcur = s->G + (size_t)(i + 1) * L;
-        const double* Gprev = s->G + (size_t)i * L;
+        const double* Gnext = s->G + (size_t)(i + 2) * L;
         float* row = s->seis + (size_t)i * 3 * m.ntrace;
         int rc;
         if (s->precision == SKS_FP64) {
-            rc = it == 0 ? step0_impl<double, false>(s, Gcur, row) : step_impl<double, false>(s, it, Gcur, Gprev, row);
+            rc = it == 0 ? step0_impl<double, false>(s, Gcur, Gnext, row) : step_impl<double, false>(s, it, Gcur, Gnext, row);
         } else {
-            rc = it == 0 ? step0_impl<float, true>(s, Gcur, row) : step_impl<float, true>(s, it, Gcur, Gprev, row);
+            rc = it == 0 ? step0_impl<float, true>(s, Gcur, Gnext, row) : step_impl<float, true>(s, it, Gcur, Gnext, row);
         }
         if (rc) return rc;
     }
@@ -523,11 +494,11 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     ce = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (ce != cudaSuccess) { sks_model_free(&s->m); delete s; return set_err(SKS_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(ce)); }
-    s->HZ = pick_hz(m, sms);
-    s->ntx = (m.nex + TEX - 1) / TEX;
-    s->ntz = (m.nez + s->HZ - 1) / s->HZ;
-    s->ntiles = s->ntx * s->ntz;
-    s->pstride = 2 * (s->HZ * N + 1) + 2 * (TW - 1);
+    s->NW = 4;
+    s->ncx = (m.nex + (TEX * s->NW - 1) - 1) / (TEX * s->NW - 1);
+    s->HZ = pick_band(m, s->ncx, sms);
+    s->ncz = (m.nez + s->HZ - 1) / s->HZ;
+    s->nblocks = s->ncx * s->ncz;
     s->chunk = 64;
     const size_t np = (size_t)m.nx * m.nz;
     rc = precision == SKS_FP64 ? upload_tables<double>(s) : upload_tables<float>(s);
@@ -536,14 +507,29 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         ce = cudaMemcpy(s->mid, m.mat_id, np * sizeof(uint16_t), cudaMemcpyHostToDevice);
         if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "upload of material indices: %s", cudaGetErrorString(ce));
     }
-    std::vector<SeamPt> seams;
-    if (!rc) {
-        build_seams(s, seams);
-        s->nseam = (int)seams.size();
-        rc = dmalloc(s, &s->seams, seams.size());
-        if (!rc && !seams.empty()) {
-            ce = cudaMemcpy(s->seams, seams.data(), seams.size() * sizeof(SeamPt), cudaMemcpyHostToDevice);
-            if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "upload of seam list: %s", cudaGetErrorString(ce));
+    if (!rc && m.ntrace > 0) {
+        // receivers inside the mesh, sorted by point, and a bitmap of their points
+        std::vector<std::pair<int64_t, int32_t>> rs;
+        for (int i = 0; i < m.ntrace; i++)
+            if (m.rec_off[i] < (int64_t)np) rs.push_back({m.rec_off[i], i});
+        std::sort(rs.begin(), rs.end());
+        s->nrec_in = (int)rs.size();
+        std::vector<int64_t> off(rs.size());
+        std::vector<int32_t> idx(rs.size());
+        std::vector<uint32_t> bits((np + 31) / 32, 0u);
+        for (size_t i = 0; i < rs.size(); i++) {
+            off[i] = rs[i].first; idx[i] = rs[i].second;
+            bits[rs[i].first >> 5] |= 1u << (rs[i].first & 31);
+        }
+        rc = dmalloc(s, &s->recbits, bits.size());
+        if (!rc) rc = dmalloc(s, &s->rec_sorted, std::max<size_t>(1, off.size()));
+        if (!rc) rc = dmalloc(s, &s->rec_idx, std::max<size_t>(1, idx.size()));
+        if (!rc) {
+            cudaMemcpy(s->recbits, bits.data(), bits.size() * 4, cudaMemcpyHostToDevice);
+            if (!off.empty()) cudaMemcpy(s->rec_sorted, off.data(), off.size() * 8, cudaMemcpyHostToDevice);
+            if (!idx.empty()) ce = cudaMemcpy(s->rec_idx, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice);
+            else ce = cudaSuccess;
+            if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "upload of receivers: %s", cudaGetErrorString(ce));
         }
     }
     if (!rc) rc = dmalloc(s, &s->rec_off, std::max(1, m.ntrace));
@@ -552,7 +538,7 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "upload of receivers: %s", cudaGetErrorString(ce));
     }
     if (!rc) rc = dmalloc(s, &s->seis, (size_t)s->chunk * 3 * std::max(1, m.ntrace));
-    if (!rc) rc = dmalloc(s, &s->G, (size_t)(s->chunk + 1) * (m.mtotal + m.shtotal));
+    if (!rc) rc = dmalloc(s, &s->G, (size_t)(s->chunk + 2) * (m.mtotal + m.shtotal));
     if (!rc && m.nt_sem > 0) {
         rc = dmalloc(s, &s->tap_psv, 4 * (size_t)m.nt_sem);
         if (!rc) rc = dmalloc(s, &s->tap_sh, 4 * (size_t)m.nt_sem);
@@ -700,7 +686,7 @@ extern "C" int sks_get_info(const sks_solver* s, sks_info_t* info)
     info->precision = s->precision;
     info->step = s->step;
     info->device_bytes = s->device_bytes;
-    info->seam_points = s->nseam;
+    info->seam_points = 0;
     info->tile_rows = s->HZ;
     return SKS_OK;
 }
