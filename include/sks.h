@@ -134,6 +134,28 @@ void sks_setup_close(sks_setup *su);
  * and on failure. */
 int sks_open_setup(sks_setup *su, int precision, int device, sks_solver **out);
 
+/* ---- tuning -------------------------------------------------------------
+ * The step kernel runs one CTA per (column of 6*W-1 elements, band of B
+ * element rows); each CTA recomputes one element column and one element row
+ * of halo.  W (warps per CTA), B and a prefetch variant are tunable; the
+ * default comes from the mesh size and the SM count. */
+typedef struct {
+    int32_t warps_per_block;      /* 2, 4 or 8                              */
+    int32_t band_rows;            /* element rows per CTA band              */
+    int32_t prefetch;             /* 1: load the next element row early     */
+    int32_t blocks;               /* CTAs per step (output)                 */
+    float   ms_per_step;          /* measured by sks_autotune (output)      */
+} sks_tuning_t;
+
+int sks_set_tuning(sks_solver *s, const sks_tuning_t *t);
+int sks_get_tuning(const sks_solver *s, sks_tuning_t *t);
+
+/* Times every candidate tuning on `steps` steps of this solve (CUDA events
+ * on the solver's stream), keeps the fastest, and leaves the solve where it
+ * was: the wavefield, step counter and boundary state are saved before and
+ * restored after.  Needs steps+1 steps left in the run. */
+int sks_autotune(sks_solver *s, int32_t steps, sks_tuning_t *best);
+
 /* ---- instrumentation --------------------------------------------------
  * Kernel launches issued by sks_run() so far. */
 int64_t sks_kernel_launches(const sks_solver *s);

@@ -254,7 +254,7 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
 // rows, plus one halo element row below it whose top-row force is carried
 // into the first owned row.  Warps hand the force of their last column to the
 // next warp through shared memory, once per element row.
-template <typename T, bool ANISO, bool LF, int NW>
+template <typename T, bool ANISO, bool LF, int NW, bool PF>
 __global__ void __launch_bounds__(NW * 32) k_step(Field<T> F, Geo<T> G, Coef<T> k)
 {
     __shared__ T xch[2][NW][N][3];
@@ -267,12 +267,17 @@ __global__ void __launch_bounds__(NW * 32) k_step(Field<T> F, Geo<T> G, Coef<T> 
     const int q = TEX * w + e;                     // element within the CTA
     const int ex = cx * S - 1 + q;
     const bool live = lane < 30 && ex >= 0 && ex < G.nex;
-    const int ix = ex * N + al;
+    const int ix = live ? ex * N + al : 0;
     const bool own_x = live && q >= 1 && (al < N || ex == G.nex - 1);
     const int ez0 = cz * G.HZ, ez1 = min(ez0 + G.HZ, G.nez);
     const int ezs = ez0 > 0 ? ez0 - 1 : 0;
     const int base = e * NP;
     const bool add_left = al == 0 && (e > 0 || w > 0);
+    const int nx = G.nx;
+    const int np = (int)G.np;                      // < 2^31 (checked on the host)
+    const T* __restrict__ U0 = F.uc;
+    const T* __restrict__ U1 = F.uc + np;
+    const T* __restrict__ U2 = F.uc + 2 * np;
 
     T Dx[NP], DWc[NP];
 #pragma unroll
@@ -281,15 +286,34 @@ __global__ void __launch_bounds__(NW * 32) k_step(Field<T> F, Geo<T> G, Coef<T> 
 
     T u[NP][3];
     uint16_t m[NP];
+    T un_[N][3];                 // next element row, rows 1..N (prefetch)
+    uint16_t mn[N];
     T kc[3] = {0, 0, 0};
     T rinvN = 0;
+    MatRow<T, ANISO> M;
+    int mcur = -1;
 
+    {
+        const int o = ezs * N * nx + ix;
 #pragma unroll
-    for (int b = 0; b < NP; b++) {
-        const int64_t g = (int64_t)(ezs * N + b) * G.nx + ix;
+        for (int b = 0; b < NP; b++) {
+            const int g = o + b * nx;
+            u[b][0] = live ? U0[g] : (T)0;
+            u[b][1] = live ? U1[g] : (T)0;
+            u[b][2] = live ? U2[g] : (T)0;
+            m[b] = live ? F.mid[g] : (uint16_t)0;
+        }
+    }
+    if (PF && ezs + 1 < ez1) {
+        const int o = (ezs + 1) * N * nx + ix;
 #pragma unroll
-        for (int c = 0; c < 3; c++) u[b][c] = live ? F.uc[c * G.np + g] : (T)0;
-        m[b] = live ? F.mid[g] : (uint16_t)0;
+        for (int b = 0; b < N; b++) {
+            const int g = o + (b + 1) * nx;
+            un_[b][0] = live ? U0[g] : (T)0;
+            un_[b][1] = live ? U1[g] : (T)0;
+            un_[b][2] = live ? U2[g] : (T)0;
+            mn[b] = live ? F.mid[g] : (uint16_t)0;
+        }
     }
     int par = 0;
     for (int ez = ezs; ez < ez1; ++ez) {
@@ -298,18 +322,40 @@ __global__ void __launch_bounds__(NW * 32) k_step(Field<T> F, Geo<T> G, Coef<T> 
 #pragma unroll
             for (int c = 0; c < 3; c++) u[0][c] = u[N][c];
             m[0] = m[N];
+            if (PF) {
 #pragma unroll
-            for (int b = 1; b < NP; b++) {
-                const int64_t g = (int64_t)(ez * N + b) * G.nx + ix;
+                for (int b = 0; b < N; b++) {
 #pragma unroll
-                for (int c = 0; c < 3; c++) u[b][c] = live ? F.uc[c * G.np + g] : (T)0;
-                m[b] = live ? F.mid[g] : (uint16_t)0;
+                    for (int c = 0; c < 3; c++) u[b + 1][c] = un_[b][c];
+                    m[b + 1] = mn[b];
+                }
+            } else {
+                const int o = ez * N * nx + ix;
+#pragma unroll
+                for (int b = 1; b < NP; b++) {
+                    const int g = o + b * nx;
+                    u[b][0] = live ? U0[g] : (T)0;
+                    u[b][1] = live ? U1[g] : (T)0;
+                    u[b][2] = live ? U2[g] : (T)0;
+                    m[b] = live ? F.mid[g] : (uint16_t)0;
+                }
+            }
+        }
+        if (PF && ez + 1 < ez1) {
+            const int o = (ez + 1) * N * nx + ix;
+#pragma unroll
+            for (int b = 0; b < N; b++) {
+                const int g = o + (b + 1) * nx;
+                un_[b][0] = live ? U0[g] : (T)0;
+                un_[b][1] = live ? U1[g] : (T)0;
+                un_[b][2] = live ? U2[g] : (T)0;
+                mn[b] = live ? F.mid[g] : (uint16_t)0;
             }
         }
         Aux<T, LF> aux[N];
         if (!halo && own_x) {
 #pragma unroll
-            for (int b = 0; b < N; b++) load_aux<T, LF>(F, G.np, (int64_t)(ez * N + b) * G.nx + ix, aux[b]);
+            for (int b = 0; b < N; b++) load_aux<T, LF>(F, G.np, (int64_t)(ez * N + b) * nx + ix, aux[b]);
         }
         T item0[NP][3], F2[NP][3];
         T rinv[NP];
@@ -328,8 +374,10 @@ __global__ void __launch_bounds__(NW * 32) k_step(Field<T> F, Geo<T> G, Coef<T> 
                 dz[c] = z;
             }
             const T ee[5] = {dx[0], dx[1], dx[2] + dz[0], dz[1], dz[2]};
-            MatRow<T, ANISO> M;
-            M.load(F.mat + (size_t)m[b] * MAT_STRIDE);
+            if ((int)m[b] != mcur) {                 // layered models: rarely taken
+                M.load(F.mat + (size_t)m[b] * MAT_STRIDE);
+                mcur = m[b];
+            }
             rinv[b] = M.s[15];
             T sg[5];
             stress<T, ANISO>(M, ee, sg);
@@ -400,7 +448,7 @@ __global__ void __launch_bounds__(NW * 32) k_step(Field<T> F, Geo<T> G, Coef<T> 
         if (own_x) {
             const int iz = G.nz - 1;
             Aux<T, LF> x;
-            load_aux<T, LF>(F, G.np, (int64_t)iz * G.nx + ix, x);
+            load_aux<T, LF>(F, G.np, (int64_t)iz * nx + ix, x);
             finish_point<T, LF>(F, G, k, ix, iz, u[N], kt, rinvN, x);
         }
     }

@@ -42,8 +42,9 @@ struct sks_solver {
     int step;                  // next step to take
     int64_t launches;
     cudaStream_t stream;
-    // geometry: CTA grid of the step kernel
-    int NW, ncx, ncz, HZ, nblocks;
+    // geometry: CTA grid of the step kernel (tunable)
+    int NW, ncx, ncz, HZ, nblocks, PF;
+    int sms;
     int nbl;
     // device buffers
     void* U[2];                // displacement buffers, [3][np] each
@@ -369,14 +370,32 @@ Geo<T> make_geo(const sks_solver* s)
     return G;
 }
 
+template <typename T, bool ANISO, bool LF, bool PF>
+void launch_step_pf(sks_solver* s, const Field<T>& F, const Geo<T>& G, const Coef<T>& k)
+{
+    switch (s->NW) {
+    case 2: k_step<T, ANISO, LF, 2, PF><<<s->nblocks, 64, 0, s->stream>>>(F, G, k); break;
+    case 8: k_step<T, ANISO, LF, 8, PF><<<s->nblocks, 256, 0, s->stream>>>(F, G, k); break;
+    default: k_step<T, ANISO, LF, 4, PF><<<s->nblocks, 128, 0, s->stream>>>(F, G, k); break;
+    }
+}
+
 template <typename T, bool ANISO, bool LF>
 void launch_step(sks_solver* s, const Field<T>& F, const Geo<T>& G, const Coef<T>& k)
 {
-    switch (s->NW) {
-    case 2: k_step<T, ANISO, LF, 2><<<s->nblocks, 64, 0, s->stream>>>(F, G, k); break;
-    case 8: k_step<T, ANISO, LF, 8><<<s->nblocks, 256, 0, s->stream>>>(F, G, k); break;
-    default: k_step<T, ANISO, LF, 4><<<s->nblocks, 128, 0, s->stream>>>(F, G, k); break;
-    }
+    if (s->PF) launch_step_pf<T, ANISO, LF, true>(s, F, G, k);
+    else launch_step_pf<T, ANISO, LF, false>(s, F, G, k);
+}
+
+// CTA grid for a tuning: NW warps (6*NW-1 owned elements) by bands of HZ rows
+void set_grid(sks_solver* s, int NW, int HZ, int PF)
+{
+    s->NW = NW;
+    s->PF = PF;
+    s->ncx = (s->m.nex + (TEX * NW - 1) - 1) / (TEX * NW - 1);
+    s->HZ = std::max(1, std::min(HZ, s->m.nez));
+    s->ncz = (s->m.nez + s->HZ - 1) / s->HZ;
+    s->nblocks = s->ncx * s->ncz;
 }
 
 // one time step it >= 1: a single fused kernel (force, assembly, update,
@@ -494,11 +513,15 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     ce = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (ce != cudaSuccess) { sks_model_free(&s->m); delete s; return set_err(SKS_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(ce)); }
-    s->NW = 4;
-    s->ncx = (m.nex + (TEX * s->NW - 1) - 1) / (TEX * s->NW - 1);
-    s->HZ = pick_band(m, s->ncx, sms);
-    s->ncz = (m.nez + s->HZ - 1) / s->HZ;
-    s->nblocks = s->ncx * s->ncz;
+    s->sms = sms;
+    if ((int64_t)m.nx * m.nz * 3 >= ((int64_t)1 << 31)) {
+        free_device(s); cudaStreamDestroy(s->stream); sks_model_free(&s->m); delete s;
+        return set_err(SKS_ERR_UNSUPPORTED, "mesh of %d x %d points: 3*nx*nz must stay below 2^31", m.nx, m.nz);
+    }
+    {
+        const int ncx4 = (m.nex + (TEX * 4 - 1) - 1) / (TEX * 4 - 1);
+        set_grid(s, 4, pick_band(m, ncx4, sms), 1);
+    }
     s->chunk = 64;
     const size_t np = (size_t)m.nx * m.nz;
     rc = precision == SKS_FP64 ? upload_tables<double>(s) : upload_tables<float>(s);
@@ -724,5 +747,110 @@ extern "C" int sks_kernel_timing(const sks_solver* s, double* ms, int64_t* count
         if (ms) ms[i] = s->kms[i];
         if (count) count[i] = s->kcount[i];
     }
+    return SKS_OK;
+}
+
+extern "C" int sks_set_tuning(sks_solver* s, const sks_tuning_t* t)
+{
+    if (!s || !t) return set_err(SKS_ERR_ARG, "NULL argument");
+    if (t->warps_per_block != 2 && t->warps_per_block != 4 && t->warps_per_block != 8)
+        return set_err(SKS_ERR_ARG, "warps_per_block=%d: 2, 4 or 8", t->warps_per_block);
+    if (t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
+    set_grid(s, t->warps_per_block, t->band_rows, t->prefetch ? 1 : 0);
+    return SKS_OK;
+}
+
+extern "C" int sks_get_tuning(const sks_solver* s, sks_tuning_t* t)
+{
+    if (!s || !t) return set_err(SKS_ERR_ARG, "NULL argument");
+    t->warps_per_block = s->NW;
+    t->band_rows = s->HZ;
+    t->prefetch = s->PF;
+    t->blocks = s->nblocks;
+    t->ms_per_step = 0.f;
+    return SKS_OK;
+}
+
+namespace {
+
+struct Snapshot {
+    std::vector<void*> dev;
+    std::vector<size_t> bytes;
+    std::vector<void*> src;
+    int step, cur, g_last;
+};
+
+int snap_take(sks_solver* s, Snapshot& S)
+{
+    const size_t np = (size_t)s->m.nx * s->m.nz;
+    const size_t el = s->precision == SKS_FP64 ? sizeof(double) : sizeof(float);
+    void* bufs[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->G};
+    const size_t sz[] = {3 * np * el, 3 * np * el, 3 * np * el, 3 * np * el,
+                         sizeof(double) * (size_t)(s->chunk + 2) * (s->m.mtotal + s->m.shtotal)};
+    for (int i = 0; i < 5; i++) {
+        if (!bufs[i]) continue;
+        void* d = nullptr;
+        cudaError_t e = cudaMalloc(&d, sz[i]);
+        if (e != cudaSuccess) {
+            for (void* p : S.dev) cudaFree(p);
+            S.dev.clear();
+            return set_err(SKS_ERR_NOMEM, "autotune snapshot: %s", cudaGetErrorString(e));
+        }
+        CK(cudaMemcpyAsync(d, bufs[i], sz[i], cudaMemcpyDeviceToDevice, s->stream));
+        S.dev.push_back(d); S.bytes.push_back(sz[i]); S.src.push_back(bufs[i]);
+    }
+    S.step = s->step; S.cur = s->cur; S.g_last = s->g_last;
+    return SKS_OK;
+}
+
+int snap_restore(sks_solver* s, const Snapshot& S)
+{
+    for (size_t i = 0; i < S.dev.size(); i++)
+        CK(cudaMemcpyAsync(S.src[i], S.dev[i], S.bytes[i], cudaMemcpyDeviceToDevice, s->stream));
+    s->step = S.step; s->cur = S.cur; s->g_last = S.g_last;
+    return SKS_OK;
+}
+
+}  // namespace
+
+extern "C" int sks_autotune(sks_solver* s, int32_t steps, sks_tuning_t* best)
+{
+    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    const sks_model& m = s->m;
+    if (steps < 1) steps = 8;
+    if (s->step < m.nt_sem && !s->boundary_ready) return set_err(SKS_ERR_STATE, "boundary records not set");
+    if (s->step + 1 + steps > m.nst) return set_err(SKS_ERR_STATE, "autotune needs %d more steps than the run has left", steps + 1);
+    cudaSetDevice(s->device);
+    Snapshot snap;
+    int rc = snap_take(s, snap);
+    if (rc) return rc;
+    const int old_timing = s->timing;
+    s->timing = 0;
+    const int nws[] = {2, 4, 8};
+    const int hzs[] = {4, 6, 8, 12, 16, 24, 32};
+    sks_tuning_t b = {s->NW, s->HZ, s->PF, s->nblocks, 1e30f};
+    for (int nw : nws)
+        for (int pf = 0; pf < 2; pf++)
+            for (int hz : hzs) {
+                if (hz > m.nez && hz != hzs[0]) continue;
+                if ((rc = snap_restore(s, snap))) break;
+                set_grid(s, nw, hz, pf);
+                // one untimed step, then the timed ones
+                rc = sks_run(s, 1, nullptr, nullptr, nullptr);
+                if (rc < 0) break;
+                rc = sks_run(s, steps, nullptr, nullptr, nullptr);
+                if (rc < 0) break;
+                const float ms = (float)(s->last_run_ms / rc);
+                if (ms < b.ms_per_step) b = {nw, s->HZ, pf, s->nblocks, ms};
+                rc = SKS_OK;
+            }
+    const int rc2 = snap_restore(s, snap);
+    cudaStreamSynchronize(s->stream);
+    for (void* p : snap.dev) cudaFree(p);
+    s->timing = old_timing;
+    set_grid(s, b.warps_per_block, b.band_rows, b.prefetch);
+    if (rc < 0) return rc;
+    if (rc2) return rc2;
+    if (best) *best = b;
     return SKS_OK;
 }

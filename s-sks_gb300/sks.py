@@ -30,6 +30,7 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_get_info", "sks_setup_open", "sks_setup_info", "sks_setup_material", "sks_setup_mass",
            "sks_setup_receivers", "sks_setup_schedule", "sks_setup_close", "sks_open_setup",
            "sks_kernel_launches", "sks_last_run_ms", "sks_enable_kernel_timing", "sks_kernel_timing",
+           "sks_set_tuning", "sks_get_tuning", "sks_autotune",
            "sks_destroy", "sks_last_error"]
 
 KERNEL_CLASSES = ["element", "seam", "inject", "record", "interp"]
@@ -47,6 +48,14 @@ class Info(C.Structure):
                                          "precision", "step")] + \
                [("eh", C.c_double), ("h", C.c_double), ("sdt", C.c_double), ("device_bytes", C.c_int64),
                 ("seam_points", C.c_int64), ("tile_rows", C.c_int32), ("reserved", C.c_int32)]
+
+    def asdict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("warps_per_block", C.c_int32), ("band_rows", C.c_int32), ("prefetch", C.c_int32),
+                ("blocks", C.c_int32), ("ms_per_step", C.c_float)]
 
     def asdict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -84,6 +93,9 @@ def lib() -> C.CDLL:
         L.sks_last_run_ms.restype = C.c_double
         L.sks_enable_kernel_timing.argtypes = [vp, C.c_int]
         L.sks_kernel_timing.argtypes = [vp, dp, C.POINTER(C.c_int64)]
+        L.sks_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+        L.sks_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
+        L.sks_autotune.argtypes = [vp, C.c_int32, C.POINTER(Tuning)]
         L.sks_destroy.argtypes = [vp]
         L.sks_destroy.restype = None
         L.sks_last_error.restype = C.c_char_p
@@ -205,6 +217,20 @@ class Solver:
 
     def reset(self):
         _check(lib().sks_reset(self.h))
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        _check(lib().sks_get_tuning(self.h, C.byref(t)))
+        return t.asdict()
+
+    def set_tuning(self, warps_per_block: int, band_rows: int, prefetch: int = 1):
+        t = Tuning(warps_per_block, band_rows, prefetch, 0, 0.0)
+        _check(lib().sks_set_tuning(self.h, C.byref(t)))
+
+    def autotune(self, steps: int = 8) -> dict:
+        t = Tuning()
+        _check(lib().sks_autotune(self.h, steps, C.byref(t)))
+        return t.asdict()
 
     def launches(self) -> int:
         return lib().sks_kernel_launches(self.h)
