@@ -55,7 +55,7 @@ TUNINGS = [(nw, hz, pf) for nw in (2, 4, 8) for hz in (1, 3, 5, 23) for pf in (0
 def test_all_tunings_bit_identical(case, prec):
     d, c = case
     ref, _, _ = _run(d, prec, c.nst, tuning=(4, 8, 1))
-    assert max(np.abs(x).max() for x in ref) > 0.5
+    assert max(np.abs(x).max() for x in ref) > 0.1
     for t in TUNINGS:
         out, _, used = _run(d, prec, c.nst, tuning=t)
         assert (used["warps_per_block"], used["band_rows"], used["prefetch"]) == t
