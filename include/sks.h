@@ -137,12 +137,14 @@ int sks_open_setup(sks_setup *su, int precision, int device, sks_solver **out);
 /* ---- tuning -------------------------------------------------------------
  * The step kernel runs one CTA per (column of 6*W-1 elements, band of B
  * element rows); each CTA recomputes one element column and one element row
- * of halo.  W (warps per CTA), B and a prefetch variant are tunable; the
- * default comes from the mesh size and the SM count. */
+ * of halo.  W (warps per CTA), B, a prefetch variant and a register cap are
+ * tunable; the default comes from the mesh size and the SM count.  Every
+ * tuning gives bit-identical results. */
 typedef struct {
     int32_t warps_per_block;      /* 2, 4 or 8                              */
     int32_t band_rows;            /* element rows per CTA band              */
     int32_t prefetch;             /* 1: load the next element row early     */
+    int32_t register_cap;         /* 1: cap registers for 16 (FP32) / 8 (FP64) warps per SM */
     int32_t blocks;               /* CTAs per step (output)                 */
     float   ms_per_step;          /* measured by sks_autotune (output)      */
 } sks_tuning_t;

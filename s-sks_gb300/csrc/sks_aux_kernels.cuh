@@ -1,0 +1,147 @@
+// Kernels of the SEM time loop other than the step kernel: boundary-trace
+// interpolation, the step-0 line set-up and injection, step-0 receiver
+// sampling.  Included by the solver's translation unit only.
+#pragma once
+#include "sks_kernels.cuh"
+
+namespace sks {
+
+// Boundary-trace interpolation for a chunk of steps (interpl.c:16-54): row r of
+// Gout (r = 1..S) is step s0+r-1; four taps of FP32 records with FP64 weights,
+// then the |g| >= 10 guard of sem2d_psvsh.c:432-444 (sequential, ends read 0).
+__global__ void __launch_bounds__(256) k_interp(double* __restrict__ Gout, int L, int s0, int nsteps,
+                                                const float* __restrict__ rpsv, int mtotal,
+                                                const float* __restrict__ rsh, int shtotal,
+                                                const int32_t* __restrict__ tap_psv, const double* __restrict__ w_psv,
+                                                const int32_t* __restrict__ tap_sh, const double* __restrict__ w_sh)
+{
+    const int r = blockIdx.x;
+    if (r >= nsteps) return;
+    const int it = s0 + r;
+    double* out = Gout + (int64_t)(r + 1) * L;
+    __shared__ int bad[2];
+    if (threadIdx.x < 2) bad[threadIdx.x] = 0;
+    __syncthreads();
+    for (int fam = 0; fam < 2; fam++) {
+        const int n = fam ? shtotal : mtotal;
+        const float* rec = fam ? rsh : rpsv;
+        const int32_t* tp = (fam ? tap_sh : tap_psv) + 4 * it;
+        const double* wp = (fam ? w_sh : w_psv) + 4 * it;
+        double* o = out + (fam ? mtotal : 0);
+        int t[4]; double w[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) { t[j] = tp[j]; w[j] = wp[j]; }
+        int anybad = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if (t[j] >= 0) s = fma(w[j], (double)rec[(int64_t)t[j] * n + i], s);
+            o[i] = s;
+            if (!(s < 10.0 && s > -10.0)) anybad = 1;
+        }
+        if (anybad) bad[fam] = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int fam = 0; fam < 2; fam++) {
+            if (!bad[fam]) continue;
+            const int n = fam ? shtotal : mtotal;
+            double* o = out + (fam ? mtotal : 0);
+            for (int i = 0; i < n; i++)
+                if (!(o[i] < 10.0 && o[i] > -10.0)) {
+                    const double l = i > 0 ? o[i - 1] : 0.0, rr = i + 1 < n ? o[i + 1] : 0.0;
+                    o[i] = (l + rr) / 2;
+                }
+        }
+    }
+}
+
+// GRT_Interface4 (sem2d_psvsh.c:2076-2111): u^n += g(it) - g(it-1) on row nbl
+// (ix >= nbl) and column nbl (iz > nbl); the vertical component changes sign.
+template <typename T, bool LF>
+__global__ void __launch_bounds__(256) k_inject(T* __restrict__ u, T* __restrict__ dv, T* __restrict__ cc, int64_t np,
+                                                int nx, int nz, int nbl, const double* __restrict__ Gcur,
+                                                const double* __restrict__ Gprev, int mtotal)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nrow = nx - nbl, ncol = nz - nbl - 1;
+    if (i >= nrow + ncol) return;
+    const double *V = Gcur + mtotal, *V0 = Gprev + mtotal;
+    int64_t g;
+    double du, dvv, dw;
+    if (i < nrow) {
+        const int ix = nbl + i;
+        g = (int64_t)nbl * nx + ix;
+        du = -Gprev[ix] + Gcur[ix];
+        dvv = -V0[ix] + V[ix];
+        dw = Gprev[nx + ix] - Gcur[nx + ix];
+    } else {
+        const int iz = nbl + 1 + (i - nrow);
+        g = (int64_t)iz * nx + nbl;
+        du = -Gprev[2 * nx + iz] + Gcur[2 * nx + iz];
+        dvv = -V0[nx + iz] + V[nx + iz];
+        dw = Gprev[2 * nx + nz + iz] - Gcur[2 * nx + nz + iz];
+    }
+    const double dd[3] = {du, dvv, dw};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        if (!LF) {
+            u[c * np + g] += (T)dd[c];
+        } else {
+            const T add = (T)dd[c];
+            const T uu = u[c * np + g], cm = cc[c * np + g];
+            const T y = add - cm;
+            const T t = uu + y;
+            cc[c * np + g] = (t - uu) - y;
+            u[c * np + g] = t;
+            dv[c * np + g] += add;
+        }
+    }
+}
+
+// GRT_Interface (sem2d_psvsh.c:1953-2005) at step 0: set the line to g(0);
+// the column pass wins at the corner (nbl, nbl).  u^{-1} = 0, so d = u.
+template <typename T, bool LF>
+__global__ void __launch_bounds__(256) k_init_line(T* __restrict__ u, T* __restrict__ dv, int64_t np,
+                                                   int nx, int nz, int nbl, const double* __restrict__ G0, int mtotal)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nrow = nx - nbl - 1, ncol = nz - nbl;
+    if (i >= nrow + ncol) return;
+    const double* V = G0 + mtotal;
+    int64_t g;
+    double v3[3];
+    if (i < nrow) {
+        const int ix = nbl + 1 + i;
+        g = (int64_t)nbl * nx + ix;
+        v3[0] = G0[ix]; v3[1] = V[ix]; v3[2] = -G0[nx + ix];
+    } else {
+        const int iz = nbl + (i - nrow);
+        g = (int64_t)iz * nx + nbl;
+        v3[0] = G0[2 * nx + iz]; v3[1] = V[nx + iz]; v3[2] = -G0[2 * nx + nz + iz];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        u[c * np + g] = (T)v3[c];
+        if (LF) dv[c * np + g] = (T)v3[c];
+    }
+}
+
+// kirrecord_zhl (sem2d_psvsh.c:2116-2160): u_x, u_y, -u_z at the receivers;
+// offset np addresses the reference's never-written extra point (reads 0)
+template <typename T>
+__global__ void __launch_bounds__(128) k_record(const T* __restrict__ u, int64_t np, const int64_t* __restrict__ off,
+                                                int ntrace, float* __restrict__ out)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= ntrace) return;
+    const int64_t g = off[r];
+    float vx = 0.f, vy = 0.f, vz = 0.f;
+    if (g < np) { vx = (float)u[g]; vy = (float)u[np + g]; vz = (float)(-u[2 * np + g]); }
+    out[r] = vx;
+    out[ntrace + r] = vy;
+    out[2 * ntrace + r] = vz;
+}
+
+}  // namespace sks

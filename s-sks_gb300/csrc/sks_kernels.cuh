@@ -45,9 +45,10 @@ constexpr int MAT_STRIDE = 16;
 template <typename T>
 struct Coef {
     T D[NP * NP];    // D[j*NP+i]  = l'_i(xi_j) * 2/eh         (dlagP_JeI)
-    T DW[NP * NP];   // DW[j*NP+i] = l'_i(xi_j) * w_j          (dlagP_Gllw)
+    T DWs[NP * NP];  // DWs[j*NP+i] = l'_i(xi_j) * w_j * eh/2  (dlagP_Gllw * Uni_JeI * Uni_Je)
     T w[NP];         // GLL weights
-    T Je, JeI;       // eh^2/4, 2/eh
+    T winv[NP];      // 1/w_a: inverse lumped-mass weight of a point inside an element edge
+    T winv2;         // 1/(2 w_0): a point shared by two elements along x (or z)
     T dt2_Je;        // sdt^2 / Je   (M^-1 dt^2 = dt2_Je / (rho Wx Wz))
 };
 
@@ -67,8 +68,6 @@ struct Field {
     T* __restrict__ cc;           // FP32 form: Kahan compensation of u, in place
     const uint16_t* __restrict__ mid;   // material index per point
     const T* __restrict__ mat;          // [nmat][16]: 15 stiffness entries, 1/rho
-    const T* __restrict__ wxi;          // 1 / (sum of GLL weights at column ix)
-    const T* __restrict__ wzi;          // 1 / (... at row iz)
     const T* __restrict__ stc;          // Stacey coefficients [nbnd][3][3]: dt^2/(M+A), 2M/(M+A), (M-A)/(M+A)
     // next step's boundary injection, fused into this step's write (FP64 traces)
     const double* __restrict__ gnow;    // g(it)
@@ -80,6 +79,7 @@ struct Field {
     const int64_t* __restrict__ rec_off;     // sorted
     const int32_t* __restrict__ rec_idx;     // trace index of each sorted offset
     int nrec, ntrace;
+    int rec_iz0, rec_iz1;                    // rows holding receivers
     float* __restrict__ seis_row;            // [3][ntrace] of this step
 };
 
@@ -167,14 +167,15 @@ __device__ __forceinline__ void load_aux(const Field<T>& F, int64_t np, int64_t 
 template <typename T, bool LF>
 __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G, const Coef<T>& k,
                                              int ix, int iz, const T u[3], const T K[3], T rinv,
-                                             const Aux<T, LF>& x)
+                                             T wxi, T wzi, const Aux<T, LF>& x)
 {
     const int64_t g = (int64_t)iz * G.nx + ix;
-    const int64_t bi = stacey_index(ix, iz, G.nx, G.nz);
+    const bool edge = ix == 0 || iz == 0 || ix == G.nx - 1 || (iz == G.nz - 1 && ix <= 3 * N);
+    const int64_t bi = edge ? stacey_index(ix, iz, G.nx, G.nz) : -1;
     T un[3], dn[3], cn[3];
     if (!LF) {
         if (bi < 0) {
-            const T mdt2 = k.dt2_Je * rinv * F.wxi[ix] * F.wzi[iz];
+            const T mdt2 = k.dt2_Je * rinv * wxi * wzi;
 #pragma unroll
             for (int c = 0; c < 3; c++) un[c] = (-mdt2 * K[c] + (T)2 * u[c]) - x.a[c];
         } else {
@@ -184,7 +185,7 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
         }
     } else {
         if (bi < 0) {
-            const T mdt2 = k.dt2_Je * rinv * F.wxi[ix] * F.wzi[iz];
+            const T mdt2 = k.dt2_Je * rinv * wxi * wzi;
 #pragma unroll
             for (int c = 0; c < 3; c++) dn[c] = fma(-mdt2, K[c], x.a[c]);
         } else {
@@ -201,7 +202,7 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
         }
     }
     // kirrecord_zhl: the field after the update, before the next injection
-    if (F.nrec > 0 && ((__ldg(F.recbits + (g >> 5)) >> (g & 31)) & 1u)) {
+    if (iz >= F.rec_iz0 && iz <= F.rec_iz1 && ((__ldg(F.recbits + (g >> 5)) >> (g & 31)) & 1u)) {
         int lo = 0, hi = F.nrec;
         while (lo < hi) { const int mdl = (lo + hi) >> 1; if (F.rec_off[mdl] < g) lo = mdl + 1; else hi = mdl; }
         for (int r = lo; r < F.nrec && F.rec_off[r] == g; r++) {
@@ -254,8 +255,11 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
 // rows, plus one halo element row below it whose top-row force is carried
 // into the first owned row.  Warps hand the force of their last column to the
 // next warp through shared memory, once per element row.
-template <typename T, bool ANISO, bool LF, int NW, bool PF>
-__global__ void __launch_bounds__(NW * 32) k_step(Field<T> F, Geo<T> G, Coef<T> k)
+// CAP: ask for 16 (FP32) / 8 (FP64) resident warps per SM, i.e. at most
+// 128 / 255 registers a thread; otherwise the compiler's choice.
+template <typename T, bool ANISO, bool LF, int NW, bool PF, bool CAP>
+__global__ void __launch_bounds__(NW * 32, CAP ? (sizeof(T) == 4 ? 16 : 8) / NW : 1)
+k_step(Field<T> F, Geo<T> G, Coef<T> k)
 {
     __shared__ T xch[2][NW][N][3];
     __shared__ T xtop[NW][3];
@@ -281,8 +285,11 @@ __global__ void __launch_bounds__(NW * 32) k_step(Field<T> F, Geo<T> G, Coef<T> 
 
     T Dx[NP], DWc[NP];
 #pragma unroll
-    for (int t = 0; t < NP; t++) { Dx[t] = k.D[al * NP + t]; DWc[t] = k.DW[t * NP + al]; }
+    for (int t = 0; t < NP; t++) { Dx[t] = k.D[al * NP + t]; DWc[t] = k.DWs[t * NP + al]; }
     const T wal = k.w[al];
+    // lumped-mass weight of this lane's column: inside an element, on an
+    // element edge shared by two elements, or on the box's left/right edge
+    const T wxi = (al > 0 && al < N) ? k.winv[al] : ((ix == 0 || ix == nx - 1) ? k.winv[0] : k.winv2);
 
     T u[NP][3];
     uint16_t m[NP];
@@ -381,26 +388,30 @@ __global__ void __launch_bounds__(NW * 32) k_step(Field<T> F, Geo<T> G, Coef<T> 
             rinv[b] = M.s[15];
             T sg[5];
             stress<T, ANISO>(M, ee, sg);
-            const T f0[3] = {sg[0] * k.JeI, sg[1] * k.JeI, sg[2] * k.JeI};
-            F2[b][0] = sg[2] * k.JeI; F2[b][1] = sg[3] * k.JeI; F2[b][2] = sg[4] * k.JeI;
+            F2[b][0] = sg[2]; F2[b][1] = sg[3]; F2[b][2] = sg[4];
+            // the halo element row only hands its top row's force upward
+            if (!halo || b == N) {
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-                T s = 0;
+                for (int c = 0; c < 3; c++) {
+                    T s = 0;
 #pragma unroll
-                for (int a = 0; a < NP; a++) s = fma(__shfl_sync(FULL, f0[c], base + a), DWc[a], s);
-                item0[b][c] = s;
+                    for (int a = 0; a < NP; a++) s = fma(__shfl_sync(FULL, sg[c], base + a), DWc[a], s);
+                    item0[b][c] = s;
+                }
             }
         }
         T kk[NP][3];
 #pragma unroll
-        for (int b = 0; b < NP; b++)
+        for (int b = 0; b < NP; b++) {
+            if (halo && b < N) continue;
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 T s = 0;
 #pragma unroll
-                for (int bb = 0; bb < NP; bb++) s = fma(F2[bb][c], k.DW[bb * NP + b], s);
-                kk[b][c] = live ? (item0[b][c] * k.w[b] + s * wal) * k.Je : (T)0;
+                for (int bb = 0; bb < NP; bb++) s = fma(F2[bb][c], k.DWs[bb * NP + b], s);
+                kk[b][c] = live ? fma(item0[b][c], k.w[b], s * wal) : (T)0;
             }
+        }
         if (ez > ezs) {
 #pragma unroll
             for (int c = 0; c < 3; c++) kk[0][c] = kc[c] + kk[0][c];
@@ -426,7 +437,10 @@ __global__ void __launch_bounds__(NW * 32) k_step(Field<T> F, Geo<T> G, Coef<T> 
                     if (e == 0) left = w > 0 ? xch[par][w > 0 ? w - 1 : 0][b][c] : (T)0;
                     kt[c] = add_left ? left + kk[b][c] : kk[b][c];
                 }
-                if (own_x) finish_point<T, LF>(F, G, k, ix, ez * N + b, u[b], kt, rinv[b], aux[b]);
+                if (own_x) {
+                    const T wzi = b > 0 ? k.winv[b] : (ez == 0 ? k.winv[0] : k.winv2);
+                    finish_point<T, LF>(F, G, k, ix, ez * N + b, u[b], kt, rinv[b], wxi, wzi, aux[b]);
+                }
             }
             par ^= 1;
         }
@@ -449,147 +463,17 @@ __global__ void __launch_bounds__(NW * 32) k_step(Field<T> F, Geo<T> G, Coef<T> 
             const int iz = G.nz - 1;
             Aux<T, LF> x;
             load_aux<T, LF>(F, G.np, (int64_t)iz * nx + ix, x);
-            finish_point<T, LF>(F, G, k, ix, iz, u[N], kt, rinvN, x);
+            finish_point<T, LF>(F, G, k, ix, iz, u[N], kt, rinvN, wxi, k.winv[0], x);
         }
     }
 }
 
-// Boundary-trace interpolation for a chunk of steps (interpl.c:16-54): row r of
-// Gout (r = 1..S) is step s0+r-1; four taps of FP32 records with FP64 weights,
-// then the |g| >= 10 guard of sem2d_psvsh.c:432-444 (sequential, ends read 0).
-__global__ void __launch_bounds__(256) k_interp(double* __restrict__ Gout, int L, int s0, int nsteps,
-                                                const float* __restrict__ rpsv, int mtotal,
-                                                const float* __restrict__ rsh, int shtotal,
-                                                const int32_t* __restrict__ tap_psv, const double* __restrict__ w_psv,
-                                                const int32_t* __restrict__ tap_sh, const double* __restrict__ w_sh)
-{
-    const int r = blockIdx.x;
-    if (r >= nsteps) return;
-    const int it = s0 + r;
-    double* out = Gout + (int64_t)(r + 1) * L;
-    __shared__ int bad[2];
-    if (threadIdx.x < 2) bad[threadIdx.x] = 0;
-    __syncthreads();
-    for (int fam = 0; fam < 2; fam++) {
-        const int n = fam ? shtotal : mtotal;
-        const float* rec = fam ? rsh : rpsv;
-        const int32_t* tp = (fam ? tap_sh : tap_psv) + 4 * it;
-        const double* wp = (fam ? w_sh : w_psv) + 4 * it;
-        double* o = out + (fam ? mtotal : 0);
-        int t[4]; double w[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) { t[j] = tp[j]; w[j] = wp[j]; }
-        int anybad = 0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            double s = 0.0;
-#pragma unroll
-            for (int j = 0; j < 4; j++)
-                if (t[j] >= 0) s = fma(w[j], (double)rec[(int64_t)t[j] * n + i], s);
-            o[i] = s;
-            if (!(s < 10.0 && s > -10.0)) anybad = 1;
-        }
-        if (anybad) bad[fam] = 1;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int fam = 0; fam < 2; fam++) {
-            if (!bad[fam]) continue;
-            const int n = fam ? shtotal : mtotal;
-            double* o = out + (fam ? mtotal : 0);
-            for (int i = 0; i < n; i++)
-                if (!(o[i] < 10.0 && o[i] > -10.0)) {
-                    const double l = i > 0 ? o[i - 1] : 0.0, rr = i + 1 < n ? o[i + 1] : 0.0;
-                    o[i] = (l + rr) / 2;
-                }
-        }
-    }
-}
+}  // namespace sks
 
-// GRT_Interface4 (sem2d_psvsh.c:2076-2111): u^n += g(it) - g(it-1) on row nbl
-// (ix >= nbl) and column nbl (iz > nbl); the vertical component changes sign.
-template <typename T, bool LF>
-__global__ void __launch_bounds__(256) k_inject(T* __restrict__ u, T* __restrict__ dv, T* __restrict__ cc, int64_t np,
-                                                int nx, int nz, int nbl, const double* __restrict__ Gcur,
-                                                const double* __restrict__ Gprev, int mtotal)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nrow = nx - nbl, ncol = nz - nbl - 1;
-    if (i >= nrow + ncol) return;
-    const double *V = Gcur + mtotal, *V0 = Gprev + mtotal;
-    int64_t g;
-    double du, dvv, dw;
-    if (i < nrow) {
-        const int ix = nbl + i;
-        g = (int64_t)nbl * nx + ix;
-        du = -Gprev[ix] + Gcur[ix];
-        dvv = -V0[ix] + V[ix];
-        dw = Gprev[nx + ix] - Gcur[nx + ix];
-    } else {
-        const int iz = nbl + 1 + (i - nrow);
-        g = (int64_t)iz * nx + nbl;
-        du = -Gprev[2 * nx + iz] + Gcur[2 * nx + iz];
-        dvv = -V0[nx + iz] + V[nx + iz];
-        dw = Gprev[2 * nx + nz + iz] - Gcur[2 * nx + nz + iz];
-    }
-    const double dd[3] = {du, dvv, dw};
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        if (!LF) {
-            u[c * np + g] += (T)dd[c];
-        } else {
-            const T add = (T)dd[c];
-            const T uu = u[c * np + g], cm = cc[c * np + g];
-            const T y = add - cm;
-            const T t = uu + y;
-            cc[c * np + g] = (t - uu) - y;
-            u[c * np + g] = t;
-            dv[c * np + g] += add;
-        }
-    }
-}
-
-// GRT_Interface (sem2d_psvsh.c:1953-2005) at step 0: set the line to g(0);
-// the column pass wins at the corner (nbl, nbl).  u^{-1} = 0, so d = u.
-template <typename T, bool LF>
-__global__ void __launch_bounds__(256) k_init_line(T* __restrict__ u, T* __restrict__ dv, int64_t np,
-                                                   int nx, int nz, int nbl, const double* __restrict__ G0, int mtotal)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nrow = nx - nbl - 1, ncol = nz - nbl;
-    if (i >= nrow + ncol) return;
-    const double* V = G0 + mtotal;
-    int64_t g;
-    double v3[3];
-    if (i < nrow) {
-        const int ix = nbl + 1 + i;
-        g = (int64_t)nbl * nx + ix;
-        v3[0] = G0[ix]; v3[1] = V[ix]; v3[2] = -G0[nx + ix];
-    } else {
-        const int iz = nbl + (i - nrow);
-        g = (int64_t)iz * nx + nbl;
-        v3[0] = G0[2 * nx + iz]; v3[1] = V[nx + iz]; v3[2] = -G0[2 * nx + nz + iz];
-    }
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        u[c * np + g] = (T)v3[c];
-        if (LF) dv[c * np + g] = (T)v3[c];
-    }
-}
-
-// kirrecord_zhl (sem2d_psvsh.c:2116-2160): u_x, u_y, -u_z at the receivers;
-// offset np addresses the reference's never-written extra point (reads 0)
-template <typename T>
-__global__ void __launch_bounds__(128) k_record(const T* __restrict__ u, int64_t np, const int64_t* __restrict__ off,
-                                                int ntrace, float* __restrict__ out)
-{
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= ntrace) return;
-    const int64_t g = off[r];
-    float vx = 0.f, vy = 0.f, vz = 0.f;
-    if (g < np) { vx = (float)u[g]; vy = (float)u[np + g]; vz = (float)(-u[2 * np + g]); }
-    out[r] = vx;
-    out[ntrace + r] = vy;
-    out[2 * ntrace + r] = vz;
-}
-
+namespace sks {
+struct StepVariant { int nw; int prefetch; int cap; };
+cudaError_t launch_step_f32(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                            const Field<float>& F, const Geo<float>& G, const Coef<float>& k);
+cudaError_t launch_step_f64(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                            const Field<double>& F, const Geo<double>& G, const Coef<double>& k);
 }  // namespace sks

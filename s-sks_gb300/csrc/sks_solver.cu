@@ -4,6 +4,7 @@
 #include "sks.h"
 #include "sks_model.h"
 #include "sks_kernels.cuh"
+#include "sks_aux_kernels.cuh"
 
 #include <cuda_runtime.h>
 #include <cstdarg>
@@ -43,7 +44,7 @@ struct sks_solver {
     int64_t launches;
     cudaStream_t stream;
     // geometry: CTA grid of the step kernel (tunable)
-    int NW, ncx, ncz, HZ, nblocks, PF;
+    int NW, ncx, ncz, HZ, nblocks, PF, CAP;
     int sms;
     int nbl;
     // device buffers
@@ -52,14 +53,13 @@ struct sks_solver {
     void* Cc;                  // FP32 form: Kahan compensation
     uint16_t* mid;
     void* mat;                 // [nmat][16] in the form's type
-    void* wxi;
-    void* wzi;
     void* stc;                 // Stacey coefficients
     int64_t* rec_off;          // per trace (step-0 recording)
     uint32_t* recbits;         // receiver bitmap over points
     int64_t* rec_sorted;       // receiver offsets, sorted
     int32_t* rec_idx;          // trace index of each sorted offset
     int nrec_in;               // receivers inside the mesh (offset < np)
+    int rec_iz0, rec_iz1;      // rows holding them (empty range when none)
     float* seis;               // [chunk][3][ntrace]
     double* G;                 // [(chunk+1)][mtotal+shtotal]
     float* rec_psv;            // boundary records
@@ -182,12 +182,12 @@ int dmalloc(sks_solver* s, T** p, size_t n)
 
 void free_device(sks_solver* s)
 {
-    void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->wxi, s->wzi, s->stc,
+    void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc,
                   s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seis, s->G, s->rec_psv, s->rec_sh,
                   s->tap_psv, s->tap_sh, s->w_psv, s->w_sh};
     for (void* p : ps)
         if (p) cudaFree(p);
-    s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->wxi = s->wzi = s->stc = nullptr;
+    s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = nullptr;
     s->mid = nullptr; s->rec_off = nullptr; s->recbits = nullptr; s->rec_sorted = nullptr; s->rec_idx = nullptr;
     s->seis = nullptr; s->G = nullptr;
     s->rec_psv = s->rec_sh = nullptr; s->tap_psv = s->tap_sh = nullptr; s->w_psv = s->w_sh = nullptr;
@@ -256,21 +256,6 @@ int upload_tables(sks_solver* s)
         for (int k = 0; k < 15; k++) mat[(size_t)i * MAT_STRIDE + k] = (T)m.mat[(size_t)i * SKS_MAT_STRIDE + k];
         mat[(size_t)i * MAT_STRIDE + 15] = (T)(1.0 / m.mat[(size_t)i * SKS_MAT_STRIDE + 15]);
     }
-    // column / row sums of GLL weights over the elements holding a point
-    std::vector<T> wxi(m.nx), wzi(m.nz);
-    for (int pass = 0; pass < 2; pass++) {
-        const int n = pass ? m.nz : m.nx, ne = pass ? m.nez : m.nex;
-        for (int i = 0; i < n; i++) {
-            double w = 0;
-            const int a = i % m.hpn;
-            if (a != 0) w = m.gllw[a];
-            else {
-                if (i / m.hpn < ne) w += m.gllw[0];          // element to the right/above
-                if (i > 0) w += m.gllw[m.hpn];              // element to the left/below
-            }
-            (pass ? wzi : wxi)[i] = (T)(1.0 / w);
-        }
-    }
     // Stacey coefficients per boundary point and component
     const int64_t nb = sks_stacey_count(m.nx, m.nz, m.hpn);
     std::vector<T> stc((size_t)nb * 9, (T)0);
@@ -289,19 +274,13 @@ int upload_tables(sks_solver* s)
             }
         }
     (void)N1;
-    T *dmat, *dwx, *dwz, *dstc;
+    T *dmat, *dstc;
     int rc;
     if ((rc = dmalloc(s, &dmat, mat.size()))) return rc;
     s->mat = dmat;
-    if ((rc = dmalloc(s, &dwx, wxi.size()))) return rc;
-    s->wxi = dwx;
-    if ((rc = dmalloc(s, &dwz, wzi.size()))) return rc;
-    s->wzi = dwz;
     if ((rc = dmalloc(s, &dstc, stc.size()))) return rc;
     s->stc = dstc;
     CK(cudaMemcpy(dmat, mat.data(), mat.size() * sizeof(T), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(dwx, wxi.data(), wxi.size() * sizeof(T), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(dwz, wzi.data(), wzi.size() * sizeof(T), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(dstc, stc.data(), stc.size() * sizeof(T), cudaMemcpyHostToDevice));
     // wavefield
     const size_t np = (size_t)m.nx * m.nz;
@@ -327,11 +306,10 @@ Coef<T> make_coef(const sks_model& m)
     for (int j = 0; j < NP; j++)
         for (int i = 0; i < NP; i++) {
             k.D[j * NP + i] = (T)(m.dlagP[j * NP + i] * m.JeI);
-            k.DW[j * NP + i] = (T)(m.dlagP[j * NP + i] * m.gllw[j]);
+            k.DWs[j * NP + i] = (T)(m.dlagP[j * NP + i] * m.gllw[j] * (m.JeI * m.Je));
         }
-    for (int i = 0; i < NP; i++) k.w[i] = (T)m.gllw[i];
-    k.Je = (T)m.Je;
-    k.JeI = (T)m.JeI;
+    for (int i = 0; i < NP; i++) { k.w[i] = (T)m.gllw[i]; k.winv[i] = (T)(1.0 / m.gllw[i]); }
+    k.winv2 = (T)(1.0 / (2.0 * m.gllw[0]));
     k.dt2_Je = (T)(m.sdt * m.sdt / m.Je);
     return k;
 }
@@ -347,8 +325,6 @@ Field<T> make_field(sks_solver* s)
     F.cc = (T*)s->Cc;
     F.mid = s->mid;
     F.mat = (const T*)s->mat;
-    F.wxi = (const T*)s->wxi;
-    F.wzi = (const T*)s->wzi;
     F.stc = (const T*)s->stc;
     F.mtotal = s->m.mtotal;
     F.recbits = s->recbits;
@@ -356,6 +332,8 @@ Field<T> make_field(sks_solver* s)
     F.rec_idx = s->rec_idx;
     F.nrec = s->nrec_in;
     F.ntrace = s->m.ntrace;
+    F.rec_iz0 = s->rec_iz0;
+    F.rec_iz1 = s->rec_iz1;
     return F;
 }
 
@@ -370,28 +348,12 @@ Geo<T> make_geo(const sks_solver* s)
     return G;
 }
 
-template <typename T, bool ANISO, bool LF, bool PF>
-void launch_step_pf(sks_solver* s, const Field<T>& F, const Geo<T>& G, const Coef<T>& k)
-{
-    switch (s->NW) {
-    case 2: k_step<T, ANISO, LF, 2, PF><<<s->nblocks, 64, 0, s->stream>>>(F, G, k); break;
-    case 8: k_step<T, ANISO, LF, 8, PF><<<s->nblocks, 256, 0, s->stream>>>(F, G, k); break;
-    default: k_step<T, ANISO, LF, 4, PF><<<s->nblocks, 128, 0, s->stream>>>(F, G, k); break;
-    }
-}
-
-template <typename T, bool ANISO, bool LF>
-void launch_step(sks_solver* s, const Field<T>& F, const Geo<T>& G, const Coef<T>& k)
-{
-    if (s->PF) launch_step_pf<T, ANISO, LF, true>(s, F, G, k);
-    else launch_step_pf<T, ANISO, LF, false>(s, F, G, k);
-}
-
 // CTA grid for a tuning: NW warps (6*NW-1 owned elements) by bands of HZ rows
-void set_grid(sks_solver* s, int NW, int HZ, int PF)
+void set_grid(sks_solver* s, int NW, int HZ, int PF, int CAP)
 {
     s->NW = NW;
     s->PF = PF;
+    s->CAP = CAP;
     s->ncx = (s->m.nex + (TEX * NW - 1) - 1) / (TEX * NW - 1);
     s->HZ = std::max(1, std::min(HZ, s->m.nez));
     s->ncz = (s->m.nez + s->HZ - 1) / s->HZ;
@@ -414,8 +376,13 @@ int step_impl(sks_solver* s, int it, const double* Gcur, const double* Gnext, fl
     k = make_coef<T>(m);
     {
         KTimer t(s, SKS_KC_ELEMENT);
-        if (m.anisotropic) launch_step<T, true, LF>(s, F, G, k);
-        else launch_step<T, false, LF>(s, F, G, k);
+        const StepVariant v{s->NW, s->PF, s->CAP};
+        if (sizeof(T) == 4)
+            launch_step_f32(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<float>*)&F,
+                            *(const Geo<float>*)&G, *(const Coef<float>*)&k);
+        else
+            launch_step_f64(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<double>*)&F,
+                            *(const Geo<double>*)&G, *(const Coef<double>*)&k);
     }
     s->cur = 1 - s->cur;
     return SKS_OK;
@@ -520,7 +487,7 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
     }
     {
         const int ncx4 = (m.nex + (TEX * 4 - 1) - 1) / (TEX * 4 - 1);
-        set_grid(s, 4, pick_band(m, ncx4, sms), 1);
+        set_grid(s, 4, pick_band(m, ncx4, sms), 0, 0);
     }
     s->chunk = 64;
     const size_t np = (size_t)m.nx * m.nz;
@@ -530,6 +497,8 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         ce = cudaMemcpy(s->mid, m.mat_id, np * sizeof(uint16_t), cudaMemcpyHostToDevice);
         if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "upload of material indices: %s", cudaGetErrorString(ce));
     }
+    s->rec_iz0 = 1 << 30;
+    s->rec_iz1 = -1;
     if (!rc && m.ntrace > 0) {
         // receivers inside the mesh, sorted by point, and a bitmap of their points
         std::vector<std::pair<int64_t, int32_t>> rs;
@@ -537,6 +506,13 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
             if (m.rec_off[i] < (int64_t)np) rs.push_back({m.rec_off[i], i});
         std::sort(rs.begin(), rs.end());
         s->nrec_in = (int)rs.size();
+        s->rec_iz0 = 1 << 30;
+        s->rec_iz1 = -1;
+        for (auto& r : rs) {
+            const int iz = (int)(r.first / m.nx);
+            s->rec_iz0 = std::min(s->rec_iz0, iz);
+            s->rec_iz1 = std::max(s->rec_iz1, iz);
+        }
         std::vector<int64_t> off(rs.size());
         std::vector<int32_t> idx(rs.size());
         std::vector<uint32_t> bits((np + 31) / 32, 0u);
@@ -756,7 +732,7 @@ extern "C" int sks_set_tuning(sks_solver* s, const sks_tuning_t* t)
     if (t->warps_per_block != 2 && t->warps_per_block != 4 && t->warps_per_block != 8)
         return set_err(SKS_ERR_ARG, "warps_per_block=%d: 2, 4 or 8", t->warps_per_block);
     if (t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
-    set_grid(s, t->warps_per_block, t->band_rows, t->prefetch ? 1 : 0);
+    set_grid(s, t->warps_per_block, t->band_rows, t->prefetch ? 1 : 0, t->register_cap ? 1 : 0);
     return SKS_OK;
 }
 
@@ -766,6 +742,7 @@ extern "C" int sks_get_tuning(const sks_solver* s, sks_tuning_t* t)
     t->warps_per_block = s->NW;
     t->band_rows = s->HZ;
     t->prefetch = s->PF;
+    t->register_cap = s->CAP;
     t->blocks = s->nblocks;
     t->ms_per_step = 0.f;
     return SKS_OK;
@@ -828,27 +805,28 @@ extern "C" int sks_autotune(sks_solver* s, int32_t steps, sks_tuning_t* best)
     s->timing = 0;
     const int nws[] = {2, 4, 8};
     const int hzs[] = {4, 6, 8, 12, 16, 24, 32};
-    sks_tuning_t b = {s->NW, s->HZ, s->PF, s->nblocks, 1e30f};
+    sks_tuning_t b = {s->NW, s->HZ, s->PF, s->CAP, s->nblocks, 1e30f};
     for (int nw : nws)
         for (int pf = 0; pf < 2; pf++)
+          for (int cap = 0; cap < 2; cap++)
             for (int hz : hzs) {
                 if (hz > m.nez && hz != hzs[0]) continue;
                 if ((rc = snap_restore(s, snap))) break;
-                set_grid(s, nw, hz, pf);
+                set_grid(s, nw, hz, pf, cap);
                 // one untimed step, then the timed ones
                 rc = sks_run(s, 1, nullptr, nullptr, nullptr);
                 if (rc < 0) break;
                 rc = sks_run(s, steps, nullptr, nullptr, nullptr);
                 if (rc < 0) break;
                 const float ms = (float)(s->last_run_ms / rc);
-                if (ms < b.ms_per_step) b = {nw, s->HZ, pf, s->nblocks, ms};
+                if (ms < b.ms_per_step) b = {nw, s->HZ, pf, cap, s->nblocks, ms};
                 rc = SKS_OK;
             }
     const int rc2 = snap_restore(s, snap);
     cudaStreamSynchronize(s->stream);
     for (void* p : snap.dev) cudaFree(p);
     s->timing = old_timing;
-    set_grid(s, b.warps_per_block, b.band_rows, b.prefetch);
+    set_grid(s, b.warps_per_block, b.band_rows, b.prefetch, b.register_cap);
     if (rc < 0) return rc;
     if (rc2) return rc2;
     if (best) *best = b;

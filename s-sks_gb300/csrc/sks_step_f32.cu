@@ -1,0 +1,48 @@
+// Instantiations of the step kernel for the FP32-compensated form, one translation unit
+// per precision so the variants compile in parallel.
+#include "sks_kernels.cuh"
+
+namespace sks {
+namespace {
+
+template <bool ANISO, int NW, bool PF, bool CAP>
+void go(int blocks, cudaStream_t st, const Field<float>& F, const Geo<float>& G, const Coef<float>& k)
+{
+    k_step<float, ANISO, true, NW, PF, CAP><<<blocks, NW * 32, 0, st>>>(F, G, k);
+}
+
+template <bool ANISO, int NW>
+void go_nw(const StepVariant& v, int blocks, cudaStream_t st, const Field<float>& F, const Geo<float>& G,
+           const Coef<float>& k)
+{
+    if (v.prefetch) {
+        if (v.cap) go<ANISO, NW, true, true>(blocks, st, F, G, k);
+        else go<ANISO, NW, true, false>(blocks, st, F, G, k);
+    } else {
+        if (v.cap) go<ANISO, NW, false, true>(blocks, st, F, G, k);
+        else go<ANISO, NW, false, false>(blocks, st, F, G, k);
+    }
+}
+
+template <bool ANISO>
+void go_aniso(const StepVariant& v, int blocks, cudaStream_t st, const Field<float>& F, const Geo<float>& G,
+              const Coef<float>& k)
+{
+    switch (v.nw) {
+    case 2: go_nw<ANISO, 2>(v, blocks, st, F, G, k); break;
+    case 8: go_nw<ANISO, 8>(v, blocks, st, F, G, k); break;
+    default: go_nw<ANISO, 4>(v, blocks, st, F, G, k); break;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_step_f32(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                            const Field<float>& F, const Geo<float>& G, const Coef<float>& k)
+{
+    if (aniso) go_aniso<true>(v, blocks, st, F, G, k);
+    else go_aniso<false>(v, blocks, st, F, G, k);
+    return cudaGetLastError();
+}
+
+}  // namespace sks

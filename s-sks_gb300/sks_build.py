@@ -42,13 +42,16 @@ def _stale(target: str, deps: list[str]) -> bool:
 def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
-    hdrs = [os.path.join(INC, "sks.h"), os.path.join(CSRC, "sks_model.h"), os.path.join(CSRC, "sks_kernels.cuh")]
+    hdrs = [os.path.join(INC, "sks.h"), os.path.join(CSRC, "sks_model.h"), os.path.join(CSRC, "sks_kernels.cuh"),
+            os.path.join(CSRC, "sks_aux_kernels.cuh")]
     units = [
         (os.path.join(CSRC, "sks_model.c"), os.path.join(OUT, "sks_model.o"),
          ["gcc", "-O2", "-std=gnu11", "-fPIC", "-Wall", "-I" + INC, "-c"]),
-        (os.path.join(CSRC, "sks_solver.cu"), os.path.join(OUT, "sks_solver.o"),
-         [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC, "-c"]),
     ]
+    for cu in ("sks_solver", "sks_step_f32", "sks_step_f64"):
+        units.append((os.path.join(CSRC, cu + ".cu"), os.path.join(OUT, cu + ".o"),
+                      [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC,
+                       "-c"]))
     jobs = []
     for src, obj, cmd in units:
         if _stale(obj, [src] + hdrs):

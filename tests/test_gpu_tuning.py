@@ -48,17 +48,17 @@ def _run(d, prec, nst, tuning=None, autotune=False):
         return out, got, s.tuning()
 
 
-TUNINGS = [(nw, hz, pf) for nw in (2, 4, 8) for hz in (1, 3, 5, 23) for pf in (0, 1)]
+TUNINGS = [(nw, hz, pf, cap) for nw in (2, 4, 8) for hz in (1, 3, 23) for pf in (0, 1) for cap in (0, 1)]
 
 
 @pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])
 def test_all_tunings_bit_identical(case, prec):
     d, c = case
-    ref, _, _ = _run(d, prec, c.nst, tuning=(4, 8, 1))
+    ref, _, _ = _run(d, prec, c.nst, tuning=(4, 8, 1, 0))
     assert max(np.abs(x).max() for x in ref) > 0.1
     for t in TUNINGS:
         out, _, used = _run(d, prec, c.nst, tuning=t)
-        assert (used["warps_per_block"], used["band_rows"], used["prefetch"]) == t
+        assert (used["warps_per_block"], used["band_rows"], used["prefetch"], used["register_cap"]) == t
         for i in range(3):
             assert np.array_equal(out[i], ref[i]), f"tuning {t} differs in component {i}"
 
