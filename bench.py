@@ -121,6 +121,27 @@ def _pinned(n: int):
     return torch.empty(n, dtype=torch.float32, pin_memory=True)
 
 
+def run_fixed(d: str, precision: int, steps: int, warmup: int, gpu: int, tuning) -> dict:
+    """Only the device-resident step loop with a given tuning (for profilers)."""
+    import sks
+    cwd = os.getcwd()
+    os.chdir(d)
+    try:
+        s = sks.Solver(["par=run.par"], precision=precision, device=gpu)
+        s.load_boundary_files()
+        if tuning:
+            s.set_tuning(*tuning)
+        lib_run_noout(s, warmup)
+        n = lib_run_noout(s, steps)
+        ms = s.last_run_ms()
+        info, t = s.info(), s.tuning()
+        s.close()
+    finally:
+        os.chdir(cwd)
+    npts = info["nx"] * info["nz"]
+    return {"steps": n, "ms_per_step": ms / n, "updates_per_s": npts * n / (ms / 1e3), "tuning": t}
+
+
 def run_form(d: str, precision: int, steps: int, warmup: int, gpu: int, clocks: bool = False) -> dict:
     """Device-resident timing of one form: autotune (state restored), W
     warm-up steps, K timed steps (CUDA events on the solver's stream), then a
@@ -265,6 +286,10 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="only the device-resident step loop of one form (profiling)")
+    ap.add_argument("--form", default="fp32c", choices=["fp32c", "fp64"])
+    ap.add_argument("--tuning", default="", help="W,B,P,C: warps per CTA, band rows, prefetch, register cap")
     a = ap.parse_args()
     a.warmup = max(3, a.warmup)
     dist, rank, world, local = _dist()
@@ -299,6 +324,16 @@ def main() -> None:
     import torch
     gpu = local if world > 1 else 0
     torch.cuda.set_device(gpu)
+    if a.kernel_only:
+        d = tempfile.mkdtemp(prefix="sks_prof_")
+        try:
+            make_case(d, a.warmup + a.steps + 8)
+            tun = tuple(int(x) for x in a.tuning.split(",")) if a.tuning else None
+            r = run_fixed(d, 1 if a.form == "fp32c" else 0, a.steps, a.warmup, gpu, tun)
+        finally:
+            shutil.rmtree(d, ignore_errors=True)
+        print(json.dumps({"kernel_only": a.form, **r}))
+        return
     d = tempfile.mkdtemp(prefix="sks_bench_")
     try:
         nst = a.warmup + a.steps + 8

@@ -60,7 +60,11 @@ struct sks_solver {
     int32_t* rec_idx;          // trace index of each sorted offset
     int nrec_in;               // receivers inside the mesh (offset < np)
     int rec_iz0, rec_iz1;      // rows holding them (empty range when none)
-    float* seis;               // [chunk][3][ntrace]
+    float* seis;               // [chunk][3][ntrace], the slot in use
+    float* seisbuf[2];         // two slots: one filled by kernels while the other is copied out
+    cudaStream_t copy_stream;
+    cudaEvent_t chunk_done[2], copy_done[2];
+    bool slot_busy[2];
     double* G;                 // [(chunk+1)][mtotal+shtotal]
     float* rec_psv;            // boundary records
     float* rec_sh;
@@ -183,13 +187,13 @@ int dmalloc(sks_solver* s, T** p, size_t n)
 void free_device(sks_solver* s)
 {
     void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc,
-                  s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seis, s->G, s->rec_psv, s->rec_sh,
+                  s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seisbuf[0], s->seisbuf[1], s->G, s->rec_psv, s->rec_sh,
                   s->tap_psv, s->tap_sh, s->w_psv, s->w_sh};
     for (void* p : ps)
         if (p) cudaFree(p);
     s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = nullptr;
     s->mid = nullptr; s->rec_off = nullptr; s->recbits = nullptr; s->rec_sorted = nullptr; s->rec_idx = nullptr;
-    s->seis = nullptr; s->G = nullptr;
+    s->seis = nullptr; s->seisbuf[0] = s->seisbuf[1] = nullptr; s->G = nullptr;
     s->rec_psv = s->rec_sh = nullptr; s->tap_psv = s->tap_sh = nullptr; s->w_psv = s->w_sh = nullptr;
 }
 
@@ -536,7 +540,17 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         ce = cudaMemcpy(s->rec_off, m.rec_off, sizeof(int64_t) * m.ntrace, cudaMemcpyHostToDevice);
         if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "upload of receivers: %s", cudaGetErrorString(ce));
     }
-    if (!rc) rc = dmalloc(s, &s->seis, (size_t)s->chunk * 3 * std::max(1, m.ntrace));
+    if (!rc) rc = dmalloc(s, &s->seisbuf[0], (size_t)s->chunk * 3 * std::max(1, m.ntrace));
+    if (!rc) rc = dmalloc(s, &s->seisbuf[1], (size_t)s->chunk * 3 * std::max(1, m.ntrace));
+    if (!rc) {
+        s->seis = s->seisbuf[0];
+        ce = cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking);
+        for (int i = 0; i < 2 && ce == cudaSuccess; i++) {
+            ce = cudaEventCreateWithFlags(&s->chunk_done[i], cudaEventDisableTiming);
+            if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&s->copy_done[i], cudaEventDisableTiming);
+        }
+        if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "copy stream/events: %s", cudaGetErrorString(ce));
+    }
     if (!rc) rc = dmalloc(s, &s->G, (size_t)(s->chunk + 2) * (m.mtotal + m.shtotal));
     if (!rc && m.nt_sem > 0) {
         rc = dmalloc(s, &s->tap_psv, 4 * (size_t)m.nt_sem);
@@ -632,8 +646,24 @@ extern "C" int sks_run(sks_solver* s, int32_t nsteps, float* su, float* sv, floa
     cudaSetDevice(s->device);
     const int end = std::min(m.nst, s->step + nsteps);
     const int total = end - s->step;
-    std::vector<float> host((size_t)s->chunk * 3 * std::max(1, m.ntrace));
-    int done = 0;
+    const bool want = m.ntrace > 0 && (su || sv || sw);
+    int done = 0, chunk_i = 0;
+    // a chunk's seismograms are copied out on the copy stream while the next
+    // chunk computes; strided copies put each component straight into the
+    // caller's arrays
+    struct Pending { int slot, n, done; } pend = {-1, 0, 0};
+    auto issue_copy = [&](const Pending& p) -> int {
+        const size_t w = sizeof(float) * (size_t)m.ntrace, sp = 3 * w;
+        float* dst[3] = {su, sv, sw};
+        CK(cudaStreamWaitEvent(s->copy_stream, s->chunk_done[p.slot], 0));
+        for (int c = 0; c < 3; c++)
+            if (dst[c])
+                CK(cudaMemcpy2DAsync(dst[c] + (size_t)p.done * m.ntrace, w, s->seisbuf[p.slot] + (size_t)c * m.ntrace, sp,
+                                     w, (size_t)p.n, cudaMemcpyDeviceToHost, s->copy_stream));
+        CK(cudaEventRecord(s->copy_done[p.slot], s->copy_stream));
+        s->slot_busy[p.slot] = true;
+        return SKS_OK;
+    };
     if (!s->run_ev[0]) {
         CK(cudaEventCreate(&s->run_ev[0]));
         CK(cudaEventCreate(&s->run_ev[1]));
@@ -641,26 +671,31 @@ extern "C" int sks_run(sks_solver* s, int32_t nsteps, float* su, float* sv, floa
     CK(cudaEventRecord(s->run_ev[0], s->stream));
     while (s->step < end) {
         const int n = std::min(s->chunk, end - s->step);
+        const int slot = chunk_i & 1;
+        if (s->slot_busy[slot]) {            // its previous contents are still being copied out
+            CK(cudaStreamWaitEvent(s->stream, s->copy_done[slot], 0));
+            s->slot_busy[slot] = false;
+        }
+        s->seis = s->seisbuf[slot];
         int rc = run_chunk(s, s->step, n);
         if (rc) return rc;
+        if (want) CK(cudaEventRecord(s->chunk_done[slot], s->stream));
         rc = collect_timing(s);
         if (rc) return rc;
-        if (m.ntrace > 0 && (su || sv || sw)) {
-            CK(cudaMemcpyAsync(host.data(), s->seis, sizeof(float) * (size_t)n * 3 * m.ntrace, cudaMemcpyDeviceToHost, s->stream));
-            CK(cudaStreamSynchronize(s->stream));
-            for (int i = 0; i < n; i++) {
-                const float* r = host.data() + (size_t)i * 3 * m.ntrace;
-                const size_t o = (size_t)(done + i) * m.ntrace;
-                if (su) memcpy(su + o, r, sizeof(float) * m.ntrace);
-                if (sv) memcpy(sv + o, r + m.ntrace, sizeof(float) * m.ntrace);
-                if (sw) memcpy(sw + o, r + 2 * m.ntrace, sizeof(float) * m.ntrace);
-            }
-        }
+        if (want && pend.slot >= 0 && (rc = issue_copy(pend))) return rc;
+        pend = want ? Pending{slot, n, done} : Pending{-1, 0, 0};
         s->step += n;
         done += n;
+        chunk_i++;
+    }
+    if (want && pend.slot >= 0) {
+        int rc = issue_copy(pend);
+        if (rc) return rc;
     }
     CK(cudaEventRecord(s->run_ev[1], s->stream));
     CK(cudaStreamSynchronize(s->stream));
+    CK(cudaStreamSynchronize(s->copy_stream));
+    s->slot_busy[0] = s->slot_busy[1] = false;
     {
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, s->run_ev[0], s->run_ev[1]));
@@ -699,6 +734,11 @@ extern "C" void sks_destroy(sks_solver* s)
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_device(s);
     for (cudaEvent_t e : s->kev) cudaEventDestroy(e);
+    for (int i = 0; i < 2; i++) {
+        if (s->chunk_done[i]) cudaEventDestroy(s->chunk_done[i]);
+        if (s->copy_done[i]) cudaEventDestroy(s->copy_done[i]);
+    }
+    if (s->copy_stream) { cudaStreamSynchronize(s->copy_stream); cudaStreamDestroy(s->copy_stream); }
     if (s->run_ev[0]) { cudaEventDestroy(s->run_ev[0]); cudaEventDestroy(s->run_ev[1]); }
     if (s->stream) cudaStreamDestroy(s->stream);
     sks_model_free(&s->m);
