@@ -190,15 +190,18 @@ def lib_run_noout(s, steps: int) -> int:
     return n
 
 
-def run_e2e(d: str, precision: int, steps: int, warmup: int, gpu: int) -> dict:
+def run_e2e(d: str, precision: int, steps: int, warmup: int, gpu: int, tuning=None) -> dict:
     """Through the C ABI with host buffers: upload the run's boundary records from
-    pinned memory, run, read the seismograms back; wall-clock timed."""
+    pinned memory, run, read the seismograms back; wall-clock timed.  The
+    tuning found for the device-resident run is reused (set before timing)."""
     import ctypes as C
     import sks
     cwd = os.getcwd()
     os.chdir(d)
     try:
         s = sks.Solver(["par=run.par", f"nst={steps}"], precision=precision, device=gpu)
+        if tuning:
+            s.set_tuning(tuning["warps_per_block"], tuning["band_rows"], tuning["prefetch"], tuning["register_cap"])
         info = s.info()
         npsv, nsh = info["nrec_psv"] * info["mtotal"], info["nrec_sh"] * info["shtotal"]
         psv, sh = _pinned(npsv), _pinned(nsh)
@@ -343,7 +346,7 @@ def main() -> None:
         torch.cuda.synchronize()
         r32 = run_form(d, 1, a.steps, a.warmup, gpu, clocks=True)
         r64 = run_form(d, 0, min(a.steps, 600), a.warmup, gpu)
-        e2e = run_e2e(d, 1, a.steps, a.warmup, gpu)
+        e2e = run_e2e(d, 1, a.steps, a.warmup, gpu, r32["tuning"])
         torch.cuda.synchronize()
         if dist:
             dist.barrier()

@@ -141,10 +141,11 @@ int sks_open_setup(sks_setup *su, int precision, int device, sks_solver **out);
  * tunable; the default comes from the mesh size and the SM count.  Every
  * tuning gives bit-identical results. */
 typedef struct {
-    int32_t warps_per_block;      /* 2, 4 or 8                              */
+    int32_t warps_per_block;      /* 2 or 4                                 */
     int32_t band_rows;            /* element rows per CTA band              */
     int32_t prefetch;             /* 1: load the next element row early     */
-    int32_t register_cap;         /* 1: cap registers for 16 (FP32) / 8 (FP64) warps per SM */
+    int32_t register_cap;         /* 0: compiler's choice; 1 / 2: registers capped for
+                                     16 / 20 (FP32) or 8 / 12 (FP64) warps per SM */
     int32_t blocks;               /* CTAs per step (output)                 */
     float   ms_per_step;          /* measured by sks_autotune (output)      */
 } sks_tuning_t;

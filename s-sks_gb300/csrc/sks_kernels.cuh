@@ -162,34 +162,42 @@ __device__ __forceinline__ void load_aux(const Field<T>& F, int64_t np, int64_t 
     }
 }
 
+// Where a lane's point sits, as far as the update cares: the lane-constant
+// part of the absorbing-edge, interface-line and receiver tests.
+struct PointFlags {
+    bool edge_x;     // left or right column of the box
+    bool top_ok;     // column 1..3N (the top-row Stacey points)
+    bool on_col;     // the interface column ix == nbl
+    bool row_ok;     // ix >= nbl (the interface row's extent)
+};
+
 // update one owned point, sample it if it is a receiver, then add the next
 // step's boundary increment if it lies on the interface line
 template <typename T, bool LF>
 __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G, const Coef<T>& k,
                                              int ix, int iz, const T u[3], const T K[3], T rinv,
-                                             T wxi, T wzi, const Aux<T, LF>& x)
+                                             T wxi, T wzi, const Aux<T, LF>& x, const PointFlags& pf)
 {
-    const int64_t g = (int64_t)iz * G.nx + ix;
-    const bool edge = ix == 0 || iz == 0 || ix == G.nx - 1 || (iz == G.nz - 1 && ix <= 3 * N);
-    const int64_t bi = edge ? stacey_index(ix, iz, G.nx, G.nz) : -1;
+    const int g = iz * G.nx + ix;
+    const bool edge = pf.edge_x || iz == 0 || (iz == G.nz - 1 && pf.top_ok);
     T un[3], dn[3], cn[3];
     if (!LF) {
-        if (bi < 0) {
+        if (!edge) {
             const T mdt2 = k.dt2_Je * rinv * wxi * wzi;
 #pragma unroll
             for (int c = 0; c < 3; c++) un[c] = (-mdt2 * K[c] + (T)2 * u[c]) - x.a[c];
         } else {
-            const T* p = F.stc + bi * 9;
+            const T* p = F.stc + stacey_index(ix, iz, G.nx, G.nz) * 9;
 #pragma unroll
             for (int c = 0; c < 3; c++) un[c] = (-p[3 * c] * K[c] + p[3 * c + 1] * u[c]) - p[3 * c + 2] * x.a[c];
         }
     } else {
-        if (bi < 0) {
+        if (!edge) {
             const T mdt2 = k.dt2_Je * rinv * wxi * wzi;
 #pragma unroll
             for (int c = 0; c < 3; c++) dn[c] = fma(-mdt2, K[c], x.a[c]);
         } else {
-            const T* p = F.stc + bi * 9;
+            const T* p = F.stc + stacey_index(ix, iz, G.nx, G.nz) * 9;
 #pragma unroll
             for (int c = 0; c < 3; c++) dn[c] = p[3 * c + 2] * x.a[c] - p[3 * c] * K[c];
         }
@@ -213,7 +221,7 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
         }
     }
     // GRT_Interface4 of the next step (sem2d_psvsh.c:2076-2111)
-    if (F.inject_next && ((iz == G.nbl && ix >= G.nbl) || (ix == G.nbl && iz > G.nbl))) {
+    if (F.inject_next && ((iz == G.nbl && pf.row_ok) || (pf.on_col && iz > G.nbl))) {
         const double* g1 = F.gnext;
         const double* g0 = F.gnow;
         const double* v1 = g1 + F.mtotal;
@@ -242,10 +250,11 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
             }
         }
     }
+    const int np = (int)G.np;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        F.un[c * G.np + g] = un[c];
-        if (LF) { F.dv[c * G.np + g] = dn[c]; F.cc[c * G.np + g] = cn[c]; }
+        F.un[c * np + g] = un[c];
+        if (LF) { F.dv[c * np + g] = dn[c]; F.cc[c * np + g] = cn[c]; }
     }
 }
 
@@ -255,10 +264,19 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
 // rows, plus one halo element row below it whose top-row force is carried
 // into the first owned row.  Warps hand the force of their last column to the
 // next warp through shared memory, once per element row.
-// CAP: ask for 16 (FP32) / 8 (FP64) resident warps per SM, i.e. at most
-// 128 / 255 registers a thread; otherwise the compiler's choice.
-template <typename T, bool ANISO, bool LF, int NW, bool PF, bool CAP>
-__global__ void __launch_bounds__(NW * 32, CAP ? (sizeof(T) == 4 ? 16 : 8) / NW : 1)
+//
+// Per element row a lane keeps its 5 displacements (3 components) and 5
+// force accumulators: row b's stress adds its x-divergence to accumulator b
+// and its z-divergence to all five, so no per-point stress is stored.
+//
+// CAP: 0 = the compiler's register choice; 1 / 2 = ask for 16 / 20 (FP32)
+// or 8 / 12 (FP64) resident warps per SM (at most 128 / 102 or 255 / 170
+// registers a thread).
+template <typename T>
+constexpr int cap_warps(int cap) { return cap == 0 ? 0 : (sizeof(T) == 4 ? (cap == 1 ? 16 : 20) : (cap == 1 ? 8 : 12)); }
+
+template <typename T, bool ANISO, bool LF, int NW, bool PF, int CAP>
+__global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
 k_step(Field<T> F, Geo<T> G, Coef<T> k)
 {
     __shared__ T xch[2][NW][N][3];
@@ -271,17 +289,24 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
     const int q = TEX * w + e;                     // element within the CTA
     const int ex = cx * S - 1 + q;
     const bool live = lane < 30 && ex >= 0 && ex < G.nex;
-    const int ix = live ? ex * N + al : 0;
+    const int nx = G.nx;
+    // lanes off the mesh read a valid column; their force never reaches a
+    // live lane (shuffles stay inside an element, the left neighbour is masked)
+    const int ix = live ? ex * N + al : min(max(ex * N + al, 0), nx - 1);
     const bool own_x = live && q >= 1 && (al < N || ex == G.nex - 1);
     const int ez0 = cz * G.HZ, ez1 = min(ez0 + G.HZ, G.nez);
     const int ezs = ez0 > 0 ? ez0 - 1 : 0;
     const int base = e * NP;
-    const bool add_left = al == 0 && (e > 0 || w > 0);
-    const int nx = G.nx;
-    const int np = (int)G.np;                      // < 2^31 (checked on the host)
+    const bool add_left = al == 0 && (e > 0 || w > 0) && ex > 0;
+    const int np = (int)G.np;                      // 3*np < 2^31 (checked on the host)
     const T* __restrict__ U0 = F.uc;
     const T* __restrict__ U1 = F.uc + np;
     const T* __restrict__ U2 = F.uc + 2 * np;
+    PointFlags pfl;
+    pfl.edge_x = ix == 0 || ix == nx - 1;
+    pfl.top_ok = ix >= 1 && ix <= 3 * N;
+    pfl.on_col = ix == G.nbl;
+    pfl.row_ok = ix >= G.nbl;
 
     T Dx[NP], DWc[NP];
 #pragma unroll
@@ -289,7 +314,7 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
     const T wal = k.w[al];
     // lumped-mass weight of this lane's column: inside an element, on an
     // element edge shared by two elements, or on the box's left/right edge
-    const T wxi = (al > 0 && al < N) ? k.winv[al] : ((ix == 0 || ix == nx - 1) ? k.winv[0] : k.winv2);
+    const T wxi = (al > 0 && al < N) ? k.winv[al] : (pfl.edge_x ? k.winv[0] : k.winv2);
 
     T u[NP][3];
     uint16_t m[NP];
@@ -305,10 +330,8 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 #pragma unroll
         for (int b = 0; b < NP; b++) {
             const int g = o + b * nx;
-            u[b][0] = live ? U0[g] : (T)0;
-            u[b][1] = live ? U1[g] : (T)0;
-            u[b][2] = live ? U2[g] : (T)0;
-            m[b] = live ? F.mid[g] : (uint16_t)0;
+            u[b][0] = U0[g]; u[b][1] = U1[g]; u[b][2] = U2[g];
+            m[b] = F.mid[g];
         }
     }
     if (PF && ezs + 1 < ez1) {
@@ -316,10 +339,8 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 #pragma unroll
         for (int b = 0; b < N; b++) {
             const int g = o + (b + 1) * nx;
-            un_[b][0] = live ? U0[g] : (T)0;
-            un_[b][1] = live ? U1[g] : (T)0;
-            un_[b][2] = live ? U2[g] : (T)0;
-            mn[b] = live ? F.mid[g] : (uint16_t)0;
+            un_[b][0] = U0[g]; un_[b][1] = U1[g]; un_[b][2] = U2[g];
+            mn[b] = F.mid[g];
         }
     }
     int par = 0;
@@ -341,10 +362,8 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 #pragma unroll
                 for (int b = 1; b < NP; b++) {
                     const int g = o + b * nx;
-                    u[b][0] = live ? U0[g] : (T)0;
-                    u[b][1] = live ? U1[g] : (T)0;
-                    u[b][2] = live ? U2[g] : (T)0;
-                    m[b] = live ? F.mid[g] : (uint16_t)0;
+                    u[b][0] = U0[g]; u[b][1] = U1[g]; u[b][2] = U2[g];
+                    m[b] = F.mid[g];
                 }
             }
         }
@@ -353,10 +372,8 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 #pragma unroll
             for (int b = 0; b < N; b++) {
                 const int g = o + (b + 1) * nx;
-                un_[b][0] = live ? U0[g] : (T)0;
-                un_[b][1] = live ? U1[g] : (T)0;
-                un_[b][2] = live ? U2[g] : (T)0;
-                mn[b] = live ? F.mid[g] : (uint16_t)0;
+                un_[b][0] = U0[g]; un_[b][1] = U1[g]; un_[b][2] = U2[g];
+                mn[b] = F.mid[g];
             }
         }
         Aux<T, LF> aux[N];
@@ -364,57 +381,52 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 #pragma unroll
             for (int b = 0; b < N; b++) load_aux<T, LF>(F, G.np, (int64_t)(ez * N + b) * nx + ix, aux[b]);
         }
-        T item0[NP][3], F2[NP][3];
+        T kk[NP][3];
+#pragma unroll
+        for (int b = 0; b < NP; b++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) kk[b][c] = (ez > ezs && b == 0) ? kc[c] : (T)0;
         T rinv[NP];
 #pragma unroll
-        for (int b = 0; b < NP; b++) {
+        for (int bb = 0; bb < NP; bb++) {
             T dx[3], dz[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 T s = 0;
 #pragma unroll
-                for (int t = 0; t < NP; t++) s = fma(__shfl_sync(FULL, u[b][c], base + t), Dx[t], s);
+                for (int t = 0; t < NP; t++) s = fma(__shfl_sync(FULL, u[bb][c], base + t), Dx[t], s);
                 dx[c] = s;
                 T z = 0;
 #pragma unroll
-                for (int t = 0; t < NP; t++) z = fma(u[t][c], k.D[b * NP + t], z);
+                for (int t = 0; t < NP; t++) z = fma(u[t][c], k.D[bb * NP + t], z);
                 dz[c] = z;
             }
             const T ee[5] = {dx[0], dx[1], dx[2] + dz[0], dz[1], dz[2]};
-            if ((int)m[b] != mcur) {                 // layered models: rarely taken
-                M.load(F.mat + (size_t)m[b] * MAT_STRIDE);
-                mcur = m[b];
+            if ((int)m[bb] != mcur) {                // layered models: rarely taken
+                M.load(F.mat + (size_t)m[bb] * MAT_STRIDE);
+                mcur = m[bb];
             }
-            rinv[b] = M.s[15];
+            rinv[bb] = M.s[15];
             T sg[5];
             stress<T, ANISO>(M, ee, sg);
-            F2[b][0] = sg[2]; F2[b][1] = sg[3]; F2[b][2] = sg[4];
-            // the halo element row only hands its top row's force upward
-            if (!halo || b == N) {
+            // x-divergence of row bb (the halo element row only needs its top row)
+            if (!halo || bb == N) {
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
                     T s = 0;
 #pragma unroll
                     for (int a = 0; a < NP; a++) s = fma(__shfl_sync(FULL, sg[c], base + a), DWc[a], s);
-                    item0[b][c] = s;
+                    kk[bb][c] = fma(s, k.w[bb], kk[bb][c]);
                 }
             }
-        }
-        T kk[NP][3];
+            // z-divergence: row bb's stress feeds every row of the element
+            const T f2[3] = {sg[2] * wal, sg[3] * wal, sg[4] * wal};
 #pragma unroll
-        for (int b = 0; b < NP; b++) {
-            if (halo && b < N) continue;
+            for (int b = 0; b < NP; b++) {
+                if (halo && b < N) continue;
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-                T s = 0;
-#pragma unroll
-                for (int bb = 0; bb < NP; bb++) s = fma(F2[bb][c], k.DWs[bb * NP + b], s);
-                kk[b][c] = live ? fma(item0[b][c], k.w[b], s * wal) : (T)0;
+                for (int c = 0; c < 3; c++) kk[b][c] = fma(f2[c], k.DWs[bb * NP + b], kk[b][c]);
             }
-        }
-        if (ez > ezs) {
-#pragma unroll
-            for (int c = 0; c < 3; c++) kk[0][c] = kc[c] + kk[0][c];
         }
 #pragma unroll
         for (int c = 0; c < 3; c++) kc[c] = kk[N][c];
@@ -434,12 +446,12 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
                     T left = __shfl_up_sync(FULL, kk[b][c], 1);
-                    if (e == 0) left = w > 0 ? xch[par][w > 0 ? w - 1 : 0][b][c] : (T)0;
+                    if (e == 0) left = xch[par][w > 0 ? w - 1 : 0][b][c];
                     kt[c] = add_left ? left + kk[b][c] : kk[b][c];
                 }
                 if (own_x) {
                     const T wzi = b > 0 ? k.winv[b] : (ez == 0 ? k.winv[0] : k.winv2);
-                    finish_point<T, LF>(F, G, k, ix, ez * N + b, u[b], kt, rinv[b], wxi, wzi, aux[b]);
+                    finish_point<T, LF>(F, G, k, ix, ez * N + b, u[b], kt, rinv[b], wxi, wzi, aux[b], pfl);
                 }
             }
             par ^= 1;
@@ -456,14 +468,14 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             T left = __shfl_up_sync(FULL, kc[c], 1);
-            if (e == 0) left = w > 0 ? xtop[w > 0 ? w - 1 : 0][c] : (T)0;
+            if (e == 0) left = xtop[w > 0 ? w - 1 : 0][c];
             kt[c] = add_left ? left + kc[c] : kc[c];
         }
         if (own_x) {
             const int iz = G.nz - 1;
             Aux<T, LF> x;
             load_aux<T, LF>(F, G.np, (int64_t)iz * nx + ix, x);
-            finish_point<T, LF>(F, G, k, ix, iz, u[N], kt, rinvN, wxi, k.winv[0], x);
+            finish_point<T, LF>(F, G, k, ix, iz, u[N], kt, rinvN, wxi, k.winv[0], x, pfl);
         }
     }
 }

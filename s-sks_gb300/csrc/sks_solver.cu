@@ -234,12 +234,11 @@ int collect_timing(sks_solver* s)
     return SKS_OK;
 }
 
-// CTA band height: at least ~4 resident CTAs' worth of work per SM for the
-// grid, and bands as tall as that allows (each band recomputes one element
-// row below it)
-int pick_band(const sks_model& m, int ncx, int sm_count)
+// CTA band height: at least `per_sm` CTAs per SM in the grid, and bands as
+// tall as that allows (each band recomputes one element row below it)
+int pick_band(const sks_model& m, int ncx, int sm_count, int per_sm)
 {
-    const int64_t target = (int64_t)sm_count * 4;
+    const int64_t target = (int64_t)sm_count * per_sm;
     const int cands[] = {32, 24, 16, 12, 10, 8, 6, 4, 3, 2};
     for (int hz : cands) {
         if (hz > m.nez) continue;
@@ -490,8 +489,12 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         return set_err(SKS_ERR_UNSUPPORTED, "mesh of %d x %d points: 3*nx*nz must stay below 2^31", m.nx, m.nz);
     }
     {
+        // defaults from sweeps on the 3.8 M-point anisotropic mesh: FP32 runs
+        // best with many short bands and registers capped for 16 warps/SM,
+        // FP64 (bound by the FP64 pipe) with fewer, taller bands and prefetch
         const int ncx4 = (m.nex + (TEX * 4 - 1) - 1) / (TEX * 4 - 1);
-        set_grid(s, 4, pick_band(m, ncx4, sms), 0, 0);
+        if (precision == SKS_FP32C) set_grid(s, 4, pick_band(m, ncx4, sms, 10), 0, 1);
+        else set_grid(s, 4, pick_band(m, ncx4, sms, 5), 1, 0);
     }
     s->chunk = 64;
     const size_t np = (size_t)m.nx * m.nz;
@@ -769,10 +772,12 @@ extern "C" int sks_kernel_timing(const sks_solver* s, double* ms, int64_t* count
 extern "C" int sks_set_tuning(sks_solver* s, const sks_tuning_t* t)
 {
     if (!s || !t) return set_err(SKS_ERR_ARG, "NULL argument");
-    if (t->warps_per_block != 2 && t->warps_per_block != 4 && t->warps_per_block != 8)
-        return set_err(SKS_ERR_ARG, "warps_per_block=%d: 2, 4 or 8", t->warps_per_block);
+    if (t->warps_per_block != 2 && t->warps_per_block != 4)
+        return set_err(SKS_ERR_ARG, "warps_per_block=%d: 2 or 4", t->warps_per_block);
+    if (t->register_cap < 0 || t->register_cap > 2)
+        return set_err(SKS_ERR_ARG, "register_cap=%d: 0, 1 or 2", t->register_cap);
     if (t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
-    set_grid(s, t->warps_per_block, t->band_rows, t->prefetch ? 1 : 0, t->register_cap ? 1 : 0);
+    set_grid(s, t->warps_per_block, t->band_rows, t->prefetch ? 1 : 0, t->register_cap);
     return SKS_OK;
 }
 
@@ -843,12 +848,12 @@ extern "C" int sks_autotune(sks_solver* s, int32_t steps, sks_tuning_t* best)
     if (rc) return rc;
     const int old_timing = s->timing;
     s->timing = 0;
-    const int nws[] = {2, 4, 8};
+    const int nws[] = {2, 4};
     const int hzs[] = {4, 6, 8, 12, 16, 24, 32};
     sks_tuning_t b = {s->NW, s->HZ, s->PF, s->CAP, s->nblocks, 1e30f};
     for (int nw : nws)
         for (int pf = 0; pf < 2; pf++)
-          for (int cap = 0; cap < 2; cap++)
+          for (int cap = 0; cap < 3; cap++)
             for (int hz : hzs) {
                 if (hz > m.nez && hz != hzs[0]) continue;
                 if ((rc = snap_restore(s, snap))) break;

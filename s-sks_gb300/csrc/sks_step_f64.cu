@@ -5,7 +5,7 @@
 namespace sks {
 namespace {
 
-template <bool ANISO, int NW, bool PF, bool CAP>
+template <bool ANISO, int NW, bool PF, int CAP>
 void go(int blocks, cudaStream_t st, const Field<double>& F, const Geo<double>& G, const Coef<double>& k)
 {
     k_step<double, ANISO, false, NW, PF, CAP><<<blocks, NW * 32, 0, st>>>(F, G, k);
@@ -16,11 +16,13 @@ void go_nw(const StepVariant& v, int blocks, cudaStream_t st, const Field<double
            const Coef<double>& k)
 {
     if (v.prefetch) {
-        if (v.cap) go<ANISO, NW, true, true>(blocks, st, F, G, k);
-        else go<ANISO, NW, true, false>(blocks, st, F, G, k);
+        if (v.cap == 2) go<ANISO, NW, true, 2>(blocks, st, F, G, k);
+        else if (v.cap == 1) go<ANISO, NW, true, 1>(blocks, st, F, G, k);
+        else go<ANISO, NW, true, 0>(blocks, st, F, G, k);
     } else {
-        if (v.cap) go<ANISO, NW, false, true>(blocks, st, F, G, k);
-        else go<ANISO, NW, false, false>(blocks, st, F, G, k);
+        if (v.cap == 2) go<ANISO, NW, false, 2>(blocks, st, F, G, k);
+        else if (v.cap == 1) go<ANISO, NW, false, 1>(blocks, st, F, G, k);
+        else go<ANISO, NW, false, 0>(blocks, st, F, G, k);
     }
 }
 
@@ -28,11 +30,8 @@ template <bool ANISO>
 void go_aniso(const StepVariant& v, int blocks, cudaStream_t st, const Field<double>& F, const Geo<double>& G,
               const Coef<double>& k)
 {
-    switch (v.nw) {
-    case 2: go_nw<ANISO, 2>(v, blocks, st, F, G, k); break;
-    case 8: go_nw<ANISO, 8>(v, blocks, st, F, G, k); break;
-    default: go_nw<ANISO, 4>(v, blocks, st, F, G, k); break;
-    }
+    if (v.nw == 2) go_nw<ANISO, 2>(v, blocks, st, F, G, k);
+    else go_nw<ANISO, 4>(v, blocks, st, F, G, k);
 }
 
 }  // namespace

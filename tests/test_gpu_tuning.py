@@ -48,7 +48,7 @@ def _run(d, prec, nst, tuning=None, autotune=False):
         return out, got, s.tuning()
 
 
-TUNINGS = [(nw, hz, pf, cap) for nw in (2, 4, 8) for hz in (1, 3, 23) for pf in (0, 1) for cap in (0, 1)]
+TUNINGS = [(nw, hz, pf, cap) for nw in (2, 4) for hz in (1, 3, 23) for pf in (0, 1) for cap in (0, 1, 2)]
 
 
 @pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])
