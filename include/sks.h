@@ -136,14 +136,15 @@ int sks_open_setup(sks_setup *su, int precision, int device, sks_solver **out);
 
 /* ---- tuning -------------------------------------------------------------
  * The step kernel runs one CTA per (column of 6*W-1 elements, band of B
- * element rows); each CTA recomputes one element column and one element row
- * of halo.  W (warps per CTA), B, a prefetch variant and a register cap are
- * tunable; the default comes from the mesh size and the SM count.  Every
- * tuning gives bit-identical results. */
+ * element rows); each CTA recomputes one element column of halo.  W (warps per CTA), B, the band-seam method and a register cap
+ * are tunable; the default comes from the mesh size and the SM count.
+ * Every tuning gives bit-identical results. */
 typedef struct {
     int32_t warps_per_block;      /* 2 or 4                                 */
     int32_t band_rows;            /* element rows per CTA band              */
-    int32_t prefetch;             /* 1: load the next element row early     */
+    int32_t zseam;                /* 0: each band recomputes the element row below
+                                     it; 1: bands exchange boundary-row partial
+                                     forces (the later band sums them)      */
     int32_t register_cap;         /* 0: compiler's choice; 1 / 2: registers capped for
                                      16 / 20 (FP32) or 8 / 12 (FP64) warps per SM */
     int32_t blocks;               /* CTAs per step (output)                 */

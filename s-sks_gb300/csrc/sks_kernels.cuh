@@ -81,6 +81,13 @@ struct Field {
     int nrec, ntrace;
     int rec_iz0, rec_iz1;                    // rows holding receivers
     float* __restrict__ seis_row;            // [3][ntrace] of this step
+    // band seams (ZS variants): the force a band-boundary row gets from the
+    // band below (lo) and the band above (hi), [segment][nx][6] = the left
+    // element's part (3) and the own element's part (3), and one arrival
+    // counter per (segment, CTA column)
+    T* __restrict__ seam_lo;
+    T* __restrict__ seam_hi;
+    int* __restrict__ seam_cnt;
 };
 
 __device__ __forceinline__ int64_t stacey_index(int ix, int iz, int nx, int nz)
@@ -260,10 +267,14 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
 
 // The SEM step.  CTA = NW warps side by side in x: 6*NW elements, the first
 // one a halo (recomputed, owned by the CTA to the left), so every owned point
-// receives all its element contributions inside the CTA; a band of HZ element
-// rows, plus one halo element row below it whose top-row force is carried
-// into the first owned row.  Warps hand the force of their last column to the
-// next warp through shared memory, once per element row.
+// receives all its x contributions inside the CTA; a band of HZ element rows.
+// Warps hand the force of their last column to the next warp through shared
+// memory, once per element row.  The row between two bands takes force from
+// both: with ZS=false each band recomputes the element row below it (halo);
+// with ZS=true each band writes its partial force of the boundary row to
+// global memory and bumps the segment's arrival counter, and the band that
+// arrives second adds the two partials (lower band first) and updates the
+// row -- nothing waits and nothing is computed twice.
 //
 // Per element row a lane keeps its 5 displacements (3 components) and 5
 // force accumulators: row b's stress adds its x-divergence to accumulator b
@@ -275,12 +286,13 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
 template <typename T>
 constexpr int cap_warps(int cap) { return cap == 0 ? 0 : (sizeof(T) == 4 ? (cap == 1 ? 16 : 20) : (cap == 1 ? 8 : 12)); }
 
-template <typename T, bool ANISO, bool LF, int NW, bool PF, int CAP>
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP>
 __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
 k_step(Field<T> F, Geo<T> G, Coef<T> k)
 {
     __shared__ T xch[2][NW][N][3];
     __shared__ T xtop[NW][3];
+    __shared__ int second_arrival;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int cx = blockIdx.x % G.ncx, cz = blockIdx.x / G.ncx;
@@ -295,7 +307,7 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
     const int ix = live ? ex * N + al : min(max(ex * N + al, 0), nx - 1);
     const bool own_x = live && q >= 1 && (al < N || ex == G.nex - 1);
     const int ez0 = cz * G.HZ, ez1 = min(ez0 + G.HZ, G.nez);
-    const int ezs = ez0 > 0 ? ez0 - 1 : 0;
+    const int ezs = (!ZS && ez0 > 0) ? ez0 - 1 : ez0;
     const int base = e * NP;
     const bool add_left = al == 0 && (e > 0 || w > 0) && ex > 0;
     const int np = (int)G.np;                      // 3*np < 2^31 (checked on the host)
@@ -318,8 +330,6 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 
     T u[NP][3];
     uint16_t m[NP];
-    T un_[N][3];                 // next element row, rows 1..N (prefetch)
-    uint16_t mn[N];
     T kc[3] = {0, 0, 0};
     T rinvN = 0;
     MatRow<T, ANISO> M;
@@ -334,46 +344,19 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
             m[b] = F.mid[g];
         }
     }
-    if (PF && ezs + 1 < ez1) {
-        const int o = (ezs + 1) * N * nx + ix;
-#pragma unroll
-        for (int b = 0; b < N; b++) {
-            const int g = o + (b + 1) * nx;
-            un_[b][0] = U0[g]; un_[b][1] = U1[g]; un_[b][2] = U2[g];
-            mn[b] = F.mid[g];
-        }
-    }
     int par = 0;
     for (int ez = ezs; ez < ez1; ++ez) {
-        const bool halo = ez < ez0;
+        const bool halo = !ZS && ez < ez0;
         if (ez > ezs) {
 #pragma unroll
             for (int c = 0; c < 3; c++) u[0][c] = u[N][c];
             m[0] = m[N];
-            if (PF) {
+            const int o = ez * N * nx + ix;
 #pragma unroll
-                for (int b = 0; b < N; b++) {
-#pragma unroll
-                    for (int c = 0; c < 3; c++) u[b + 1][c] = un_[b][c];
-                    m[b + 1] = mn[b];
-                }
-            } else {
-                const int o = ez * N * nx + ix;
-#pragma unroll
-                for (int b = 1; b < NP; b++) {
-                    const int g = o + b * nx;
-                    u[b][0] = U0[g]; u[b][1] = U1[g]; u[b][2] = U2[g];
-                    m[b] = F.mid[g];
-                }
-            }
-        }
-        if (PF && ez + 1 < ez1) {
-            const int o = (ez + 1) * N * nx + ix;
-#pragma unroll
-            for (int b = 0; b < N; b++) {
-                const int g = o + (b + 1) * nx;
-                un_[b][0] = U0[g]; un_[b][1] = U1[g]; un_[b][2] = U2[g];
-                mn[b] = F.mid[g];
+            for (int b = 1; b < NP; b++) {
+                const int g = o + b * nx;
+                u[b][0] = U0[g]; u[b][1] = U1[g]; u[b][2] = U2[g];
+                m[b] = F.mid[g];
             }
         }
         Aux<T, LF> aux[N];
@@ -385,7 +368,7 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 #pragma unroll
         for (int b = 0; b < NP; b++)
 #pragma unroll
-            for (int c = 0; c < 3; c++) kk[b][c] = (ez > ezs && b == 0) ? kc[c] : (T)0;
+            for (int c = 0; c < 3; c++) kk[b][c] = (T)0;
         T rinv[NP];
 #pragma unroll
         for (int bb = 0; bb < NP; bb++) {
@@ -409,7 +392,7 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
             rinv[bb] = M.s[15];
             T sg[5];
             stress<T, ANISO>(M, ee, sg);
-            // x-divergence of row bb (the halo element row only needs its top row)
+            // x-divergence of row bb (a halo element row only needs its top row)
             if (!halo || bb == N) {
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
@@ -428,6 +411,11 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
                 for (int c = 0; c < 3; c++) kk[b][c] = fma(f2[c], k.DWs[bb * NP + b], kk[b][c]);
             }
         }
+        // the element row below contributed to row 0 first (the reference's order)
+        if (ez > ezs) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) kk[0][c] = kc[c] + kk[0][c];
+        }
 #pragma unroll
         for (int c = 0; c < 3; c++) kc[c] = kk[N][c];
         rinvN = rinv[N];
@@ -440,42 +428,98 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
                     for (int c = 0; c < 3; c++) xch[par][w][b][c] = kk[b][c];
             }
             __syncthreads();
+            const bool seam_row0 = ZS && ez == ez0 && ez0 > 0;
 #pragma unroll
             for (int b = 0; b < N; b++) {
-                T kt[3];
+                T kt[3], lft[3];
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
                     T left = __shfl_up_sync(FULL, kk[b][c], 1);
                     if (e == 0) left = xch[par][w > 0 ? w - 1 : 0][b][c];
+                    lft[c] = add_left ? left : (T)0;
                     kt[c] = add_left ? left + kk[b][c] : kk[b][c];
+                }
+                if (b == 0 && seam_row0) {
+                    // the band's bottom row: publish this band's parts of its force
+                    if (own_x) {
+                        T* p = F.seam_hi + ((size_t)cz * nx + ix) * 6;
+#pragma unroll
+                        for (int c = 0; c < 3; c++) { p[c] = lft[c]; p[3 + c] = kk[0][c]; }
+                    }
+                    continue;
                 }
                 if (own_x) {
                     const T wzi = b > 0 ? k.winv[b] : (ez == 0 ? k.winv[0] : k.winv2);
                     finish_point<T, LF>(F, G, k, ix, ez * N + b, u[b], kt, rinv[b], wxi, wzi, aux[b], pfl);
                 }
             }
+            if (seam_row0) {
+                __threadfence();
+                __syncthreads();
+                if (threadIdx.x == 0) second_arrival = atomicAdd(F.seam_cnt + cz * G.ncx + cx, 1) & 1;
+                __syncthreads();
+                if (second_arrival) {
+                    __threadfence();
+                    if (own_x) {
+                        // (left carry + left row) + (own carry + own row), as inside a band
+                        const T* lo = F.seam_lo + ((size_t)cz * nx + ix) * 6;
+                        const T* hi = F.seam_hi + ((size_t)cz * nx + ix) * 6;
+                        T K[3];
+#pragma unroll
+                        for (int c = 0; c < 3; c++)
+                            K[c] = (__ldcg(lo + c) + __ldcg(hi + c)) + (__ldcg(lo + 3 + c) + __ldcg(hi + 3 + c));
+                        finish_point<T, LF>(F, G, k, ix, ez0 * N, u[0], K, rinv[0], wxi, k.winv2, aux[0], pfl);
+                    }
+                }
+            }
             par ^= 1;
         }
     }
-    if (ez1 == G.nez) {
-        // the domain's top row: no element above, complete now
+    // the band's top row: the box's top (complete now) or a seam with the band above
+    if (ez1 == G.nez || ZS) {
         if (lane == 29) {
 #pragma unroll
             for (int c = 0; c < 3; c++) xtop[w][c] = kc[c];
         }
         __syncthreads();
-        T kt[3];
+        T kt[3], lft[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             T left = __shfl_up_sync(FULL, kc[c], 1);
             if (e == 0) left = xtop[w > 0 ? w - 1 : 0][c];
+            lft[c] = add_left ? left : (T)0;
             kt[c] = add_left ? left + kc[c] : kc[c];
         }
-        if (own_x) {
-            const int iz = G.nz - 1;
-            Aux<T, LF> x;
-            load_aux<T, LF>(F, G.np, (int64_t)iz * nx + ix, x);
-            finish_point<T, LF>(F, G, k, ix, iz, u[N], kt, rinvN, wxi, k.winv[0], x, pfl);
+        const int iz = ez1 * N;
+        if (ez1 == G.nez) {
+            if (own_x) {
+                Aux<T, LF> x;
+                load_aux<T, LF>(F, G.np, (int64_t)iz * nx + ix, x);
+                finish_point<T, LF>(F, G, k, ix, iz, u[N], kt, rinvN, wxi, k.winv[0], x, pfl);
+            }
+        } else {
+            if (own_x) {
+                T* p = F.seam_lo + ((size_t)(cz + 1) * nx + ix) * 6;
+#pragma unroll
+                for (int c = 0; c < 3; c++) { p[c] = lft[c]; p[3 + c] = kc[c]; }
+            }
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0) second_arrival = atomicAdd(F.seam_cnt + (cz + 1) * G.ncx + cx, 1) & 1;
+            __syncthreads();
+            if (second_arrival) {
+                __threadfence();
+                if (own_x) {
+                    const T* hi = F.seam_hi + ((size_t)(cz + 1) * nx + ix) * 6;
+                    T K[3];
+#pragma unroll
+                    for (int c = 0; c < 3; c++)
+                        K[c] = (lft[c] + __ldcg(hi + c)) + (kc[c] + __ldcg(hi + 3 + c));
+                    Aux<T, LF> x;
+                    load_aux<T, LF>(F, G.np, (int64_t)iz * nx + ix, x);
+                    finish_point<T, LF>(F, G, k, ix, iz, u[N], K, rinvN, wxi, k.winv2, x, pfl);
+                }
+            }
         }
     }
 }
@@ -483,7 +527,7 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 }  // namespace sks
 
 namespace sks {
-struct StepVariant { int nw; int prefetch; int cap; };
+struct StepVariant { int nw; int zseam; int cap; };
 cudaError_t launch_step_f32(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
                             const Field<float>& F, const Geo<float>& G, const Coef<float>& k);
 cudaError_t launch_step_f64(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,

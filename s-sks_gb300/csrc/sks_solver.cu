@@ -44,7 +44,11 @@ struct sks_solver {
     int64_t launches;
     cudaStream_t stream;
     // geometry: CTA grid of the step kernel (tunable)
-    int NW, ncx, ncz, HZ, nblocks, PF, CAP;
+    int NW, ncx, ncz, HZ, nblocks, ZS, CAP;
+    void* seam_lo;             // band-seam partial forces (grow-only)
+    void* seam_hi;
+    int* seam_cnt;
+    size_t seam_bytes, seam_cnt_n;
     int sms;
     int nbl;
     // device buffers
@@ -188,13 +192,14 @@ void free_device(sks_solver* s)
 {
     void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc,
                   s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seisbuf[0], s->seisbuf[1], s->G, s->rec_psv, s->rec_sh,
-                  s->tap_psv, s->tap_sh, s->w_psv, s->w_sh};
+                  s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt};
     for (void* p : ps)
         if (p) cudaFree(p);
     s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = nullptr;
     s->mid = nullptr; s->rec_off = nullptr; s->recbits = nullptr; s->rec_sorted = nullptr; s->rec_idx = nullptr;
     s->seis = nullptr; s->seisbuf[0] = s->seisbuf[1] = nullptr; s->G = nullptr;
     s->rec_psv = s->rec_sh = nullptr; s->tap_psv = s->tap_sh = nullptr; s->w_psv = s->w_sh = nullptr;
+    s->seam_lo = s->seam_hi = nullptr; s->seam_cnt = nullptr; s->seam_bytes = 0; s->seam_cnt_n = 0;
 }
 
 // per-kernel-class timing: an event pair around each launch when enabled
@@ -337,6 +342,9 @@ Field<T> make_field(sks_solver* s)
     F.ntrace = s->m.ntrace;
     F.rec_iz0 = s->rec_iz0;
     F.rec_iz1 = s->rec_iz1;
+    F.seam_lo = (T*)s->seam_lo;
+    F.seam_hi = (T*)s->seam_hi;
+    F.seam_cnt = s->seam_cnt;
     return F;
 }
 
@@ -351,16 +359,40 @@ Geo<T> make_geo(const sks_solver* s)
     return G;
 }
 
-// CTA grid for a tuning: NW warps (6*NW-1 owned elements) by bands of HZ rows
-void set_grid(sks_solver* s, int NW, int HZ, int PF, int CAP)
+// CTA grid for a tuning: NW warps (6*NW-1 owned elements) by bands of HZ
+// rows; the band-seam buffers grow to fit and their counters restart at 0
+int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP)
 {
     s->NW = NW;
-    s->PF = PF;
+    s->ZS = ZS;
     s->CAP = CAP;
     s->ncx = (s->m.nex + (TEX * NW - 1) - 1) / (TEX * NW - 1);
     s->HZ = std::max(1, std::min(HZ, s->m.nez));
     s->ncz = (s->m.nez + s->HZ - 1) / s->HZ;
     s->nblocks = s->ncx * s->ncz;
+    if (!ZS) return SKS_OK;
+    const size_t el = s->precision == SKS_FP64 ? sizeof(double) : sizeof(float);
+    const size_t need = (size_t)s->ncz * s->m.nx * 6 * el;
+    const size_t ncnt = (size_t)s->ncz * s->ncx;
+    if (need > s->seam_bytes) {
+        if (s->seam_lo) { cudaFree(s->seam_lo); cudaFree(s->seam_hi); s->device_bytes -= 2 * (int64_t)s->seam_bytes; }
+        s->seam_lo = s->seam_hi = nullptr;
+        s->seam_bytes = 0;
+        CK(cudaMalloc(&s->seam_lo, need));
+        CK(cudaMalloc(&s->seam_hi, need));
+        s->seam_bytes = need;
+        s->device_bytes += 2 * (int64_t)need;
+    }
+    if (ncnt > s->seam_cnt_n) {
+        if (s->seam_cnt) { cudaFree(s->seam_cnt); s->device_bytes -= 4 * (int64_t)s->seam_cnt_n; }
+        s->seam_cnt = nullptr;
+        s->seam_cnt_n = 0;
+        CK(cudaMalloc(&s->seam_cnt, ncnt * sizeof(int)));
+        s->seam_cnt_n = ncnt;
+        s->device_bytes += 4 * (int64_t)ncnt;
+    }
+    CK(cudaMemsetAsync(s->seam_cnt, 0, ncnt * sizeof(int), s->stream));
+    return SKS_OK;
 }
 
 // one time step it >= 1: a single fused kernel (force, assembly, update,
@@ -379,7 +411,7 @@ int step_impl(sks_solver* s, int it, const double* Gcur, const double* Gnext, fl
     k = make_coef<T>(m);
     {
         KTimer t(s, SKS_KC_ELEMENT);
-        const StepVariant v{s->NW, s->PF, s->CAP};
+        const StepVariant v{s->NW, s->ZS, s->CAP};
         if (sizeof(T) == 4)
             launch_step_f32(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<float>*)&F,
                             *(const Geo<float>*)&G, *(const Coef<float>*)&k);
@@ -491,10 +523,11 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
     {
         // defaults from sweeps on the 3.8 M-point anisotropic mesh: FP32 runs
         // best with many short bands and registers capped for 16 warps/SM,
-        // FP64 (bound by the FP64 pipe) with fewer, taller bands and prefetch
+        // FP64 (bound by the FP64 pipe) with fewer, taller bands
         const int ncx4 = (m.nex + (TEX * 4 - 1) - 1) / (TEX * 4 - 1);
-        if (precision == SKS_FP32C) set_grid(s, 4, pick_band(m, ncx4, sms, 10), 0, 1);
-        else set_grid(s, 4, pick_band(m, ncx4, sms, 5), 1, 0);
+        const int rcg = precision == SKS_FP32C ? set_grid(s, 4, pick_band(m, ncx4, sms, 10), 1, 1)
+                                               : set_grid(s, 4, pick_band(m, ncx4, sms, 5), 1, 0);
+        if (rcg) { free_device(s); cudaStreamDestroy(s->stream); sks_model_free(&s->m); delete s; return rcg; }
     }
     s->chunk = 64;
     const size_t np = (size_t)m.nx * m.nz;
@@ -777,8 +810,7 @@ extern "C" int sks_set_tuning(sks_solver* s, const sks_tuning_t* t)
     if (t->register_cap < 0 || t->register_cap > 2)
         return set_err(SKS_ERR_ARG, "register_cap=%d: 0, 1 or 2", t->register_cap);
     if (t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
-    set_grid(s, t->warps_per_block, t->band_rows, t->prefetch ? 1 : 0, t->register_cap);
-    return SKS_OK;
+    return set_grid(s, t->warps_per_block, t->band_rows, t->zseam ? 1 : 0, t->register_cap);
 }
 
 extern "C" int sks_get_tuning(const sks_solver* s, sks_tuning_t* t)
@@ -786,7 +818,7 @@ extern "C" int sks_get_tuning(const sks_solver* s, sks_tuning_t* t)
     if (!s || !t) return set_err(SKS_ERR_ARG, "NULL argument");
     t->warps_per_block = s->NW;
     t->band_rows = s->HZ;
-    t->prefetch = s->PF;
+    t->zseam = s->ZS;
     t->register_cap = s->CAP;
     t->blocks = s->nblocks;
     t->ms_per_step = 0.f;
@@ -850,29 +882,30 @@ extern "C" int sks_autotune(sks_solver* s, int32_t steps, sks_tuning_t* best)
     s->timing = 0;
     const int nws[] = {2, 4};
     const int hzs[] = {4, 6, 8, 12, 16, 24, 32};
-    sks_tuning_t b = {s->NW, s->HZ, s->PF, s->CAP, s->nblocks, 1e30f};
+    sks_tuning_t b = {s->NW, s->HZ, s->ZS, s->CAP, s->nblocks, 1e30f};
     for (int nw : nws)
-        for (int pf = 0; pf < 2; pf++)
+        for (int zs = 0; zs < 2; zs++)
           for (int cap = 0; cap < 3; cap++)
             for (int hz : hzs) {
                 if (hz > m.nez && hz != hzs[0]) continue;
                 if ((rc = snap_restore(s, snap))) break;
-                set_grid(s, nw, hz, pf, cap);
+                if ((rc = set_grid(s, nw, hz, zs, cap))) break;
                 // one untimed step, then the timed ones
                 rc = sks_run(s, 1, nullptr, nullptr, nullptr);
                 if (rc < 0) break;
                 rc = sks_run(s, steps, nullptr, nullptr, nullptr);
                 if (rc < 0) break;
                 const float ms = (float)(s->last_run_ms / rc);
-                if (ms < b.ms_per_step) b = {nw, s->HZ, pf, cap, s->nblocks, ms};
+                if (ms < b.ms_per_step) b = {nw, s->HZ, zs, cap, s->nblocks, ms};
                 rc = SKS_OK;
             }
     const int rc2 = snap_restore(s, snap);
     cudaStreamSynchronize(s->stream);
     for (void* p : snap.dev) cudaFree(p);
     s->timing = old_timing;
-    set_grid(s, b.warps_per_block, b.band_rows, b.prefetch, b.register_cap);
+    const int rc3 = set_grid(s, b.warps_per_block, b.band_rows, b.zseam, b.register_cap);
     if (rc < 0) return rc;
+    if (rc3) return rc3;
     if (rc2) return rc2;
     if (best) *best = b;
     return SKS_OK;

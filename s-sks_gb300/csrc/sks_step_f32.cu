@@ -5,17 +5,17 @@
 namespace sks {
 namespace {
 
-template <bool ANISO, int NW, bool PF, int CAP>
+template <bool ANISO, int NW, bool ZS, int CAP>
 void go(int blocks, cudaStream_t st, const Field<float>& F, const Geo<float>& G, const Coef<float>& k)
 {
-    k_step<float, ANISO, true, NW, PF, CAP><<<blocks, NW * 32, 0, st>>>(F, G, k);
+    k_step<float, ANISO, true, NW, ZS, CAP><<<blocks, NW * 32, 0, st>>>(F, G, k);
 }
 
 template <bool ANISO, int NW>
 void go_nw(const StepVariant& v, int blocks, cudaStream_t st, const Field<float>& F, const Geo<float>& G,
            const Coef<float>& k)
 {
-    if (v.prefetch) {
+    if (v.zseam) {
         if (v.cap == 2) go<ANISO, NW, true, 2>(blocks, st, F, G, k);
         else if (v.cap == 1) go<ANISO, NW, true, 1>(blocks, st, F, G, k);
         else go<ANISO, NW, true, 0>(blocks, st, F, G, k);

@@ -5,17 +5,17 @@
 namespace sks {
 namespace {
 
-template <bool ANISO, int NW, bool PF, int CAP>
+template <bool ANISO, int NW, bool ZS, int CAP>
 void go(int blocks, cudaStream_t st, const Field<double>& F, const Geo<double>& G, const Coef<double>& k)
 {
-    k_step<double, ANISO, false, NW, PF, CAP><<<blocks, NW * 32, 0, st>>>(F, G, k);
+    k_step<double, ANISO, false, NW, ZS, CAP><<<blocks, NW * 32, 0, st>>>(F, G, k);
 }
 
 template <bool ANISO, int NW>
 void go_nw(const StepVariant& v, int blocks, cudaStream_t st, const Field<double>& F, const Geo<double>& G,
            const Coef<double>& k)
 {
-    if (v.prefetch) {
+    if (v.zseam) {
         if (v.cap == 2) go<ANISO, NW, true, 2>(blocks, st, F, G, k);
         else if (v.cap == 1) go<ANISO, NW, true, 1>(blocks, st, F, G, k);
         else go<ANISO, NW, true, 0>(blocks, st, F, G, k);

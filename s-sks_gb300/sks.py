@@ -54,7 +54,7 @@ class Info(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("warps_per_block", C.c_int32), ("band_rows", C.c_int32), ("prefetch", C.c_int32),
+    _fields_ = [("warps_per_block", C.c_int32), ("band_rows", C.c_int32), ("zseam", C.c_int32),
                 ("register_cap", C.c_int32), ("blocks", C.c_int32), ("ms_per_step", C.c_float)]
 
     def asdict(self) -> dict:
@@ -223,8 +223,8 @@ class Solver:
         _check(lib().sks_get_tuning(self.h, C.byref(t)))
         return t.asdict()
 
-    def set_tuning(self, warps_per_block: int, band_rows: int, prefetch: int = 1, register_cap: int = 0):
-        t = Tuning(warps_per_block, band_rows, prefetch, register_cap, 0, 0.0)
+    def set_tuning(self, warps_per_block: int, band_rows: int, zseam: int = 1, register_cap: int = 0):
+        t = Tuning(warps_per_block, band_rows, zseam, register_cap, 0, 0.0)
         _check(lib().sks_set_tuning(self.h, C.byref(t)))
 
     def autotune(self, steps: int = 8) -> dict:

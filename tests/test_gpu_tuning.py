@@ -1,7 +1,7 @@
 """GPU: every tuning of the step kernel gives bit-identical seismograms, and the
 autotuner leaves the solve where it found it.
 
-The CTA grid (warps per CTA, band height, prefetch) changes which CTA computes
+The CTA grid (warps per CTA, band height, band-seam method, register cap) changes which CTA computes
 an element, never the arithmetic: a halo element is recomputed with the same
 inputs and code, and each point's force is summed in the same order.
 """
@@ -58,7 +58,7 @@ def test_all_tunings_bit_identical(case, prec):
     assert max(np.abs(x).max() for x in ref) > 0.1
     for t in TUNINGS:
         out, _, used = _run(d, prec, c.nst, tuning=t)
-        assert (used["warps_per_block"], used["band_rows"], used["prefetch"], used["register_cap"]) == t
+        assert (used["warps_per_block"], used["band_rows"], used["zseam"], used["register_cap"]) == t
         for i in range(3):
             assert np.array_equal(out[i], ref[i]), f"tuning {t} differs in component {i}"
 
@@ -69,7 +69,7 @@ def test_autotune_restores_state(case, prec):
     ref, _, _ = _run(d, prec, c.nst)
     out, best, used = _run(d, prec, c.nst, autotune=True)
     assert best["ms_per_step"] > 0
-    assert (used["warps_per_block"], used["band_rows"], used["prefetch"]) == \
-           (best["warps_per_block"], best["band_rows"], best["prefetch"])
+    assert (used["warps_per_block"], used["band_rows"], used["zseam"]) == \
+           (best["warps_per_block"], best["band_rows"], best["zseam"])
     for i in range(3):
         assert np.array_equal(out[i], ref[i])
