@@ -201,7 +201,8 @@ def run_e2e(d: str, precision: int, steps: int, warmup: int, gpu: int, tuning=No
     try:
         s = sks.Solver(["par=run.par", f"nst={steps}"], precision=precision, device=gpu)
         if tuning:
-            s.set_tuning(tuning["warps_per_block"], tuning["band_rows"], tuning["zseam"], tuning["register_cap"])
+            s.set_tuning(tuning["warps_per_block"], tuning["band_rows"], tuning["zseam"], tuning["register_cap"],
+                         tuning["waves"])
         info = s.info()
         npsv, nsh = info["nrec_psv"] * info["mtotal"], info["nrec_sh"] * info["shtotal"]
         psv, sh = _pinned(npsv), _pinned(nsh)
@@ -292,7 +293,7 @@ def main() -> None:
     ap.add_argument("--kernel-only", action="store_true",
                     help="only the device-resident step loop of one form (profiling)")
     ap.add_argument("--form", default="fp32c", choices=["fp32c", "fp64"])
-    ap.add_argument("--tuning", default="", help="W,B,Z,C: warps per CTA, band rows, band seams, register cap")
+    ap.add_argument("--tuning", default="", help="W,B,Z,C[,V]: warps per CTA, band rows, band seams, register cap, waves")
     a = ap.parse_args()
     a.warmup = max(3, a.warmup)
     dist, rank, world, local = _dist()

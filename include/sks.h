@@ -136,8 +136,9 @@ int sks_open_setup(sks_setup *su, int precision, int device, sks_solver **out);
 
 /* ---- tuning -------------------------------------------------------------
  * The step kernel runs one CTA per (column of 6*W-1 elements, band of B
- * element rows); each CTA recomputes one element column of halo.  W (warps per CTA), B, the band-seam method and a register cap
- * are tunable; the default comes from the mesh size and the SM count.
+ * element rows); each CTA recomputes one element column of halo.  W (warps
+ * per CTA), the band layout, the band-seam method and a register cap are
+ * tunable; the default comes from the mesh size and the SM count.
  * Every tuning gives bit-identical results. */
 typedef struct {
     int32_t warps_per_block;      /* 2 or 4                                 */
@@ -147,6 +148,9 @@ typedef struct {
                                      forces (the later band sums them)      */
     int32_t register_cap;         /* 0: compiler's choice; 1 / 2: registers capped for
                                      16 / 20 (FP32) or 8 / 12 (FP64) warps per SM */
+    int32_t waves;                /* 0: bands of band_rows rows; W > 0: exactly
+                                     W waves of CTAs (SMs x resident CTAs x W),
+                                     columns split into near-equal bands   */
     int32_t blocks;               /* CTAs per step (output)                 */
     float   ms_per_step;          /* measured by sks_autotune (output)      */
 } sks_tuning_t;

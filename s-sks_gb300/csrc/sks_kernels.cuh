@@ -56,6 +56,7 @@ template <typename T>
 struct Geo {
     int nex, nez, nx, nz;
     int ncx, ncz, HZ, nblocks;    // CTA grid: ncx columns x ncz row bands of HZ element rows
+    const int4* items;            // or per CTA (column, band, first row, end row): balanced bands
     int nbl;                      // GRT interface line: row nbl (ix >= nbl), column nbl (iz > nbl)
     int64_t np;                   // nx*nz
 };
@@ -295,7 +296,14 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
     __shared__ int second_arrival;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int cx = blockIdx.x % G.ncx, cz = blockIdx.x / G.ncx;
+    int cx, cz, ez0, ez1;
+    if (G.items) {
+        const int4 it = G.items[blockIdx.x];
+        cx = it.x; cz = it.y; ez0 = it.z; ez1 = it.w;
+    } else {
+        cx = blockIdx.x % G.ncx; cz = blockIdx.x / G.ncx;
+        ez0 = cz * G.HZ; ez1 = min(ez0 + G.HZ, G.nez);
+    }
     constexpr int S = TEX * NW - 1;                // owned elements per CTA
     const int e = lane / NP, al = lane - e * NP;   // lanes 30,31: e = 6
     const int q = TEX * w + e;                     // element within the CTA
@@ -306,7 +314,6 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
     // live lane (shuffles stay inside an element, the left neighbour is masked)
     const int ix = live ? ex * N + al : min(max(ex * N + al, 0), nx - 1);
     const bool own_x = live && q >= 1 && (al < N || ex == G.nex - 1);
-    const int ez0 = cz * G.HZ, ez1 = min(ez0 + G.HZ, G.nez);
     const int ezs = (!ZS && ez0 > 0) ? ez0 - 1 : ez0;
     const int base = e * NP;
     const bool add_left = al == 0 && (e > 0 || w > 0) && ex > 0;
@@ -532,4 +539,7 @@ cudaError_t launch_step_f32(const StepVariant& v, bool aniso, int blocks, cudaSt
                             const Field<float>& F, const Geo<float>& G, const Coef<float>& k);
 cudaError_t launch_step_f64(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
                             const Field<double>& F, const Geo<double>& G, const Coef<double>& k);
+// resident CTAs per SM of a variant (cudaOccupancyMaxActiveBlocksPerMultiprocessor)
+int step_occupancy_f32(const StepVariant& v, bool aniso);
+int step_occupancy_f64(const StepVariant& v, bool aniso);
 }  // namespace sks

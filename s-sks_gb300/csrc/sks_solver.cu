@@ -44,7 +44,9 @@ struct sks_solver {
     int64_t launches;
     cudaStream_t stream;
     // geometry: CTA grid of the step kernel (tunable)
-    int NW, ncx, ncz, HZ, nblocks, ZS, CAP;
+    int NW, ncx, ncz, HZ, nblocks, ZS, CAP, WAVES;
+    int4* items;               // balanced band table (grow-only)
+    size_t items_n;
     void* seam_lo;             // band-seam partial forces (grow-only)
     void* seam_hi;
     int* seam_cnt;
@@ -192,7 +194,7 @@ void free_device(sks_solver* s)
 {
     void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc,
                   s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seisbuf[0], s->seisbuf[1], s->G, s->rec_psv, s->rec_sh,
-                  s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt};
+                  s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt, s->items};
     for (void* p : ps)
         if (p) cudaFree(p);
     s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = nullptr;
@@ -200,6 +202,7 @@ void free_device(sks_solver* s)
     s->seis = nullptr; s->seisbuf[0] = s->seisbuf[1] = nullptr; s->G = nullptr;
     s->rec_psv = s->rec_sh = nullptr; s->tap_psv = s->tap_sh = nullptr; s->w_psv = s->w_sh = nullptr;
     s->seam_lo = s->seam_hi = nullptr; s->seam_cnt = nullptr; s->seam_bytes = 0; s->seam_cnt_n = 0;
+    s->items = nullptr; s->items_n = 0;
 }
 
 // per-kernel-class timing: an event pair around each launch when enabled
@@ -354,22 +357,61 @@ Geo<T> make_geo(const sks_solver* s)
     Geo<T> G;
     G.nex = s->m.nex; G.nez = s->m.nez; G.nx = s->m.nx; G.nz = s->m.nz;
     G.ncx = s->ncx; G.ncz = s->ncz; G.HZ = s->HZ; G.nblocks = s->nblocks;
+    G.items = s->WAVES > 0 ? s->items : nullptr;
     G.nbl = s->nbl;
     G.np = (int64_t)s->m.nx * s->m.nz;
     return G;
 }
 
-// CTA grid for a tuning: NW warps (6*NW-1 owned elements) by bands of HZ
-// rows; the band-seam buffers grow to fit and their counters restart at 0
-int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP)
+// CTA grid for a tuning: NW warps (6*NW-1 owned elements) by bands of rows.
+// waves == 0: bands of HZ rows.  waves > 0: exactly SMs x resident-CTAs x
+// waves CTAs, each column split into bands of near-equal height, so every
+// SM carries the same work (no partly filled last wave).  The band-seam
+// buffers grow to fit and their counters restart at 0.
+int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES)
 {
     s->NW = NW;
     s->ZS = ZS;
     s->CAP = CAP;
+    s->WAVES = WAVES;
     s->ncx = (s->m.nex + (TEX * NW - 1) - 1) / (TEX * NW - 1);
-    s->HZ = std::max(1, std::min(HZ, s->m.nez));
-    s->ncz = (s->m.nez + s->HZ - 1) / s->HZ;
-    s->nblocks = s->ncx * s->ncz;
+    const int nez = s->m.nez;
+    if (WAVES <= 0) {
+        s->HZ = std::max(1, std::min(HZ, nez));
+        s->ncz = (nez + s->HZ - 1) / s->HZ;
+        s->nblocks = s->ncx * s->ncz;
+    } else {
+        const StepVariant v{NW, ZS, CAP};
+        const int occ = s->precision == SKS_FP64 ? step_occupancy_f64(v, s->m.anisotropic != 0)
+                                                 : step_occupancy_f32(v, s->m.anisotropic != 0);
+        int64_t target = (int64_t)s->sms * occ * WAVES;
+        target = std::max<int64_t>(s->ncx, std::min<int64_t>(target, (int64_t)s->ncx * nez));
+        std::vector<int4> it;
+        it.reserve((size_t)target);
+        int maxb = 1;
+        for (int cx = 0; cx < s->ncx; cx++) {
+            const int nb = (int)(target / s->ncx + (cx < target % s->ncx ? 1 : 0));
+            maxb = std::max(maxb, nb);
+            for (int b = 0; b < nb; b++) {
+                const int e0 = (int)((int64_t)nez * b / nb), e1 = (int)((int64_t)nez * (b + 1) / nb);
+                it.push_back(make_int4(cx, b, e0, e1));
+            }
+        }
+        // lower bands first, columns side by side
+        std::stable_sort(it.begin(), it.end(), [](const int4& a, const int4& b) { return a.z < b.z; });
+        if (it.size() > s->items_n) {
+            if (s->items) { cudaFree(s->items); s->device_bytes -= (int64_t)(s->items_n * sizeof(int4)); }
+            s->items = nullptr;
+            s->items_n = 0;
+            CK(cudaMalloc(&s->items, it.size() * sizeof(int4)));
+            s->items_n = it.size();
+            s->device_bytes += (int64_t)(it.size() * sizeof(int4));
+        }
+        CK(cudaMemcpy(s->items, it.data(), it.size() * sizeof(int4), cudaMemcpyHostToDevice));
+        s->ncz = maxb;
+        s->HZ = (nez + maxb - 1) / maxb;
+        s->nblocks = (int)it.size();
+    }
     if (!ZS) return SKS_OK;
     const size_t el = s->precision == SKS_FP64 ? sizeof(double) : sizeof(float);
     const size_t need = (size_t)s->ncz * s->m.nx * 6 * el;
@@ -525,8 +567,8 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         // best with many short bands and registers capped for 16 warps/SM,
         // FP64 (bound by the FP64 pipe) with fewer, taller bands
         const int ncx4 = (m.nex + (TEX * 4 - 1) - 1) / (TEX * 4 - 1);
-        const int rcg = precision == SKS_FP32C ? set_grid(s, 4, pick_band(m, ncx4, sms, 10), 1, 1)
-                                               : set_grid(s, 4, pick_band(m, ncx4, sms, 5), 1, 0);
+        const int rcg = precision == SKS_FP32C ? set_grid(s, 4, pick_band(m, ncx4, sms, 10), 0, 1, 1)
+                                               : set_grid(s, 4, pick_band(m, ncx4, sms, 5), 1, 0, 1);
         if (rcg) { free_device(s); cudaStreamDestroy(s->stream); sks_model_free(&s->m); delete s; return rcg; }
     }
     s->chunk = 64;
@@ -809,8 +851,9 @@ extern "C" int sks_set_tuning(sks_solver* s, const sks_tuning_t* t)
         return set_err(SKS_ERR_ARG, "warps_per_block=%d: 2 or 4", t->warps_per_block);
     if (t->register_cap < 0 || t->register_cap > 2)
         return set_err(SKS_ERR_ARG, "register_cap=%d: 0, 1 or 2", t->register_cap);
-    if (t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
-    return set_grid(s, t->warps_per_block, t->band_rows, t->zseam ? 1 : 0, t->register_cap);
+    if (t->waves == 0 && t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
+    if (t->waves < 0 || t->waves > 64) return set_err(SKS_ERR_ARG, "waves=%d: 0..64", t->waves);
+    return set_grid(s, t->warps_per_block, t->band_rows, t->zseam ? 1 : 0, t->register_cap, t->waves);
 }
 
 extern "C" int sks_get_tuning(const sks_solver* s, sks_tuning_t* t)
@@ -819,6 +862,7 @@ extern "C" int sks_get_tuning(const sks_solver* s, sks_tuning_t* t)
     t->warps_per_block = s->NW;
     t->band_rows = s->HZ;
     t->zseam = s->ZS;
+    t->waves = s->WAVES;
     t->register_cap = s->CAP;
     t->blocks = s->nblocks;
     t->ms_per_step = 0.f;
@@ -881,29 +925,32 @@ extern "C" int sks_autotune(sks_solver* s, int32_t steps, sks_tuning_t* best)
     const int old_timing = s->timing;
     s->timing = 0;
     const int nws[] = {2, 4};
-    const int hzs[] = {4, 6, 8, 12, 16, 24, 32};
-    sks_tuning_t b = {s->NW, s->HZ, s->ZS, s->CAP, s->nblocks, 1e30f};
+    const int hzs[] = {4, 6, 8, 12};
+    sks_tuning_t b = {s->NW, s->HZ, s->ZS, s->CAP, s->WAVES, s->nblocks, 1e30f};
+    // fixed band heights, then balanced partitions of 1..3 waves
+    const int nhz = (int)(sizeof hzs / sizeof hzs[0]);
     for (int nw : nws)
         for (int zs = 0; zs < 2; zs++)
           for (int cap = 0; cap < 3; cap++)
-            for (int hz : hzs) {
-                if (hz > m.nez && hz != hzs[0]) continue;
+            for (int cand = 0; cand < nhz + 3; cand++) {
+                const int hz = cand < nhz ? hzs[cand] : 0, wv = cand < nhz ? 0 : cand - nhz + 1;
+                if (wv == 0 && hz > m.nez && hz != hzs[0]) continue;
                 if ((rc = snap_restore(s, snap))) break;
-                if ((rc = set_grid(s, nw, hz, zs, cap))) break;
+                if ((rc = set_grid(s, nw, hz, zs, cap, wv))) break;
                 // one untimed step, then the timed ones
                 rc = sks_run(s, 1, nullptr, nullptr, nullptr);
                 if (rc < 0) break;
                 rc = sks_run(s, steps, nullptr, nullptr, nullptr);
                 if (rc < 0) break;
                 const float ms = (float)(s->last_run_ms / rc);
-                if (ms < b.ms_per_step) b = {nw, s->HZ, zs, cap, s->nblocks, ms};
+                if (ms < b.ms_per_step) b = {nw, s->HZ, zs, cap, wv, s->nblocks, ms};
                 rc = SKS_OK;
             }
     const int rc2 = snap_restore(s, snap);
     cudaStreamSynchronize(s->stream);
     for (void* p : snap.dev) cudaFree(p);
     s->timing = old_timing;
-    const int rc3 = set_grid(s, b.warps_per_block, b.band_rows, b.zseam, b.register_cap);
+    const int rc3 = set_grid(s, b.warps_per_block, b.band_rows, b.zseam, b.register_cap, b.waves);
     if (rc < 0) return rc;
     if (rc3) return rc3;
     if (rc2) return rc2;

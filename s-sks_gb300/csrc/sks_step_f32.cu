@@ -34,7 +34,29 @@ void go_aniso(const StepVariant& v, int blocks, cudaStream_t st, const Field<flo
     else go_nw<ANISO, 4>(v, blocks, st, F, G, k);
 }
 
+template <bool ANISO, int NW, bool ZS, int CAP>
+int occ()
+{
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<float, ANISO, true, NW, ZS, CAP>, NW * 32, 0) != cudaSuccess)
+        return 1;
+    return n > 0 ? n : 1;
+}
+
+template <bool ANISO, int NW>
+int occ_nw(const StepVariant& v)
+{
+    if (v.zseam) return v.cap == 2 ? occ<ANISO, NW, true, 2>() : v.cap == 1 ? occ<ANISO, NW, true, 1>() : occ<ANISO, NW, true, 0>();
+    return v.cap == 2 ? occ<ANISO, NW, false, 2>() : v.cap == 1 ? occ<ANISO, NW, false, 1>() : occ<ANISO, NW, false, 0>();
+}
+
 }  // namespace
+
+int step_occupancy_f32(const StepVariant& v, bool aniso)
+{
+    if (aniso) return v.nw == 2 ? occ_nw<true, 2>(v) : occ_nw<true, 4>(v);
+    return v.nw == 2 ? occ_nw<false, 2>(v) : occ_nw<false, 4>(v);
+}
 
 cudaError_t launch_step_f32(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
                             const Field<float>& F, const Geo<float>& G, const Coef<float>& k)

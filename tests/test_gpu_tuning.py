@@ -48,17 +48,21 @@ def _run(d, prec, nst, tuning=None, autotune=False):
         return out, got, s.tuning()
 
 
-TUNINGS = [(nw, hz, pf, cap) for nw in (2, 4) for hz in (1, 3, 23) for pf in (0, 1) for cap in (0, 1, 2)]
+TUNINGS = [(nw, hz, zs, cap, wv) for nw in (2, 4) for hz in (1, 3, 23) for zs in (0, 1) for cap in (0, 1, 2)
+           for wv in (0,)] + [(nw, 4, zs, 1, wv) for nw in (2, 4) for zs in (0, 1) for wv in (1, 2, 5)]
 
 
 @pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])
 def test_all_tunings_bit_identical(case, prec):
     d, c = case
-    ref, _, _ = _run(d, prec, c.nst, tuning=(4, 8, 1, 0))
+    ref, _, _ = _run(d, prec, c.nst, tuning=(4, 8, 1, 0, 0))
     assert max(np.abs(x).max() for x in ref) > 0.1
     for t in TUNINGS:
         out, _, used = _run(d, prec, c.nst, tuning=t)
-        assert (used["warps_per_block"], used["band_rows"], used["zseam"], used["register_cap"]) == t
+        got = (used["warps_per_block"], used["zseam"], used["register_cap"], used["waves"])
+        assert got == (t[0], t[2], t[3], t[4])
+        if t[4] == 0:
+            assert used["band_rows"] == t[1]
         for i in range(3):
             assert np.array_equal(out[i], ref[i]), f"tuning {t} differs in component {i}"
 
