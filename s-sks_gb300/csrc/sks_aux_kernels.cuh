@@ -57,6 +57,38 @@ __global__ void __launch_bounds__(256) k_interp(double* __restrict__ Gout, int L
     }
 }
 
+// Increments of the interface line for the steps of a chunk, in the form's
+// type: row r of Dl is step it0+r's injection g(it0+r) - g(it0+r-1) taken
+// from G rows r+1 and r (the same FP64 expressions as GRT_Interface4,
+// sem2d_psvsh.c:2076-2111, converted once).  Line points: row nbl (ix >=
+// nbl), then column nbl (iz > nbl).
+template <typename T>
+__global__ void __launch_bounds__(256) k_line_delta(T* __restrict__ Dl, const double* __restrict__ G, int L,
+                                                    int nsteps, int nx, int nz, int nbl, int mtotal)
+{
+    const int nrow = nx - nbl, ncol = nz - nbl - 1, nline = nrow + ncol;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)nsteps * nline) return;
+    const int r = (int)(i / nline), li = (int)(i - (int64_t)r * nline);
+    const double* g1 = G + (int64_t)(r + 1) * L;
+    const double* g0 = G + (int64_t)r * L;
+    const double *v1 = g1 + mtotal, *v0 = g0 + mtotal;
+    double d3[3];
+    if (li < nrow) {
+        const int ix = nbl + li;
+        d3[0] = -g0[ix] + g1[ix];
+        d3[1] = -v0[ix] + v1[ix];
+        d3[2] = g0[nx + ix] - g1[nx + ix];
+    } else {
+        const int iz = nbl + 1 + (li - nrow);
+        d3[0] = -g0[2 * nx + iz] + g1[2 * nx + iz];
+        d3[1] = -v0[nx + iz] + v1[nx + iz];
+        d3[2] = g0[2 * nx + nz + iz] - g1[2 * nx + nz + iz];
+    }
+    T* o = Dl + ((int64_t)r * nline + li) * 3;
+    o[0] = (T)d3[0]; o[1] = (T)d3[1]; o[2] = (T)d3[2];
+}
+
 // GRT_Interface4 (sem2d_psvsh.c:2076-2111): u^n += g(it) - g(it-1) on row nbl
 // (ix >= nbl) and column nbl (iz > nbl); the vertical component changes sign.
 template <typename T, bool LF>
@@ -86,16 +118,19 @@ __global__ void __launch_bounds__(256) k_inject(T* __restrict__ u, T* __restrict
     const double dd[3] = {du, dvv, dw};
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        if (!LF) {
+        if constexpr (!LF) {
             u[c * np + g] += (T)dd[c];
         } else {
+            float2* dc = reinterpret_cast<float2*>(dv);
             const T add = (T)dd[c];
-            const T uu = u[c * np + g], cm = cc[c * np + g];
-            const T y = add - cm;
+            float2 p = dc[c * np + g];
+            const T uu = u[c * np + g];
+            const T y = add - p.y;
             const T t = uu + y;
-            cc[c * np + g] = (t - uu) - y;
+            p.y = (t - uu) - y;
+            p.x += add;
             u[c * np + g] = t;
-            dv[c * np + g] += add;
+            dc[c * np + g] = p;
         }
     }
 }
@@ -124,7 +159,7 @@ __global__ void __launch_bounds__(256) k_init_line(T* __restrict__ u, T* __restr
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         u[c * np + g] = (T)v3[c];
-        if (LF) dv[c * np + g] = (T)v3[c];
+        if constexpr (LF) reinterpret_cast<float2*>(dv)[c * np + g] = make_float2((T)v3[c], 0.f);
     }
 }
 

@@ -65,15 +65,16 @@ template <typename T>
 struct Field {
     const T* __restrict__ uc;     // u^n, [3][np]
     T* __restrict__ un;           // FP64: u^{n-1} in, u^{n+1} out; FP32: u^{n+1} out
-    T* __restrict__ dv;           // FP32 form: d = u^n - u^{n-1}, in place
-    T* __restrict__ cc;           // FP32 form: Kahan compensation of u, in place
+    T* __restrict__ dv;           // FP32 form: per component a float2 (d, c): the increment
+                                  // d = u^n - u^{n-1} and the Kahan compensation of u, [3][np]
+    T* __restrict__ cc;           // unused
     const uint16_t* __restrict__ mid;   // material index per point
     const T* __restrict__ mat;          // [nmat][16]: 15 stiffness entries, 1/rho
     const T* __restrict__ stc;          // Stacey coefficients [nbnd][3][3]: dt^2/(M+A), 2M/(M+A), (M-A)/(M+A)
-    // next step's boundary injection, fused into this step's write (FP64 traces)
-    const double* __restrict__ gnow;    // g(it)
-    const double* __restrict__ gnext;   // g(it+1)
-    int mtotal;
+    // next step's boundary injection, fused into this step's write: the
+    // increments g(it+1) - g(it) of the interface line, [line point][3]
+    // (row points ix >= nbl first, then column points iz > nbl)
+    const T* __restrict__ dline;
     int inject_next;                    // it+1 < number of injecting steps
     // receivers, fused: a bitmap over points, then the sorted offsets
     const uint32_t* __restrict__ recbits;
@@ -165,8 +166,13 @@ __device__ __forceinline__ void load_aux(const Field<T>& F, int64_t np, int64_t 
 {
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        if (!LF) x.a[c] = F.un[c * np + g];
-        else { x.a[c] = F.dv[c * np + g]; x.b[c] = F.cc[c * np + g]; }
+        if constexpr (!LF) {
+            x.a[c] = F.un[c * np + g];
+        } else {
+            const float2 v = reinterpret_cast<const float2*>(F.dv)[c * np + g];
+            x.a[c] = v.x;
+            x.b[c] = v.y;
+        }
     }
 }
 
@@ -230,26 +236,14 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
     }
     // GRT_Interface4 of the next step (sem2d_psvsh.c:2076-2111)
     if (F.inject_next && ((iz == G.nbl && pf.row_ok) || (pf.on_col && iz > G.nbl))) {
-        const double* g1 = F.gnext;
-        const double* g0 = F.gnow;
-        const double* v1 = g1 + F.mtotal;
-        const double* v0 = g0 + F.mtotal;
-        double d3[3];
-        if (iz == G.nbl) {
-            d3[0] = -g0[ix] + g1[ix];
-            d3[1] = -v0[ix] + v1[ix];
-            d3[2] = g0[G.nx + ix] - g1[G.nx + ix];
-        } else {
-            d3[0] = -g0[2 * G.nx + iz] + g1[2 * G.nx + iz];
-            d3[1] = -v0[G.nx + iz] + v1[G.nx + iz];
-            d3[2] = g0[2 * G.nx + G.nz + iz] - g1[2 * G.nx + G.nz + iz];
-        }
+        const int li = iz == G.nbl ? ix - G.nbl : (G.nx - G.nbl) + (iz - G.nbl - 1);
+        const T* d3 = F.dline + 3 * li;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             if (!LF) {
-                un[c] += (T)d3[c];
+                un[c] += d3[c];
             } else {
-                const T add = (T)d3[c];
+                const T add = d3[c];
                 const T y = add - cn[c];
                 const T t = un[c] + y;
                 cn[c] = (t - un[c]) - y;
@@ -262,7 +256,7 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         F.un[c * np + g] = un[c];
-        if (LF) { F.dv[c * np + g] = dn[c]; F.cc[c * np + g] = cn[c]; }
+        if constexpr (LF) reinterpret_cast<float2*>(F.dv)[c * np + g] = make_float2(dn[c], cn[c]);
     }
 }
 

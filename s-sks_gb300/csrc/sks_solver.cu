@@ -71,7 +71,8 @@ struct sks_solver {
     cudaStream_t copy_stream;
     cudaEvent_t chunk_done[2], copy_done[2];
     bool slot_busy[2];
-    double* G;                 // [(chunk+1)][mtotal+shtotal]
+    double* G;                 // [(chunk+2)][mtotal+shtotal]
+    void* Dl;                  // [chunk+1][nline][3] line increments in the form's type
     float* rec_psv;            // boundary records
     float* rec_sh;
     int32_t* tap_psv;
@@ -193,13 +194,13 @@ int dmalloc(sks_solver* s, T** p, size_t n)
 void free_device(sks_solver* s)
 {
     void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc,
-                  s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seisbuf[0], s->seisbuf[1], s->G, s->rec_psv, s->rec_sh,
+                  s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seisbuf[0], s->seisbuf[1], s->G, s->Dl, s->rec_psv, s->rec_sh,
                   s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt, s->items};
     for (void* p : ps)
         if (p) cudaFree(p);
     s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = nullptr;
     s->mid = nullptr; s->rec_off = nullptr; s->recbits = nullptr; s->rec_sorted = nullptr; s->rec_idx = nullptr;
-    s->seis = nullptr; s->seisbuf[0] = s->seisbuf[1] = nullptr; s->G = nullptr;
+    s->seis = nullptr; s->seisbuf[0] = s->seisbuf[1] = nullptr; s->G = nullptr; s->Dl = nullptr;
     s->rec_psv = s->rec_sh = nullptr; s->tap_psv = s->tap_sh = nullptr; s->w_psv = s->w_sh = nullptr;
     s->seam_lo = s->seam_hi = nullptr; s->seam_cnt = nullptr; s->seam_bytes = 0; s->seam_cnt_n = 0;
     s->items = nullptr; s->items_n = 0;
@@ -301,11 +302,10 @@ int upload_tables(sks_solver* s)
     if ((rc = dmalloc(s, &u1, 3 * np))) return rc;
     s->U[1] = u1;
     if (s->precision == SKS_FP32C) {
-        T *dv, *cc;
-        if ((rc = dmalloc(s, &dv, 3 * np))) return rc;
+        T* dv;                      // (d, Kahan c) pairs, [3][np] float2
+        if ((rc = dmalloc(s, &dv, 6 * np))) return rc;
         s->Dv = dv;
-        if ((rc = dmalloc(s, &cc, 3 * np))) return rc;
-        s->Cc = cc;
+        s->Cc = nullptr;
     }
     return SKS_OK;
 }
@@ -337,7 +337,6 @@ Field<T> make_field(sks_solver* s)
     F.mid = s->mid;
     F.mat = (const T*)s->mat;
     F.stc = (const T*)s->stc;
-    F.mtotal = s->m.mtotal;
     F.recbits = s->recbits;
     F.rec_off = s->rec_sorted;
     F.rec_idx = s->rec_idx;
@@ -440,12 +439,11 @@ int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES)
 // one time step it >= 1: a single fused kernel (force, assembly, update,
 // receivers, and the boundary increment of step it+1)
 template <typename T, bool LF>
-int step_impl(sks_solver* s, int it, const double* Gcur, const double* Gnext, float* seis_row)
+int step_impl(sks_solver* s, int it, const T* dline, float* seis_row)
 {
     const sks_model& m = s->m;
     Field<T> F = make_field<T>(s);
-    F.gnow = Gcur;
-    F.gnext = Gnext;
+    F.dline = dline;
     F.inject_next = (it + 1 < m.nt_sem) ? 1 : 0;
     F.seis_row = seis_row;
     Geo<T> G = make_geo<T>(s);
@@ -475,8 +473,7 @@ int step0_impl(sks_solver* s, const double* G0, const double* G1, float* seis_ro
     CK(cudaMemsetAsync(s->U[0], 0, 3 * np * sizeof(T), st));
     CK(cudaMemsetAsync(s->U[1], 0, 3 * np * sizeof(T), st));
     if (LF) {
-        CK(cudaMemsetAsync(s->Dv, 0, 3 * np * sizeof(T), st));
-        CK(cudaMemsetAsync(s->Cc, 0, 3 * np * sizeof(T), st));
+        CK(cudaMemsetAsync(s->Dv, 0, 6 * np * sizeof(T), st));
     }
     if (m.nt_sem > 0) {
         const int n = (m.nx - s->nbl - 1) + (m.nz - s->nbl);
@@ -513,18 +510,34 @@ int run_chunk(sks_solver* s, int it0, int n)
                                          s->tap_psv, s->w_psv, s->tap_sh, s->w_sh);
         }
         s->g_last = n;     // row of step it0+n-1: the previous step of the next chunk
+        // increments g(it+1) - g(it) for the steps it0..it0+n-1 that inject next
+        const int nd = std::max(0, std::min(it0 + n + 1, m.nt_sem) - it0 - 1);
+        if (nd > 0) {
+            const int nline = (m.nx - s->nbl) + (m.nz - s->nbl - 1);
+            const int64_t tot = (int64_t)nd * nline;
+            KTimer t(s, SKS_KC_INTERP);
+            if (s->precision == SKS_FP64)
+                k_line_delta<double><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>((double*)s->Dl, s->G + L, L, nd, m.nx, m.nz,
+                                                                                  s->nbl, m.mtotal);
+            else
+                k_line_delta<float><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>((float*)s->Dl, s->G + L, L, nd, m.nx, m.nz,
+                                                                                 s->nbl, m.mtotal);
+        }
     }
     if (m.ntrace > 0) CK(cudaMemsetAsync(s->seis, 0, sizeof(float) * (size_t)n * 3 * m.ntrace, st));
     for (int i = 0; i < n; i++) {
         const int it = it0 + i;
         const double* Gcur = s->G + (size_t)(i + 1) * L;
         const double* Gnext = s->G + (size_t)(i + 2) * L;
+        const size_t nline = (size_t)(m.nx - s->nbl) + (m.nz - s->nbl - 1);
         float* row = s->seis + (size_t)i * 3 * m.ntrace;
         int rc;
         if (s->precision == SKS_FP64) {
-            rc = it == 0 ? step0_impl<double, false>(s, Gcur, Gnext, row) : step_impl<double, false>(s, it, Gcur, Gnext, row);
+            rc = it == 0 ? step0_impl<double, false>(s, Gcur, Gnext, row)
+                         : step_impl<double, false>(s, it, (const double*)s->Dl + (size_t)i * nline * 3, row);
         } else {
-            rc = it == 0 ? step0_impl<float, true>(s, Gcur, Gnext, row) : step_impl<float, true>(s, it, Gcur, Gnext, row);
+            rc = it == 0 ? step0_impl<float, true>(s, Gcur, Gnext, row)
+                         : step_impl<float, true>(s, it, (const float*)s->Dl + (size_t)i * nline * 3, row);
         }
         if (rc) return rc;
     }
@@ -630,6 +643,13 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "copy stream/events: %s", cudaGetErrorString(ce));
     }
     if (!rc) rc = dmalloc(s, &s->G, (size_t)(s->chunk + 2) * (m.mtotal + m.shtotal));
+    if (!rc) {
+        const size_t nline = (size_t)(m.nx - s->nbl) + (m.nz - s->nbl - 1);
+        double* dl = nullptr;
+        const size_t el = precision == SKS_FP64 ? 1 : 2;   // doubles, or floats packed two per double
+        rc = dmalloc(s, &dl, ((size_t)s->chunk + 1) * nline * 3 / el + 1);
+        s->Dl = dl;
+    }
     if (!rc && m.nt_sem > 0) {
         rc = dmalloc(s, &s->tap_psv, 4 * (size_t)m.nt_sem);
         if (!rc) rc = dmalloc(s, &s->tap_sh, 4 * (size_t)m.nt_sem);
@@ -883,7 +903,7 @@ int snap_take(sks_solver* s, Snapshot& S)
     const size_t np = (size_t)s->m.nx * s->m.nz;
     const size_t el = s->precision == SKS_FP64 ? sizeof(double) : sizeof(float);
     void* bufs[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->G};
-    const size_t sz[] = {3 * np * el, 3 * np * el, 3 * np * el, 3 * np * el,
+    const size_t sz[] = {3 * np * el, 3 * np * el, 6 * np * el, 3 * np * el,
                          sizeof(double) * (size_t)(s->chunk + 2) * (s->m.mtotal + s->m.shtotal)};
     for (int i = 0; i < 5; i++) {
         if (!bufs[i]) continue;
