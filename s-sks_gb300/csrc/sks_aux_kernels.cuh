@@ -119,17 +119,17 @@ __global__ void __launch_bounds__(256) k_inject(T* __restrict__ u, T* __restrict
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         if constexpr (!LF) {
-            u[c * np + g] += (T)dd[c];
+            u[ucomp(c, g, np)] += (T)dd[c];
         } else {
             float2* dc = reinterpret_cast<float2*>(dv);
             const T add = (T)dd[c];
             float2 p = dc[c * np + g];
-            const T uu = u[c * np + g];
+            const T uu = u[ucomp(c, g, np)];
             const T y = add - p.y;
             const T t = uu + y;
             p.y = (t - uu) - y;
             p.x += add;
-            u[c * np + g] = t;
+            u[ucomp(c, g, np)] = t;
             dc[c * np + g] = p;
         }
     }
@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(256) k_init_line(T* __restrict__ u, T* __restr
     }
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        u[c * np + g] = (T)v3[c];
+        u[ucomp(c, g, np)] = (T)v3[c];
         if constexpr (LF) reinterpret_cast<float2*>(dv)[c * np + g] = make_float2((T)v3[c], 0.f);
     }
 }
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(128) k_record(const T* __restrict__ u, int64_t
     if (r >= ntrace) return;
     const int64_t g = off[r];
     float vx = 0.f, vy = 0.f, vz = 0.f;
-    if (g < np) { vx = (float)u[g]; vy = (float)u[np + g]; vz = (float)(-u[2 * np + g]); }
+    if (g < np) { vx = (float)u[2 * g]; vy = (float)u[2 * np + g]; vz = (float)(-u[2 * g + 1]); }
     out[r] = vx;
     out[ntrace + r] = vy;
     out[2 * ntrace + r] = vz;

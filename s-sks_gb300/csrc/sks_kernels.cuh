@@ -63,7 +63,7 @@ struct Geo {
 
 template <typename T>
 struct Field {
-    const T* __restrict__ uc;     // u^n, [3][np]
+    const T* __restrict__ uc;     // u^n: (u_x, u_z) pairs [np], then u_y [np]
     T* __restrict__ un;           // FP64: u^{n-1} in, u^{n+1} out; FP32: u^{n+1} out
     T* __restrict__ dv;           // FP32 form: per component a float2 (d, c): the increment
                                   // d = u^n - u^{n-1} and the Kahan compensation of u, [3][np]
@@ -91,6 +91,38 @@ struct Field {
     T* __restrict__ seam_hi;
     int* __restrict__ seam_cnt;
 };
+
+// Displacement layout: the P-SV pair (u_x, u_z) of every point as one 2-vector
+// ([np] pairs), then u_y ([np]); 3*np values in all.
+template <typename T> struct Pair;
+template <> struct Pair<float> { using type = float2; };
+template <> struct Pair<double> { using type = double2; };
+
+__device__ __forceinline__ int64_t ucomp(int c, int64_t g, int64_t np)
+{
+    return c == 1 ? 2 * np + g : 2 * g + (c == 2 ? 1 : 0);
+}
+
+template <typename T>
+__device__ __forceinline__ void load_u(const T* __restrict__ U, int np, int g, T out[3])
+{
+    using V = typename Pair<T>::type;
+    const V p = reinterpret_cast<const V*>(U)[g];
+    out[0] = p.x;
+    out[2] = p.y;
+    out[1] = U[2 * np + g];
+}
+
+template <typename T>
+__device__ __forceinline__ void store_u(T* __restrict__ U, int np, int g, const T v[3])
+{
+    using V = typename Pair<T>::type;
+    V p;
+    p.x = v[0];
+    p.y = v[2];
+    reinterpret_cast<V*>(U)[g] = p;
+    U[2 * np + g] = v[1];
+}
 
 __device__ __forceinline__ int64_t stacey_index(int ix, int iz, int nx, int nz)
 {
@@ -165,10 +197,11 @@ template <typename T, bool LF>
 __device__ __forceinline__ void load_aux(const Field<T>& F, int64_t np, int64_t g, Aux<T, LF>& x)
 {
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-        if constexpr (!LF) {
-            x.a[c] = F.un[c * np + g];
-        } else {
+    if constexpr (!LF) {
+        load_u<T>(F.un, (int)np, (int)g, x.a);
+    } else {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
             const float2 v = reinterpret_cast<const float2*>(F.dv)[c * np + g];
             x.a[c] = v.x;
             x.b[c] = v.y;
@@ -253,10 +286,10 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
         }
     }
     const int np = (int)G.np;
+    store_u<T>(F.un, np, g, un);
+    if constexpr (LF) {
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-        F.un[c * np + g] = un[c];
-        if constexpr (LF) reinterpret_cast<float2*>(F.dv)[c * np + g] = make_float2(dn[c], cn[c]);
+        for (int c = 0; c < 3; c++) reinterpret_cast<float2*>(F.dv)[c * np + g] = make_float2(dn[c], cn[c]);
     }
 }
 
@@ -312,9 +345,6 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
     const int base = e * NP;
     const bool add_left = al == 0 && (e > 0 || w > 0) && ex > 0;
     const int np = (int)G.np;                      // 3*np < 2^31 (checked on the host)
-    const T* __restrict__ U0 = F.uc;
-    const T* __restrict__ U1 = F.uc + np;
-    const T* __restrict__ U2 = F.uc + 2 * np;
     PointFlags pfl;
     pfl.edge_x = ix == 0 || ix == nx - 1;
     pfl.top_ok = ix >= 1 && ix <= 3 * N;
@@ -341,7 +371,7 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 #pragma unroll
         for (int b = 0; b < NP; b++) {
             const int g = o + b * nx;
-            u[b][0] = U0[g]; u[b][1] = U1[g]; u[b][2] = U2[g];
+            load_u<T>(F.uc, np, g, u[b]);
             m[b] = F.mid[g];
         }
     }
@@ -356,7 +386,7 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 #pragma unroll
             for (int b = 1; b < NP; b++) {
                 const int g = o + b * nx;
-                u[b][0] = U0[g]; u[b][1] = U1[g]; u[b][2] = U2[g];
+                load_u<T>(F.uc, np, g, u[b]);
                 m[b] = F.mid[g];
             }
         }
