@@ -61,8 +61,8 @@ typedef struct {
     double  eh, h, sdt;           /* element size, GLL spacing, time step */
     int64_t device_bytes;         /* device memory held by the handle     */
     int64_t seam_points;          /* points shared by warp tiles          */
-    int32_t tile_rows;            /* element rows per warp tile           */
-    int32_t reserved;
+    int32_t tile_rows;            /* element rows per CTA band            */
+    int32_t neh;                  /* interface line offset in elements    */
 } sks_info_t;
 
 /* Replaces main() of sem2d_psvsh up to its time loop (sem2d_psvsh.c:82-416):
@@ -91,6 +91,16 @@ int sks_set_boundary(sks_solver *s, const float *psv, int32_t nrec_psv,
  * (sem2d_psvsh.c:2116-2160).  Buffers hold nsteps*ntrace floats; any may be
  * NULL.  Returns the number of steps taken (>= 0) or a negative status. */
 int sks_run(sks_solver *s, int32_t nsteps, float *seis_u, float *seis_v, float *seis_w);
+
+/* The boundary increments the time loop injects, as GRT_Interface4 adds them
+ * (sem2d_psvsh.c:2076-2111) from the interpolated traces of interpl()
+ * (interpl.c:16-54): for each step it in [it0, it0+nsteps), the FP64
+ * difference g(it+1) - g(it) at every interface-line point -- row nbl for
+ * ix >= nbl, then column nbl for iz > nbl, nline = (nx-nbl)+(nz-nbl-1)
+ * points -- as (u_x, u_y, u_z) with z up.  out receives nsteps*nline*3
+ * doubles (host memory); steps that inject nothing get zeros.  Scratch for
+ * the interpolated traces is allocated on the device for the call. */
+int sks_line_increments(sks_solver *s, int32_t it0, int32_t nsteps, double *out);
 
 /* Back to step 0 with a zero wavefield (boundary records are kept). */
 int sks_reset(sks_solver *s);

@@ -9,7 +9,7 @@ namespace sks {
 // Boundary-trace interpolation for a chunk of steps (interpl.c:16-54): row r of
 // Gout (r = 1..S) is step s0+r-1; four taps of FP32 records with FP64 weights,
 // then the |g| >= 10 guard of sem2d_psvsh.c:432-444 (sequential, ends read 0).
-__global__ void __launch_bounds__(256) k_interp(double* __restrict__ Gout, int L, int s0, int nsteps,
+static __global__ void __launch_bounds__(256) k_interp(double* __restrict__ Gout, int L, int s0, int nsteps,
                                                 const float* __restrict__ rpsv, int mtotal,
                                                 const float* __restrict__ rsh, int shtotal,
                                                 const int32_t* __restrict__ tap_psv, const double* __restrict__ w_psv,

@@ -109,6 +109,7 @@ static void fill_info(const sks_model& m, sks_info_t* info)
     info->nrec_psv = m.nrec_psv; info->nrec_sh = m.nrec_sh; info->nmat = m.nmat;
     info->anisotropic = m.anisotropic;
     info->eh = m.eh; info->h = m.h; info->sdt = m.sdt;
+    info->neh = m.neh;
 }
 
 extern "C" int sks_setup_open(int argc, const char* const* argv, sks_setup** out)
@@ -975,5 +976,39 @@ extern "C" int sks_autotune(sks_solver* s, int32_t steps, sks_tuning_t* best)
     if (rc3) return rc3;
     if (rc2) return rc2;
     if (best) *best = b;
+    return SKS_OK;
+}
+
+extern "C" int sks_line_increments(sks_solver* s, int32_t it0, int32_t nsteps, double* out)
+{
+    if (!s || !out) return set_err(SKS_ERR_ARG, "NULL argument");
+    const sks_model& m = s->m;
+    const int nline = (m.nx - s->nbl) + (m.nz - s->nbl - 1);
+    if (it0 < 0 || nsteps < 0) return set_err(SKS_ERR_ARG, "it0=%d nsteps=%d", it0, nsteps);
+    memset(out, 0, sizeof(double) * (size_t)nsteps * nline * 3);
+    // step it injects into its output g(it+1) - g(it) while it+1 < nt_inject
+    const int nd = std::max(0, std::min(it0 + nsteps, m.nt_sem - 1) - it0);
+    if (nd == 0) return SKS_OK;
+    if (!s->boundary_ready) return set_err(SKS_ERR_STATE, "boundary records not set");
+    cudaSetDevice(s->device);
+    const int L = m.mtotal + m.shtotal;
+    double *G = nullptr, *D = nullptr;
+    cudaError_t e = cudaMalloc((void**)&G, sizeof(double) * (size_t)(nd + 2) * L);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&D, sizeof(double) * (size_t)nd * nline * 3);
+    if (e != cudaSuccess) {
+        cudaFree(G);
+        return set_err(SKS_ERR_NOMEM, "cudaMalloc for the boundary increments: %s", cudaGetErrorString(e));
+    }
+    // rows 1..nd+1 of G: steps it0..it0+nd (k_interp writes row r+1 for step it0+r)
+    k_interp<<<nd + 1, 256, 0, s->stream>>>(G, L, it0, nd + 1, s->rec_psv, m.mtotal, s->rec_sh, m.shtotal,
+                                             s->tap_psv, s->w_psv, s->tap_sh, s->w_sh);
+    const int64_t tot = (int64_t)nd * nline;
+    k_line_delta<double><<<(unsigned)((tot + 255) / 256), 256, 0, s->stream>>>(D, G + L, L, nd, m.nx, m.nz, s->nbl, m.mtotal);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, D, sizeof(double) * (size_t)tot * 3, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(G);
+    cudaFree(D);
+    if (e != cudaSuccess) return set_err(SKS_ERR_CUDA, "boundary increments: %s", cudaGetErrorString(e));
     return SKS_OK;
 }

@@ -30,7 +30,7 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_get_info", "sks_setup_open", "sks_setup_info", "sks_setup_material", "sks_setup_mass",
            "sks_setup_receivers", "sks_setup_schedule", "sks_setup_close", "sks_open_setup",
            "sks_kernel_launches", "sks_last_run_ms", "sks_enable_kernel_timing", "sks_kernel_timing",
-           "sks_set_tuning", "sks_get_tuning", "sks_autotune",
+           "sks_set_tuning", "sks_get_tuning", "sks_autotune", "sks_line_increments",
            "sks_destroy", "sks_last_error"]
 
 KERNEL_CLASSES = ["element", "seam", "inject", "record", "interp"]
@@ -47,7 +47,7 @@ class Info(C.Structure):
                                          "mtotal", "shtotal", "nrec_psv", "nrec_sh", "nmat", "anisotropic",
                                          "precision", "step")] + \
                [("eh", C.c_double), ("h", C.c_double), ("sdt", C.c_double), ("device_bytes", C.c_int64),
-                ("seam_points", C.c_int64), ("tile_rows", C.c_int32), ("reserved", C.c_int32)]
+                ("seam_points", C.c_int64), ("tile_rows", C.c_int32), ("neh", C.c_int32)]
 
     def asdict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -97,6 +97,7 @@ def lib() -> C.CDLL:
         L.sks_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
         L.sks_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
         L.sks_autotune.argtypes = [vp, C.c_int32, C.POINTER(Tuning)]
+        L.sks_line_increments.argtypes = [vp, C.c_int32, C.c_int32, dp]
         L.sks_destroy.argtypes = [vp]
         L.sks_destroy.restype = None
         L.sks_last_error.restype = C.c_char_p
@@ -218,6 +219,17 @@ class Solver:
 
     def reset(self):
         _check(lib().sks_reset(self.h))
+
+    def nline(self) -> int:
+        i = self.info()
+        nbl = i["neh"] * i["hpn"]
+        return (i["nx"] - nbl) + (i["nz"] - nbl - 1)
+
+    def line_increments(self, it0: int, nsteps: int) -> np.ndarray:
+        """FP64 boundary increments g(it+1)-g(it) of steps [it0, it0+nsteps): [nsteps, nline, 3]."""
+        out = np.zeros((nsteps, self.nline(), 3))
+        _check(lib().sks_line_increments(self.h, it0, nsteps, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
 
     def tuning(self) -> dict:
         t = Tuning()

@@ -182,3 +182,48 @@ def test_golden_inputs_fp64_vs_oracle_and_reference(path, tmp_path):
                 out = s.run(nst)
             assert seis_err(out, ref) <= tol
             assert seis_err(out, gold) <= 5e-5
+
+
+def _ring_traces(d, info, tp, wp, ts, ws, it):
+    """g(it) from the files and the schedule: four taps, then the |g| >= 10 guard."""
+    L = info["mtotal"]
+    psv = np.fromfile(os.path.join(d, "greenfile"), np.float32).reshape(-1, L).astype(np.float64)
+    sh = np.fromfile(os.path.join(d, "shgreenfile"), np.float32).reshape(-1, info["shtotal"]).astype(np.float64)
+    out = []
+    for rec, taps, w in ((psv, tp, wp), (sh, ts, ws)):
+        g = np.zeros(rec.shape[1])
+        for j in range(4):
+            if taps[it, j] >= 0:
+                g += w[it, j] * rec[taps[it, j]]
+        assert np.all(np.abs(g) < 10)
+        out.append(g)
+    return out
+
+
+def test_line_increments_match_schedule(casedirs):
+    """sks_line_increments = g(it+1) - g(it) of the four-tap interpolation."""
+    d, c, _ = casedirs["rdt_half_short_grt"]
+    with chdir(d), sks.Solver(["par=run.par"], precision=sks.FP64) as s, sks.Setup(["par=run.par"]) as su:
+        s.load_boundary_files()
+        info = s.info()
+        tp, wp, ts, ws = su.schedule()
+        it0, n = 3, 40
+        got = s.line_increments(it0, n)
+        nx, nz, nbl = info["nx"], info["nz"], info["neh"] * info["hpn"]
+        for k in range(n):
+            it = it0 + k
+            if it + 1 >= info["nt_inject"]:
+                assert not got[k].any()
+                continue
+            g0, v0 = _ring_traces(d, info, tp, wp, ts, ws, it)
+            g1, v1 = _ring_traces(d, info, tp, wp, ts, ws, it + 1)
+            row = np.stack([-g0[nbl:nx] + g1[nbl:nx], -v0[nbl:nx] + v1[nbl:nx],
+                            g0[nx + nbl:2 * nx] - g1[nx + nbl:2 * nx]], axis=1)
+            iz = np.arange(nbl + 1, nz)
+            col = np.stack([-g0[2 * nx + iz] + g1[2 * nx + iz], -v0[nx + iz] + v1[nx + iz],
+                            g0[2 * nx + nz + iz] - g1[2 * nx + nz + iz]], axis=1)
+            ref = np.concatenate([row, col])
+            assert np.allclose(got[k], ref, rtol=0, atol=1e-12 * max(1.0, np.abs(ref).max()))
+        # the injection window ends: the tail is zeros
+        tail = s.line_increments(info["nt_inject"] - 2, 5)
+        assert tail[0].any() and not tail[1:].any()
