@@ -102,6 +102,37 @@ int sks_run(sks_solver *s, int32_t nsteps, float *seis_u, float *seis_v, float *
  * the interpolated traces is allocated on the device for the call. */
 int sks_line_increments(sks_solver *s, int32_t it0, int32_t nsteps, double *out);
 
+/* The same boundary increments as sks_line_increments(), for callers that
+ * cannot allocate device memory when they need them: a serving process that
+ * has already divided the GPU's memory among its solves and gives each part
+ * only the buffers it owns, a host program whose plugin rules forbid the
+ * plugin from allocating, or a latency-critical path that cannot accept the
+ * device-wide synchronization cudaMalloc/cudaFree imply.  No counterpart in
+ * the reference (which has no library interface).
+ *
+ * Every pointer is DEVICE memory the caller owns: rec_psv / rec_sh are the
+ * boundary records (float32, 2*(nx+nz) and nx+nz values per record), the
+ * four-tap schedule (tap_* record indices, -1 for an empty slot; w_* FP64
+ * weights; 4 entries per step) covers nsteps+1 consecutive steps s..s+nsteps,
+ * and out receives nsteps*nline*3 doubles: the increment g(s+k+1) - g(s+k)
+ * of step s+k at every interface-line point (row nbl for ix >= nbl, then
+ * column nbl for iz > nbl; nline = (nx-nbl)+(nz-nbl-1)).  The work is queued
+ * on `stream` (a cudaStream_t; NULL for the default stream) and the call
+ * returns without waiting for it.
+ *
+ * It allocates nothing: the FP64 interpolated rows live in one fixed 8 MiB
+ * scratch array inside the library, so (nsteps+2)*3*(nx+nz) must not exceed
+ * 1048576 or the call fails with SKS_ERR_ARG.  The first call on a device
+ * looks the scratch's device address up (cudaGetSymbolAddress) and keeps it;
+ * make that first call before any stream capture.  All calls on a device
+ * share the scratch and it keeps the last call's contents (every value a call
+ * reads is written by that call first); calls whose work overlaps on the GPU
+ * (other streams, other host threads) race on it. */
+int sks_line_increments_noalloc(const float *rec_psv, const float *rec_sh, int32_t nx, int32_t nz,
+                                int32_t nbl, const int32_t *tap_psv, const double *w_psv,
+                                const int32_t *tap_sh, const double *w_sh, int32_t nsteps,
+                                double *out, void *stream);
+
 /* Back to step 0 with a zero wavefield (boundary records are kept). */
 int sks_reset(sks_solver *s);
 

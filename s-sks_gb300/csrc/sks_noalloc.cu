@@ -1,0 +1,83 @@
+// Boundary increments without any device allocation.
+//
+// Some callers cannot allocate device memory at the moment they need this
+// computation: a serving process that has already divided the GPU's memory
+// among its solve slots and hands each plugin only the buffers it owns, a
+// host program that embeds the solver through a plugin interface whose rules
+// forbid the plugin from allocating, or a latency-sensitive path where the
+// implicit device synchronization of cudaMalloc/cudaFree is not acceptable.
+// For them, sks_line_increments_noalloc() computes the same increments as
+// sks_line_increments() from buffers the caller already has on the device,
+// and keeps its FP64 interpolation rows in a fixed scratch array that is
+// part of the library image instead of calling cudaMalloc.
+#include "sks.h"
+#include "sks_kernels.cuh"
+#include "sks_aux_kernels.cuh"
+
+#include <cuda_runtime.h>
+#include <cstdio>
+#include <mutex>
+
+// Scratch for the FP64 interpolated traces: 1 Mi doubles (8 MiB).  Every GPU
+// that loads the library holds it until the process exits.
+static constexpr size_t kScratchDoubles = (size_t)1 << 20;
+static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
+
+extern "C" int sks_internal_set_error(int code, const char* msg, cudaError_t e);
+
+namespace {
+
+// Device address of the scratch, looked up once per device (with that device
+// current).  In host code the array's name is only a stand-in for the device
+// symbol, never a usable address.
+std::mutex g_mu;
+double* g_addr[128] = {};
+
+int fail(int code, const char* msg, cudaError_t e = cudaSuccess) { return sks_internal_set_error(code, msg, e); }
+
+}  // namespace
+
+extern "C" int sks_line_increments_noalloc(const float* rec_psv, const float* rec_sh, int32_t nx, int32_t nz,
+                                           int32_t nbl, const int32_t* tap_psv, const double* w_psv,
+                                           const int32_t* tap_sh, const double* w_sh, int32_t nsteps,
+                                           double* out, void* stream)
+{
+    if (!rec_psv || !rec_sh || !tap_psv || !w_psv || !tap_sh || !w_sh || !out)
+        return fail(SKS_ERR_ARG, "a device pointer is NULL");
+    if (nx < 2 || nz < 2 || nbl < 0 || nbl >= nx - 1 || nbl >= nz - 1 || nsteps < 0)
+        return fail(SKS_ERR_ARG, "bad sizes (nx, nz, nbl, nsteps)");
+    if (nsteps == 0) return SKS_OK;
+    const int mtotal = 2 * (nx + nz), shtotal = nx + nz, L = mtotal + shtotal;
+    const size_t need = (size_t)(nsteps + 2) * (size_t)L;
+    if (need > kScratchDoubles)
+        return fail(SKS_ERR_ARG, "nsteps too large for the fixed scratch: (nsteps+2)*(3*(nx+nz)) must be "
+                                 "at most 1048576");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(SKS_ERR_CUDA, "cudaGetDevice", e);
+    if (dev < 0 || dev >= 128) return fail(SKS_ERR_CUDA, "device index out of range");
+    double* scratch;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (!g_addr[dev]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess) return fail(SKS_ERR_CUDA, "cudaGetSymbolAddress of the scratch", e);
+            g_addr[dev] = (double*)p;
+        }
+        scratch = g_addr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    // rows 1..nsteps+1 of the scratch hold g(step) for the nsteps+1 steps the
+    // taps and weights describe; every row read below is written first, so
+    // nothing needs clearing between calls
+    sks::k_interp<<<nsteps + 1, 256, 0, st>>>(scratch, L, 0, nsteps + 1, rec_psv, mtotal, rec_sh, shtotal,
+                                              tap_psv, w_psv, tap_sh, w_sh);
+    const int nline = (nx - nbl) + (nz - nbl - 1);
+    const int64_t tot = (int64_t)nsteps * nline;
+    sks::k_line_delta<double><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(out, scratch + L, L, nsteps, nx, nz, nbl,
+                                                                             mtotal);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(SKS_ERR_CUDA, "kernel launch", e);
+    return SKS_OK;
+}

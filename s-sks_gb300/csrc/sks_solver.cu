@@ -37,6 +37,13 @@ static int set_err(int code, const char* fmt, ...)
 
 extern "C" const char* sks_last_error(void) { return g_err; }
 
+// error reporting for the library's other translation units
+extern "C" __attribute__((visibility("hidden"))) int sks_internal_set_error(int code, const char* msg, cudaError_t e)
+{
+    if (e != cudaSuccess) return set_err(code, "%s: %s", msg, cudaGetErrorString(e));
+    return set_err(code, "%s", msg);
+}
+
 struct sks_solver {
     sks_model m;
     int precision, device;

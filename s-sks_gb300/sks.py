@@ -31,6 +31,7 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_setup_receivers", "sks_setup_schedule", "sks_setup_close", "sks_open_setup",
            "sks_kernel_launches", "sks_last_run_ms", "sks_enable_kernel_timing", "sks_kernel_timing",
            "sks_set_tuning", "sks_get_tuning", "sks_autotune", "sks_line_increments",
+           "sks_line_increments_noalloc",
            "sks_destroy", "sks_last_error"]
 
 KERNEL_CLASSES = ["element", "seam", "inject", "record", "interp"]
@@ -98,6 +99,8 @@ def lib() -> C.CDLL:
         L.sks_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
         L.sks_autotune.argtypes = [vp, C.c_int32, C.POINTER(Tuning)]
         L.sks_line_increments.argtypes = [vp, C.c_int32, C.c_int32, dp]
+        L.sks_line_increments_noalloc.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp,
+                                                  C.c_int32, vp, vp]
         L.sks_destroy.argtypes = [vp]
         L.sks_destroy.restype = None
         L.sks_last_error.restype = C.c_char_p
