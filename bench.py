@@ -41,7 +41,14 @@ import numpy as np  # noqa: E402
 
 NEX, NEZ = 800, 300
 FULL_STEPS = 24000
-BYTES_PER_POINT = {"fp32c": 74, "fp64": 74}   # see the roofline note in main()
+# Algorithmic bytes per GLL-point update of the anisotropic 3-component step:
+# W x (3 u^n read + 3 u^(n-1) read + 3 u^(n+1) write + 1 inverse mass + 15 c_ij)
+# plus, for the compensated FP32 form, 4 B x 3 compensation words read and
+# written: 124 B (FP32C), 200 B (FP64).  The kernels move less than that (the
+# material is a 2-byte index into a table and the inverse mass is rebuilt from
+# GLL weights): 74 B per point in both forms (LAYOUT_BYTES_PER_POINT).
+BYTES_PER_POINT = {"fp32c": 124, "fp64": 200}
+LAYOUT_BYTES_PER_POINT = {"fp32c": 74, "fp64": 74}
 WORKLOAD = ("anisotropic 3-component SKS solve: 800x300 elements of 1 km, GLL degree 4, "
             "3,844,401 points, 100 km hexagonal layer (4 %, azimuth 45, tilt 20), dt 5 ms, 201 receivers")
 
@@ -366,13 +373,16 @@ def main() -> None:
     v64 = world * npts * r64["steps"] / (ms64 / 1e3)
     peak, peak_kind = _peaks()
     # roofline of the dominant kernel (the fused step kernel): algorithmic
-    # bytes per launch = points it updates x 74 B (u, d, Kahan c: 3 x 4 B read
-    # and written each, 2 B material index) over its mean event-timed duration
+    # bytes per launch = points it updates x 124 B over its mean event-timed
+    # duration; the same with the 74 B the layout actually moves beside it
     km, kc = r32["kernels"]["element"]
     main_pts = npts
     t_launch = km / max(1, kc) / 1e3
     achieved = main_pts * BYTES_PER_POINT["fp32c"] / t_launch / 1e9
+    achieved_layout = main_pts * LAYOUT_BYTES_PER_POINT["fp32c"] / t_launch / 1e9
     traffic = _traffic_per_launch(main_pts)
+    km64, kc64 = r64["kernels"]["element"]
+    t64 = km64 / max(1, kc64) / 1e3
     total_k = sum(v[0] for v in r32["kernels"].values())
     line = {
         "metric": "GLL-pt updates/s", "value": value, "unit": "GLL-pt updates/s", "n_gpus": world,
@@ -384,13 +394,19 @@ def main() -> None:
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "k_step (element force + assembly + update + receivers + injection)",
-                     "kernel_ms_per_launch": t_launch * 1e3, "kernel_share": km / max(total_k, 1e-12)},
+                     "kernel_ms_per_launch": t_launch * 1e3, "kernel_share": km / max(total_k, 1e-12),
+                     "bytes_per_point": BYTES_PER_POINT["fp32c"], "points_per_launch": main_pts,
+                     "layout_bytes_per_point": LAYOUT_BYTES_PER_POINT["fp32c"],
+                     "achieved_layout_bytes": achieved_layout, "frac_layout_bytes": achieved_layout / peak},
         "e2e": {"value": world * npts * e2e["steps"] / e2e_wall, "unit": "GLL-pt updates/s",
                 "h2d_bytes_per_step": e2e["h2d_bytes_per_step"], "d2h_bytes_per_step": e2e["d2h_bytes_per_step"]},
         "gpu_launches": r32["launches"],
         "clocks": r32.get("clocks"),
         "fp64": {"value": v64, "unit": "GLL-pt updates/s", "ms_per_step": ms64 / r64["steps"],
-                 "steps": r64["steps"]},
+                 "steps": r64["steps"],
+                 "roofline": {"bound": "fp64 pipe", "kernel_ms_per_launch": t64 * 1e3,
+                              "achieved_gbs": npts * BYTES_PER_POINT["fp64"] / t64 / 1e9,
+                              "bytes_per_point": BYTES_PER_POINT["fp64"], "peak_gbs": peak}},
         "solves_per_hour": {"fp32c": 3600.0 / (FULL_STEPS * ms32 / r32["steps"] / 1e3) * world,
                             "fp64": 3600.0 / (FULL_STEPS * ms64 / r64["steps"] / 1e3) * world,
                             "solve_steps": FULL_STEPS},
@@ -410,7 +426,7 @@ def _traffic_per_launch(points: int):
         return None
     with open(p) as f:
         t = json.load(f)
-    bpp = t.get("fp32c_bytes_per_point")
+    bpp = t.get("fp32c_dram_bytes_per_point")
     return None if bpp is None else bpp * points
 
 
