@@ -224,7 +224,49 @@ double sks_last_run_ms(const sks_solver *s);
 int sks_enable_kernel_timing(sks_solver *s, int on);   /* also clears the sums */
 int sks_kernel_timing(const sks_solver *s, double *ms, int64_t *count);  /* arrays of SKS_KERNEL_CLASSES */
 
+/* Destroys the solver; a batch member leaves its batch first. */
 void sks_destroy(sks_solver *s);
+
+/* ---- batches ----------------------------------------------------------
+ * Many solves advanced together on one GPU.  The reference runs one solve per
+ * process (sem2d_psvsh.c:82, launched once per event by the driver scripts,
+ * applications/test/prem_epi83.pl:81-82); a batch replaces a set of such
+ * processes.  Members are ordinary solvers of one form and device, each with
+ * its own mesh, materials, time step, boundary records and step count.  One
+ * step of every member is one launch of a persistent kernel; a chunk of 64
+ * steps (boundary interpolation, increments, 64 step launches) is one launch
+ * of a CUDA graph that the batch captures once and reuses.  A member runs
+ * with the batch's tuning, and its seismograms are bit-identical to the same
+ * solver run alone with that tuning.  Members keep their wavefields on the
+ * device between calls; solvers may join and leave between calls.  A
+ * member's tuning belongs to the batch (sks_set_tuning / sks_autotune on a
+ * member return SKS_ERR_STATE); sks_run on a member runs it alone. */
+typedef struct sks_batch sks_batch;
+
+int sks_batch_create(int precision, int device, sks_batch **out);
+/* Joins at the solver's current step; allocates its whole-run seismogram
+ * buffer on the device ([nst][3][ntrace] floats) on first joining. */
+int sks_batch_add(sks_batch *b, sks_solver *s);
+int sks_batch_remove(sks_batch *b, sks_solver *s);
+int sks_batch_size(const sks_batch *b);
+
+/* Advances every member by min(nsteps, the steps its run has left).  Member
+ * i's new seismogram rows go to su[i], sv[i], sw[i] as sks_run() writes them
+ * (any array, or any entry, may be NULL).  Returns the most steps any member
+ * took, or a negative status. */
+int sks_batch_run(sks_batch *b, int32_t nsteps, float *const *su, float *const *sv, float *const *sw);
+
+/* Tuning shared by the members (waves must be 0: the batch's persistent grid
+ * balances the tiles).  sks_batch_autotune times every candidate on the
+ * members' next `steps` steps and restores their state afterwards. */
+int sks_batch_set_tuning(sks_batch *b, const sks_tuning_t *t);
+int sks_batch_get_tuning(const sks_batch *b, sks_tuning_t *t);
+int sks_batch_autotune(sks_batch *b, int32_t steps, sks_tuning_t *best);
+
+double sks_batch_last_run_ms(const sks_batch *b);     /* events on the batch's stream */
+int64_t sks_batch_kernel_launches(const sks_batch *b);
+/* Destroys the batch; the members stay open and leave it. */
+void sks_batch_destroy(sks_batch *b);
 
 const char *sks_last_error(void);
 

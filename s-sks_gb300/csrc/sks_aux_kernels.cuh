@@ -6,20 +6,16 @@
 
 namespace sks {
 
-// Boundary-trace interpolation for a chunk of steps (interpl.c:16-54): row r of
-// Gout (r = 1..S) is step s0+r-1; four taps of FP32 records with FP64 weights,
+// Boundary-trace interpolation of one step (interpl.c:16-54) into one row of
+// L = mtotal + shtotal values: four taps of FP32 records with FP64 weights,
 // then the |g| >= 10 guard of sem2d_psvsh.c:432-444 (sequential, ends read 0).
-static __global__ void __launch_bounds__(256) k_interp(double* __restrict__ Gout, int L, int s0, int nsteps,
-                                                const float* __restrict__ rpsv, int mtotal,
-                                                const float* __restrict__ rsh, int shtotal,
-                                                const int32_t* __restrict__ tap_psv, const double* __restrict__ w_psv,
-                                                const int32_t* __restrict__ tap_sh, const double* __restrict__ w_sh)
+// Called by a whole block.
+__device__ __forceinline__ void interp_row(double* __restrict__ out, int it, const float* __restrict__ rpsv, int mtotal,
+                                           const float* __restrict__ rsh, int shtotal,
+                                           const int32_t* __restrict__ tap_psv, const double* __restrict__ w_psv,
+                                           const int32_t* __restrict__ tap_sh, const double* __restrict__ w_sh,
+                                           int* bad)
 {
-    const int r = blockIdx.x;
-    if (r >= nsteps) return;
-    const int it = s0 + r;
-    double* out = Gout + (int64_t)(r + 1) * L;
-    __shared__ int bad[2];
     if (threadIdx.x < 2) bad[threadIdx.x] = 0;
     __syncthreads();
     for (int fam = 0; fam < 2; fam++) {
@@ -57,19 +53,28 @@ static __global__ void __launch_bounds__(256) k_interp(double* __restrict__ Gout
     }
 }
 
-// Increments of the interface line for the steps of a chunk, in the form's
-// type: row r of Dl is step it0+r's injection g(it0+r) - g(it0+r-1) taken
-// from G rows r+1 and r (the same FP64 expressions as GRT_Interface4,
-// sem2d_psvsh.c:2076-2111, converted once).  Line points: row nbl (ix >=
-// nbl), then column nbl (iz > nbl).
-template <typename T>
-__global__ void __launch_bounds__(256) k_line_delta(T* __restrict__ Dl, const double* __restrict__ G, int L,
-                                                    int nsteps, int nx, int nz, int nbl, int mtotal)
+// Interpolation for a chunk of steps: row r of Gout (r = 1..nsteps) is step s0+r-1.
+static __global__ void __launch_bounds__(256) k_interp(double* __restrict__ Gout, int L, int s0, int nsteps,
+                                                const float* __restrict__ rpsv, int mtotal,
+                                                const float* __restrict__ rsh, int shtotal,
+                                                const int32_t* __restrict__ tap_psv, const double* __restrict__ w_psv,
+                                                const int32_t* __restrict__ tap_sh, const double* __restrict__ w_sh)
 {
-    const int nrow = nx - nbl, ncol = nz - nbl - 1, nline = nrow + ncol;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (int64_t)nsteps * nline) return;
-    const int r = (int)(i / nline), li = (int)(i - (int64_t)r * nline);
+    const int r = blockIdx.x;
+    if (r >= nsteps) return;
+    __shared__ int bad[2];
+    interp_row(Gout + (int64_t)(r + 1) * L, s0 + r, rpsv, mtotal, rsh, shtotal, tap_psv, w_psv, tap_sh, w_sh, bad);
+}
+
+// One value triple of the interface-line increments: g(step of G row r+1) -
+// g(step of G row r) at line point li, with the FP64 expressions of
+// GRT_Interface4 (sem2d_psvsh.c:2076-2111), converted once to the form's type.
+// Line points: row nbl (ix >= nbl), then column nbl (iz > nbl).
+template <typename T>
+__device__ __forceinline__ void line_delta_one(T* __restrict__ o, const double* __restrict__ G, int L, int r, int li,
+                                               int nx, int nz, int nbl, int mtotal)
+{
+    const int nrow = nx - nbl;
     const double* g1 = G + (int64_t)(r + 1) * L;
     const double* g0 = G + (int64_t)r * L;
     const double *v1 = g1 + mtotal, *v0 = g0 + mtotal;
@@ -85,8 +90,83 @@ __global__ void __launch_bounds__(256) k_line_delta(T* __restrict__ Dl, const do
         d3[1] = -v0[nx + iz] + v1[nx + iz];
         d3[2] = g0[2 * nx + nz + iz] - g1[2 * nx + nz + iz];
     }
-    T* o = Dl + ((int64_t)r * nline + li) * 3;
     o[0] = (T)d3[0]; o[1] = (T)d3[1]; o[2] = (T)d3[2];
+}
+
+// Increments of the interface line for the steps of a chunk: row r of Dl is
+// step it0+r's injection g(it0+r) - g(it0+r-1) taken from G rows r+1 and r.
+template <typename T>
+__global__ void __launch_bounds__(256) k_line_delta(T* __restrict__ Dl, const double* __restrict__ G, int L,
+                                                    int nsteps, int nx, int nz, int nbl, int mtotal)
+{
+    const int nline = (nx - nbl) + (nz - nbl - 1);
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)nsteps * nline) return;
+    const int r = (int)(i / nline), li = (int)(i - (int64_t)r * nline);
+    line_delta_one<T>(Dl + ((int64_t)r * nline + li) * 3, G, L, r, li, nx, nz, nbl, mtotal);
+}
+
+// Boundary inputs of one batch member, for the batched interpolation.
+struct BatchAux {
+    double* G;                     // interpolation rows [(chunk+2)][L]
+    void* dl;                      // line increments [chunk+1][nline][3] in the form's type
+    const float* rec_psv;
+    const float* rec_sh;
+    const int32_t* tap_psv;
+    const int32_t* tap_sh;
+    const double* w_psv;
+    const double* w_sh;
+    int mtotal, shtotal, nt_sem, nx, nz, nbl, L, nline;
+};
+
+// Batched interpolation: block (r, m) computes member m's G row r+1, the step
+// it0+r, for the rows its chunk injects from (as run by one mesh's chunk).
+static __global__ void __launch_bounds__(256) k_interp_batch(const BatchAux* __restrict__ aux,
+                                                      const BatchState* __restrict__ state,
+                                                      const BatchHeader* __restrict__ hdr)
+{
+    const int m = blockIdx.y, r = blockIdx.x;
+    if (m >= hdr->nmem) return;
+    const BatchState st = state[m];
+    const BatchAux a = aux[m];
+    if (st.n <= 0) return;
+    const int ni = min(st.it0 + st.n + 1, a.nt_sem) - st.it0;
+    if (r >= ni) return;
+    __shared__ int bad[2];
+    interp_row(a.G + (int64_t)(r + 1) * a.L, st.it0 + r, a.rec_psv, a.mtotal, a.rec_sh, a.shtotal, a.tap_psv, a.w_psv,
+               a.tap_sh, a.w_sh, bad);
+}
+
+// Batched line increments: blocks (x, m) stride over member m's rows.
+template <typename T>
+__global__ void __launch_bounds__(256) k_line_delta_batch(const BatchAux* __restrict__ aux,
+                                                          const BatchState* __restrict__ state,
+                                                          const BatchHeader* __restrict__ hdr)
+{
+    const int m = blockIdx.y;
+    if (m >= hdr->nmem) return;
+    const BatchState st = state[m];
+    const BatchAux a = aux[m];
+    if (st.n <= 0) return;
+    const int nd = max(0, min(st.it0 + st.n + 1, a.nt_sem) - st.it0 - 1);
+    const int64_t tot = (int64_t)nd * a.nline;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / a.nline), li = (int)(i - (int64_t)r * a.nline);
+        line_delta_one<T>((T*)a.dl + ((int64_t)r * a.nline + li) * 3, a.G + a.L, a.L, r, li, a.nx, a.nz, a.nbl,
+                          a.mtotal);
+    }
+}
+
+// End of a chunk: every member's step moves on by the steps it took, and the
+// next chunk takes up to `chunk` more, stopping at the member's target.
+static __global__ void k_batch_advance(BatchState* __restrict__ state, const BatchHeader* __restrict__ hdr)
+{
+    for (int m = threadIdx.x; m < hdr->nmem; m += blockDim.x) {
+        BatchState st = state[m];
+        st.it0 += st.n;
+        st.n = max(0, min(hdr->chunk, st.target - st.it0));
+        state[m] = st;
+    }
 }
 
 // GRT_Interface4 (sem2d_psvsh.c:2076-2111): u^n += g(it) - g(it-1) on row nbl

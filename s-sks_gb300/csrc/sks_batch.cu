@@ -1,0 +1,552 @@
+// Batches: many meshes advanced together, one step of every member per launch
+// of a persistent kernel, a chunk of 64 steps per launch of one captured CUDA
+// graph.
+//
+// A member is an ordinary solver (sks_open_par / sks_open_setup) with its own
+// mesh size, materials, time step, boundary records and step count.  While in
+// a batch it runs with the batch's tuning (warps per CTA, band rows, band
+// seams, register cap), so the tiles and the summation order are those of a
+// solver with that tuning alone: a member's seismograms are bit-identical to
+// the same solver run by itself with the same tuning.
+//
+// The device keeps every member's step (BatchState) and advances it at the end
+// of each chunk, so the graph -- batched boundary interpolation, batched
+// interface increments, 64 step launches, the advance -- is the same for every
+// chunk and every call; joining and leaving members only rewrite the tables
+// the graph reads.  Step 0 (zero the field, set the interface line, record,
+// inject step 1) runs once per member through the single-mesh path before its
+// first batched chunk.
+#include "sks_internal.h"
+#include "sks_aux_kernels.cuh"
+
+#include <algorithm>
+#include <cstdio>
+
+using namespace sks;
+using namespace sksi;
+
+struct sks_batch {
+    int precision = SKS_FP32C, device = 0, sms = 152;
+    std::vector<sks_solver*> mem;
+    cudaStream_t stream = nullptr;
+    int NW = 4, HZ = 6, ZS = 0, CAP = 1;  // tuning shared by the members
+    int chunk = 64;
+    bool aniso = false;                   // the step variant: any member anisotropic
+    int grid = 0;                         // persistent CTAs of a step launch
+    // device tables (capacity `cap` members, `items_cap` tiles)
+    void* dmem = nullptr;                 // BatchMember<T>[cap]
+    BatchAux* daux = nullptr;
+    BatchState* dstate = nullptr;
+    BatchHeader* dhdr = nullptr;
+    int4* ditems = nullptr;
+    int cap = 0;
+    size_t items_cap = 0;
+    int nitems = 0;
+    BatchState* hstate = nullptr;         // pinned staging of the members' steps
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int graph_kernels = 0;                // kernels one graph launch runs
+    bool tables_dirty = true;
+    bool graph_dirty = true;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    double last_ms = 0.0;
+    int64_t launches = 0;
+    int64_t device_bytes = 0;
+};
+
+namespace {
+
+bool member_aniso(const sks_solver* s) { return s->m.anisotropic != 0; }
+
+int nline_of(const sks_solver* s) { return (s->m.nx - s->nbl) + (s->m.nz - s->nbl - 1); }
+
+void free_tables(sks_batch* b)
+{
+    void* ps[] = {b->dmem, b->daux, b->dstate, b->dhdr, b->ditems};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    if (b->hstate) cudaFreeHost(b->hstate);
+    b->dmem = nullptr; b->daux = nullptr; b->dstate = nullptr; b->dhdr = nullptr; b->ditems = nullptr;
+    b->hstate = nullptr;
+    b->cap = 0;
+    b->items_cap = 0;
+    b->device_bytes = 0;
+}
+
+void free_graph(sks_batch* b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->graph_dirty = true;
+}
+
+// a member's grid follows the batch's tuning (plain bands of HZ rows)
+int apply_tuning(sks_batch* b, sks_solver* s)
+{
+    int rc = set_grid(s, b->NW, b->HZ, b->ZS, b->CAP, 0);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    return SKS_OK;
+}
+
+template <typename T>
+BatchMember<T> member_desc(sks_solver* s)
+{
+    BatchMember<T> d;
+    memset(&d, 0, sizeof d);
+    d.F = make_field<T>(s);
+    d.G = make_geo<T>(s);
+    d.G.items = nullptr;
+    d.U[0] = (T*)s->U[0];
+    d.U[1] = (T*)s->U[1];
+    d.dl = (const T*)s->Dl;
+    d.seis = s->seis_full;
+    d.nt_sem = s->m.nt_sem;
+    d.nline = nline_of(s);
+    return d;
+}
+
+BatchAux aux_desc(sks_solver* s)
+{
+    BatchAux a;
+    memset(&a, 0, sizeof a);
+    a.G = s->G;
+    a.dl = s->Dl;
+    a.rec_psv = s->rec_psv;
+    a.rec_sh = s->rec_sh;
+    a.tap_psv = s->tap_psv;
+    a.tap_sh = s->tap_sh;
+    a.w_psv = s->w_psv;
+    a.w_sh = s->w_sh;
+    a.mtotal = s->m.mtotal;
+    a.shtotal = s->m.shtotal;
+    a.nt_sem = s->m.nt_sem;
+    a.nx = s->m.nx;
+    a.nz = s->m.nz;
+    a.nbl = s->nbl;
+    a.L = s->m.mtotal + s->m.shtotal;
+    a.nline = nline_of(s);
+    return a;
+}
+
+// Rebuild and upload the member descriptors and the tile table; the tables
+// grow (and the graph is captured again) when they are too small.
+template <typename T>
+int build_tables(sks_batch* b)
+{
+    const int n = (int)b->mem.size();
+    std::vector<BatchMember<T>> md;
+    std::vector<BatchAux> ad;
+    std::vector<int4> items;
+    bool aniso = false;
+    for (int i = 0; i < n; i++) {
+        sks_solver* s = b->mem[i];
+        aniso = aniso || member_aniso(s);
+        md.push_back(member_desc<T>(s));
+        ad.push_back(aux_desc(s));
+        if (s->ncx >= (1 << 16) || s->ncz >= (1 << 15))
+            return set_err(SKS_ERR_UNSUPPORTED, "member %d: %d x %d tiles exceed the batch's tile index", i, s->ncx, s->ncz);
+        for (int cz = 0; cz < s->ncz; cz++)
+            for (int cx = 0; cx < s->ncx; cx++)
+                items.push_back(make_int4(i, cx | (cz << 16), cz * s->HZ, std::min((cz + 1) * s->HZ, s->m.nez)));
+    }
+    if (aniso != b->aniso) {
+        b->aniso = aniso;
+        b->graph_dirty = true;
+    }
+    if (n > b->cap) {
+        const int cap = std::max(n, std::max(8, 2 * b->cap));
+        void* ps[] = {b->dmem, b->daux, b->dstate};
+        for (void* p : ps)
+            if (p) cudaFree(p);
+        if (b->hstate) cudaFreeHost(b->hstate);
+        b->dmem = nullptr; b->daux = nullptr; b->dstate = nullptr; b->hstate = nullptr;
+        b->cap = 0;
+        CK(cudaMalloc(&b->dmem, sizeof(BatchMember<T>) * cap));
+        CK(cudaMalloc((void**)&b->daux, sizeof(BatchAux) * cap));
+        CK(cudaMalloc((void**)&b->dstate, sizeof(BatchState) * cap));
+        CK(cudaMallocHost((void**)&b->hstate, sizeof(BatchState) * cap));
+        CK(cudaMemset(b->dstate, 0, sizeof(BatchState) * cap));
+        b->cap = cap;
+        b->graph_dirty = true;
+    }
+    if (!b->dhdr) {
+        CK(cudaMalloc((void**)&b->dhdr, sizeof(BatchHeader)));
+        b->graph_dirty = true;
+    }
+    if (items.size() > b->items_cap) {
+        const size_t ic = std::max(items.size(), 2 * b->items_cap);
+        if (b->ditems) cudaFree(b->ditems);
+        b->ditems = nullptr;
+        b->items_cap = 0;
+        CK(cudaMalloc((void**)&b->ditems, sizeof(int4) * ic));
+        b->items_cap = ic;
+        b->graph_dirty = true;
+    }
+    b->device_bytes = (int64_t)(sizeof(BatchMember<T>) + sizeof(BatchAux) + sizeof(BatchState)) * b->cap +
+                      (int64_t)sizeof(int4) * (int64_t)b->items_cap + (int64_t)sizeof(BatchHeader);
+    if (n) {
+        CK(cudaMemcpyAsync(b->dmem, md.data(), sizeof(BatchMember<T>) * n, cudaMemcpyHostToDevice, b->stream));
+        CK(cudaMemcpyAsync(b->daux, ad.data(), sizeof(BatchAux) * n, cudaMemcpyHostToDevice, b->stream));
+    }
+    if (!items.empty())
+        CK(cudaMemcpyAsync(b->ditems, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, b->stream));
+    BatchHeader h = {(int)items.size(), n, b->chunk, 0};
+    CK(cudaMemcpyAsync(b->dhdr, &h, sizeof h, cudaMemcpyHostToDevice, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    b->nitems = (int)items.size();
+    b->tables_dirty = false;
+    return SKS_OK;
+}
+
+template <typename T>
+cudaError_t launch_steps(sks_batch* b, int j)
+{
+    const StepVariant v{b->NW, b->ZS, b->CAP};
+    static thread_local Coef<T> k;
+    k = make_coef<T>(b->mem[0]->m);     // GLL tables: the same for every member
+    if (sizeof(T) == 4)
+        return launch_batch_f32(v, b->aniso, b->grid, b->stream, (const BatchMember<float>*)b->dmem, b->dstate, b->ditems,
+                                b->dhdr, j, *(const Coef<float>*)&k);
+    return launch_batch_f64(v, b->aniso, b->grid, b->stream, (const BatchMember<double>*)b->dmem, b->dstate, b->ditems,
+                            b->dhdr, j, *(const Coef<double>*)&k);
+}
+
+// persistent grid: every SM full of resident CTAs of the step variant
+void set_persistent_grid(sks_batch* b)
+{
+    const StepVariant v{b->NW, b->ZS, b->CAP};
+    const int occ = b->precision == SKS_FP64 ? batch_occupancy_f64(v, b->aniso) : batch_occupancy_f32(v, b->aniso);
+    b->grid = b->sms * occ;
+}
+
+template <typename T>
+int capture_graph(sks_batch* b)
+{
+    free_graph(b);
+    set_persistent_grid(b);
+    cudaStream_t st = b->stream;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    k_interp_batch<<<dim3(b->chunk + 1, b->cap), 256, 0, st>>>(b->daux, b->dstate, b->dhdr);
+    k_line_delta_batch<T><<<dim3(32, b->cap), 256, 0, st>>>(b->daux, b->dstate, b->dhdr);
+    cudaError_t e = cudaSuccess;
+    for (int j = 0; j < b->chunk && e == cudaSuccess; j++) e = launch_steps<T>(b, j);
+    k_batch_advance<<<1, 256, 0, st>>>(b->dstate, b->dhdr);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(st, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return set_err(SKS_ERR_CUDA, "capture of the batch graph: %s",
+                       cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    b->graph = g;
+    CK(cudaGraphInstantiate(&b->exec, g, 0));
+    b->graph_kernels = b->chunk + 3;
+    b->graph_dirty = false;
+    return SKS_OK;
+}
+
+int prepare(sks_batch* b)
+{
+    int rc = SKS_OK;
+    if (b->tables_dirty)
+        rc = b->precision == SKS_FP64 ? build_tables<double>(b) : build_tables<float>(b);
+    if (!rc && b->graph_dirty)
+        rc = b->precision == SKS_FP64 ? capture_graph<double>(b) : capture_graph<float>(b);
+    return rc;
+}
+
+// step 0 of a member through the single-mesh path, its seismogram row into
+// the member's whole-run buffer
+int first_step(sks_solver* s)
+{
+    s->seis = s->seis_full;
+    int rc = run_chunk(s, 0, 1);
+    s->seis = s->seisbuf[0];
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    s->step = 1;
+    return SKS_OK;
+}
+
+int check_member(const sks_batch* b, const sks_solver* s, int i)
+{
+    if (s->step < s->m.nt_sem && !s->boundary_ready)
+        return set_err(SKS_ERR_STATE, "member %d: boundary records not set", i);
+    (void)b;
+    return SKS_OK;
+}
+
+}  // namespace
+
+namespace sksi {
+
+void batch_detach(sks_solver* s)
+{
+    sks_batch* b = s->batch;
+    if (!b) return;
+    cudaStreamSynchronize(b->stream);
+    b->mem.erase(std::remove(b->mem.begin(), b->mem.end(), s), b->mem.end());
+    b->tables_dirty = true;
+    s->batch = nullptr;
+}
+
+}  // namespace sksi
+
+extern "C" int sks_batch_create(int precision, int device, sks_batch** out)
+{
+    if (!out) return set_err(SKS_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (precision != SKS_FP64 && precision != SKS_FP32C) return set_err(SKS_ERR_ARG, "unknown precision %d", precision);
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return set_err(SKS_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+    sks_batch* b = new (std::nothrow) sks_batch();
+    if (!b) return set_err(SKS_ERR_NOMEM, "cannot allocate the batch");
+    b->precision = precision;
+    b->device = device;
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
+    if (precision == SKS_FP64) { b->NW = 4; b->HZ = 8; b->ZS = 1; b->CAP = 0; }
+    e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev[0]);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev[1]);
+    if (e != cudaSuccess) {
+        if (b->stream) cudaStreamDestroy(b->stream);
+        delete b;
+        return set_err(SKS_ERR_CUDA, "batch stream/events: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return SKS_OK;
+}
+
+extern "C" int sks_batch_add(sks_batch* b, sks_solver* s)
+{
+    if (!b || !s) return set_err(SKS_ERR_ARG, "NULL argument");
+    if (s->batch) return set_err(SKS_ERR_STATE, "the solver is already a member of a batch");
+    if (s->precision != b->precision) return set_err(SKS_ERR_ARG, "the solver's form differs from the batch's");
+    if (s->device != b->device) return set_err(SKS_ERR_ARG, "the solver is on device %d, the batch on %d", s->device, b->device);
+    cudaSetDevice(b->device);
+    const sks_model& m = s->m;
+    if (!s->seis_full) {
+        const size_t n = (size_t)std::max(1, m.nst) * 3 * std::max(1, m.ntrace);
+        cudaError_t e = cudaMalloc((void**)&s->seis_full, n * sizeof(float));
+        if (e != cudaSuccess) {
+            s->seis_full = nullptr;
+            return set_err(SKS_ERR_NOMEM, "whole-run seismograms (%zu bytes): %s", n * sizeof(float), cudaGetErrorString(e));
+        }
+        s->device_bytes += (int64_t)(n * sizeof(float));
+        CK(cudaMemsetAsync(s->seis_full, 0, n * sizeof(float), s->stream));
+    }
+    int rc = apply_tuning(b, s);
+    if (rc) return rc;
+    s->batch = b;
+    b->mem.push_back(s);
+    b->tables_dirty = true;
+    return SKS_OK;
+}
+
+extern "C" int sks_batch_remove(sks_batch* b, sks_solver* s)
+{
+    if (!b || !s) return set_err(SKS_ERR_ARG, "NULL argument");
+    if (s->batch != b) return set_err(SKS_ERR_STATE, "the solver is not a member of this batch");
+    batch_detach(s);
+    return SKS_OK;
+}
+
+extern "C" int sks_batch_size(const sks_batch* b) { return b ? (int)b->mem.size() : -1; }
+
+extern "C" int sks_batch_run(sks_batch* b, int32_t nsteps, float* const* su, float* const* sv, float* const* sw)
+{
+    if (!b) return set_err(SKS_ERR_ARG, "batch is NULL");
+    if (nsteps < 0) return set_err(SKS_ERR_ARG, "nsteps=%d", nsteps);
+    cudaSetDevice(b->device);
+    const int n = (int)b->mem.size();
+    if (n == 0) return 0;
+    std::vector<int> start(n), target(n);
+    int rc = SKS_OK;
+    for (int i = 0; i < n; i++) {
+        sks_solver* s = b->mem[i];
+        if ((rc = check_member(b, s, i))) return rc;
+        start[i] = s->step;
+        target[i] = std::min(s->m.nst, s->step + nsteps);
+    }
+    CK(cudaEventRecord(b->ev[0], b->stream));
+    for (int i = 0; i < n; i++) {
+        sks_solver* s = b->mem[i];
+        if (s->step == 0 && target[i] > 0 && (rc = first_step(s))) return rc;
+    }
+    if ((rc = prepare(b))) return rc;
+    int most = 0;
+    for (int i = 0; i < n; i++) {
+        sks_solver* s = b->mem[i];
+        const int left = std::max(0, target[i] - s->step);
+        b->hstate[i] = BatchState{s->step, std::min(b->chunk, left), target[i], 0};
+        most = std::max(most, left);
+    }
+    if (n) CK(cudaMemcpyAsync(b->dstate, b->hstate, sizeof(BatchState) * n, cudaMemcpyHostToDevice, b->stream));
+    const int nchunks = (most + b->chunk - 1) / b->chunk;
+    for (int c = 0; c < nchunks; c++) {
+        CK(cudaGraphLaunch(b->exec, b->stream));
+        b->launches += b->graph_kernels;
+    }
+    CK(cudaEventRecord(b->ev[1], b->stream));
+    // the new seismogram rows of each member into the caller's arrays
+    for (int i = 0; i < n; i++) {
+        sks_solver* s = b->mem[i];
+        const int nt = s->m.ntrace, rows = target[i] - start[i];
+        if (nt <= 0 || rows <= 0) continue;
+        float* dst[3] = {su ? su[i] : nullptr, sv ? sv[i] : nullptr, sw ? sw[i] : nullptr};
+        const size_t w = sizeof(float) * (size_t)nt;
+        for (int c = 0; c < 3; c++)
+            if (dst[c])
+                CK(cudaMemcpy2DAsync(dst[c], w, s->seis_full + (size_t)start[i] * 3 * nt + (size_t)c * nt, 3 * w, w,
+                                     (size_t)rows, cudaMemcpyDeviceToHost, b->stream));
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
+    b->last_ms = ms;
+    int adv = 0;
+    for (int i = 0; i < n; i++) {
+        sks_solver* s = b->mem[i];
+        if (target[i] > s->step) {
+            s->step = target[i];
+            s->cur = (target[i] - 1) & 1;
+            s->g_last = 0;
+        }
+        adv = std::max(adv, target[i] - start[i]);
+    }
+    return adv;
+}
+
+extern "C" int sks_batch_set_tuning(sks_batch* b, const sks_tuning_t* t)
+{
+    if (!b || !t) return set_err(SKS_ERR_ARG, "NULL argument");
+    if (t->warps_per_block != 2 && t->warps_per_block != 4)
+        return set_err(SKS_ERR_ARG, "warps_per_block=%d: 2 or 4", t->warps_per_block);
+    if (t->register_cap < 0 || t->register_cap > 2) return set_err(SKS_ERR_ARG, "register_cap=%d: 0, 1 or 2", t->register_cap);
+    if (t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
+    if (t->waves != 0) return set_err(SKS_ERR_ARG, "a batch uses plain bands (waves=0)");
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);
+    b->NW = t->warps_per_block;
+    b->HZ = t->band_rows;
+    b->ZS = t->zseam ? 1 : 0;
+    b->CAP = t->register_cap;
+    for (sks_solver* s : b->mem) {
+        int rc = apply_tuning(b, s);
+        if (rc) return rc;
+    }
+    b->tables_dirty = true;
+    b->graph_dirty = true;
+    return SKS_OK;
+}
+
+extern "C" int sks_batch_get_tuning(const sks_batch* b, sks_tuning_t* t)
+{
+    if (!b || !t) return set_err(SKS_ERR_ARG, "NULL argument");
+    t->warps_per_block = b->NW;
+    t->band_rows = b->HZ;
+    t->zseam = b->ZS;
+    t->register_cap = b->CAP;
+    t->waves = 0;
+    t->blocks = b->grid;
+    t->ms_per_step = 0.f;
+    return SKS_OK;
+}
+
+// Time candidate tunings on the members' own next steps (state restored): each
+// candidate runs `steps` batched step launches once untimed and once timed.
+extern "C" int sks_batch_autotune(sks_batch* b, int32_t steps, sks_tuning_t* best)
+{
+    if (!b) return set_err(SKS_ERR_ARG, "batch is NULL");
+    if (steps < 1) steps = 4;
+    const int n = (int)b->mem.size();
+    if (n == 0) return set_err(SKS_ERR_STATE, "the batch is empty");
+    cudaSetDevice(b->device);
+    for (int i = 0; i < n; i++) {
+        sks_solver* s = b->mem[i];
+        int rc = check_member(b, s, i);
+        if (rc) return rc;
+        if (s->step + 1 + steps > s->m.nst)
+            return set_err(SKS_ERR_STATE, "member %d: autotune needs %d more steps than its run has left", i, steps + 1);
+    }
+    std::vector<Snapshot> snaps(n);
+    int rc = SKS_OK;
+    for (int i = 0; i < n && !rc; i++) rc = snap_take(b->mem[i], snaps[i]);
+    for (int i = 0; i < n && !rc; i++) rc = cudaStreamSynchronize(b->mem[i]->stream) == cudaSuccess ? SKS_OK : SKS_ERR_CUDA;
+    for (int i = 0; i < n && !rc; i++)
+        if (b->mem[i]->step == 0) rc = first_step(b->mem[i]);
+    const sks_tuning_t old = {b->NW, b->HZ, b->ZS, b->CAP, 0, b->grid, 0.f};
+    sks_tuning_t bt = old;
+    bt.ms_per_step = 1e30f;
+    const int hzs[] = {3, 4, 6, 8, 12};
+    for (int nw = 2; nw <= 4 && !rc; nw += 2)
+        for (int zs = 0; zs < 2 && !rc; zs++)
+            for (int cap = 0; cap < 3 && !rc; cap++)
+                for (int hz : hzs) {
+                    sks_tuning_t t = {nw, hz, zs, cap, 0, 0, 0.f};
+                    if ((rc = sks_batch_set_tuning(b, &t))) break;
+                    rc = b->precision == SKS_FP64 ? build_tables<double>(b) : build_tables<float>(b);
+                    if (rc) break;
+                    set_persistent_grid(b);
+                    for (int i = 0; i < n; i++) {
+                        sks_solver* s = b->mem[i];
+                        b->hstate[i] = BatchState{s->step, steps, s->step + steps, 0};
+                    }
+                    cudaMemcpyAsync(b->dstate, b->hstate, sizeof(BatchState) * n, cudaMemcpyHostToDevice, b->stream);
+                    // the chunk's boundary increments, so every launch reads defined values
+                    k_interp_batch<<<dim3(b->chunk + 1, n), 256, 0, b->stream>>>(b->daux, b->dstate, b->dhdr);
+                    if (b->precision == SKS_FP64)
+                        k_line_delta_batch<double><<<dim3(32, n), 256, 0, b->stream>>>(b->daux, b->dstate, b->dhdr);
+                    else
+                        k_line_delta_batch<float><<<dim3(32, n), 256, 0, b->stream>>>(b->daux, b->dstate, b->dhdr);
+                    cudaError_t e = cudaSuccess;
+                    for (int pass = 0; pass < 2 && e == cudaSuccess; pass++) {
+                        if (pass) cudaEventRecord(b->ev[0], b->stream);
+                        for (int j = 0; j < steps && e == cudaSuccess; j++)
+                            e = b->precision == SKS_FP64 ? launch_steps<double>(b, j) : launch_steps<float>(b, j);
+                    }
+                    cudaEventRecord(b->ev[1], b->stream);
+                    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+                    if (e != cudaSuccess) { rc = set_err(SKS_ERR_CUDA, "batch autotune: %s", cudaGetErrorString(e)); break; }
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]);
+                    b->launches += 2 + 2 * steps;
+                    ms /= (float)steps;
+                    if (ms < bt.ms_per_step) bt = {nw, hz, zs, cap, 0, b->grid, ms};
+                }
+    for (int i = 0; i < n; i++) {
+        const int r2 = snap_restore(b->mem[i], snaps[i]);
+        cudaStreamSynchronize(b->mem[i]->stream);
+        snap_free(snaps[i]);
+        if (!rc) rc = r2;
+    }
+    const sks_tuning_t use = rc ? old : bt;
+    const int r3 = sks_batch_set_tuning(b, &use);
+    if (rc) return rc;
+    if (r3) return r3;
+    if (best) *best = bt;
+    return SKS_OK;
+}
+
+extern "C" double sks_batch_last_run_ms(const sks_batch* b) { return b ? b->last_ms : -1.0; }
+
+extern "C" int64_t sks_batch_kernel_launches(const sks_batch* b) { return b ? b->launches : -1; }
+
+extern "C" void sks_batch_destroy(sks_batch* b)
+{
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (sks_solver* s : b->mem) s->batch = nullptr;
+    b->mem.clear();
+    free_graph(b);
+    free_tables(b);
+    if (b->ev[0]) cudaEventDestroy(b->ev[0]);
+    if (b->ev[1]) cudaEventDestroy(b->ev[1]);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}

@@ -1,0 +1,21 @@
+// Batch step kernel variants of the FP64 form.
+#include "sks_batch_inst.cuh"
+
+namespace sks {
+
+int batch_occupancy_f64(const StepVariant& v, bool aniso)
+{
+    BatchOcc<double, false> o;
+    return visit_variant(v, aniso, o);
+}
+
+cudaError_t launch_batch_f64(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const BatchMember<double>* mem,
+                             const BatchState* state, const int4* items, const BatchHeader* hdr, int j,
+                             const Coef<double>& k)
+{
+    BatchLaunch<double, false> l{blocks, st, mem, state, items, hdr, j, k};
+    visit_variant(v, aniso, l);
+    return cudaGetLastError();
+}
+
+}  // namespace sks

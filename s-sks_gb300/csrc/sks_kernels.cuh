@@ -42,14 +42,18 @@ constexpr int TEX = 6;        // elements per warp tile in x
 constexpr int TW = TEX * N;   // grid columns per warp tile
 constexpr int MAT_STRIDE = 16;
 
+// GLL tables of degree N, the same for every mesh.  The element size drops out
+// of the internal force: d/dx = (2/eh) d/dxi and the quadrature carries
+// (eh/2)^2, so K = sum C (l' u) l' w w with unscaled derivatives.  The tables
+// hold l'_i(xi_j) and l'_i(xi_j) w_j without the 2/eh and eh/2 factors, and
+// one kernel argument serves every instance of a batch.
 template <typename T>
 struct Coef {
-    T D[NP * NP];    // D[j*NP+i]  = l'_i(xi_j) * 2/eh         (dlagP_JeI)
-    T DWs[NP * NP];  // DWs[j*NP+i] = l'_i(xi_j) * w_j * eh/2  (dlagP_Gllw * Uni_JeI * Uni_Je)
+    T D[NP * NP];    // D[j*NP+i]  = l'_i(xi_j)
+    T DWs[NP * NP];  // DWs[j*NP+i] = l'_i(xi_j) * w_j
     T w[NP];         // GLL weights
     T winv[NP];      // 1/w_a: inverse lumped-mass weight of a point inside an element edge
     T winv2;         // 1/(2 w_0): a point shared by two elements along x (or z)
-    T dt2_Je;        // sdt^2 / Je   (M^-1 dt^2 = dt2_Je / (rho Wx Wz))
 };
 
 template <typename T>
@@ -59,6 +63,7 @@ struct Geo {
     const int4* items;            // or per CTA (column, band, first row, end row): balanced bands
     int nbl;                      // GRT interface line: row nbl (ix >= nbl), column nbl (iz > nbl)
     int64_t np;                   // nx*nz
+    T dt2_Je;                     // sdt^2 / Je   (M^-1 dt^2 = dt2_Je / (rho Wx Wz))
 };
 
 template <typename T>
@@ -196,7 +201,6 @@ struct Aux {
 template <typename T, bool LF>
 __device__ __forceinline__ void load_aux(const Field<T>& F, int64_t np, int64_t g, Aux<T, LF>& x)
 {
-#pragma unroll
     if constexpr (!LF) {
         load_u<T>(F.un, (int)np, (int)g, x.a);
     } else {
@@ -230,7 +234,7 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
     T un[3], dn[3], cn[3];
     if (!LF) {
         if (!edge) {
-            const T mdt2 = k.dt2_Je * rinv * wxi * wzi;
+            const T mdt2 = G.dt2_Je * rinv * wxi * wzi;
 #pragma unroll
             for (int c = 0; c < 3; c++) un[c] = (-mdt2 * K[c] + (T)2 * u[c]) - x.a[c];
         } else {
@@ -240,7 +244,7 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
         }
     } else {
         if (!edge) {
-            const T mdt2 = k.dt2_Je * rinv * wxi * wzi;
+            const T mdt2 = G.dt2_Je * rinv * wxi * wzi;
 #pragma unroll
             for (int c = 0; c < 3; c++) dn[c] = fma(-mdt2, K[c], x.a[c]);
         } else {
@@ -314,23 +318,22 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
 template <typename T>
 constexpr int cap_warps(int cap) { return cap == 0 ? 0 : (sizeof(T) == 4 ? (cap == 1 ? 16 : 20) : (cap == 1 ? 8 : 12)); }
 
-template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP>
-__global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
-k_step(Field<T> F, Geo<T> G, Coef<T> k)
+// shared memory of one CTA tile
+template <typename T, int NW>
+struct TileShared {
+    T xch[2][NW][N][3];     // force of a warp's last column, for the next warp
+    T xtop[NW][3];          // the same for the band's top row
+    int second_arrival;
+};
+
+// One CTA tile: element column cx (S = 6*NW-1 owned elements), band cz of
+// element rows [ez0, ez1).
+template <typename T, bool ANISO, bool LF, int NW, bool ZS>
+__device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, const Coef<T>& k, int cx, int cz,
+                                          int ez0, int ez1, TileShared<T, NW>& sh)
 {
-    __shared__ T xch[2][NW][N][3];
-    __shared__ T xtop[NW][3];
-    __shared__ int second_arrival;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int cx, cz, ez0, ez1;
-    if (G.items) {
-        const int4 it = G.items[blockIdx.x];
-        cx = it.x; cz = it.y; ez0 = it.z; ez1 = it.w;
-    } else {
-        cx = blockIdx.x % G.ncx; cz = blockIdx.x / G.ncx;
-        ez0 = cz * G.HZ; ez1 = min(ez0 + G.HZ, G.nez);
-    }
     constexpr int S = TEX * NW - 1;                // owned elements per CTA
     const int e = lane / NP, al = lane - e * NP;   // lanes 30,31: e = 6
     const int q = TEX * w + e;                     // element within the CTA
@@ -456,7 +459,7 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 #pragma unroll
                 for (int b = 0; b < N; b++)
 #pragma unroll
-                    for (int c = 0; c < 3; c++) xch[par][w][b][c] = kk[b][c];
+                    for (int c = 0; c < 3; c++) sh.xch[par][w][b][c] = kk[b][c];
             }
             __syncthreads();
             const bool seam_row0 = ZS && ez == ez0 && ez0 > 0;
@@ -466,7 +469,7 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
                     T left = __shfl_up_sync(FULL, kk[b][c], 1);
-                    if (e == 0) left = xch[par][w > 0 ? w - 1 : 0][b][c];
+                    if (e == 0) left = sh.xch[par][w > 0 ? w - 1 : 0][b][c];
                     lft[c] = add_left ? left : (T)0;
                     kt[c] = add_left ? left + kk[b][c] : kk[b][c];
                 }
@@ -487,9 +490,9 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
             if (seam_row0) {
                 __threadfence();
                 __syncthreads();
-                if (threadIdx.x == 0) second_arrival = atomicAdd(F.seam_cnt + cz * G.ncx + cx, 1) & 1;
+                if (threadIdx.x == 0) sh.second_arrival = atomicAdd(F.seam_cnt + cz * G.ncx + cx, 1) & 1;
                 __syncthreads();
-                if (second_arrival) {
+                if (sh.second_arrival) {
                     __threadfence();
                     if (own_x) {
                         // (left carry + left row) + (own carry + own row), as inside a band
@@ -510,14 +513,14 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
     if (ez1 == G.nez || ZS) {
         if (lane == 29) {
 #pragma unroll
-            for (int c = 0; c < 3; c++) xtop[w][c] = kc[c];
+            for (int c = 0; c < 3; c++) sh.xtop[w][c] = kc[c];
         }
         __syncthreads();
         T kt[3], lft[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             T left = __shfl_up_sync(FULL, kc[c], 1);
-            if (e == 0) left = xtop[w > 0 ? w - 1 : 0][c];
+            if (e == 0) left = sh.xtop[w > 0 ? w - 1 : 0][c];
             lft[c] = add_left ? left : (T)0;
             kt[c] = add_left ? left + kc[c] : kc[c];
         }
@@ -536,9 +539,9 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
             }
             __threadfence();
             __syncthreads();
-            if (threadIdx.x == 0) second_arrival = atomicAdd(F.seam_cnt + (cz + 1) * G.ncx + cx, 1) & 1;
+            if (threadIdx.x == 0) sh.second_arrival = atomicAdd(F.seam_cnt + (cz + 1) * G.ncx + cx, 1) & 1;
             __syncthreads();
-            if (second_arrival) {
+            if (sh.second_arrival) {
                 __threadfence();
                 if (own_x) {
                     const T* hi = F.seam_hi + ((size_t)(cz + 1) * nx + ix) * 6;
@@ -555,6 +558,102 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
     }
 }
 
+// The step of one mesh: CTA b takes tile b of the band table, or of the
+// regular ncx x ncz grid.
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP>
+__global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
+k_step(const __grid_constant__ Field<T> F, const __grid_constant__ Geo<T> G, const __grid_constant__ Coef<T> k)
+{
+    __shared__ TileShared<T, NW> sh;
+    int cx, cz, ez0, ez1;
+    if (G.items) {
+        const int4 it = G.items[blockIdx.x];
+        cx = it.x; cz = it.y; ez0 = it.z; ez1 = it.w;
+    } else {
+        cx = blockIdx.x % G.ncx; cz = blockIdx.x / G.ncx;
+        ez0 = cz * G.HZ; ez1 = min(ez0 + G.HZ, G.nez);
+    }
+    step_tile<T, ANISO, LF, NW, ZS>(F, G, k, cx, cz, ez0, ez1, sh);
+}
+
+// ---------------------------------------------------------------------------
+// Batches: many meshes (sizes, materials, time steps of their own) advance one
+// step each in one launch.  Per member, a device descriptor holds its Field
+// and Geo; the per-launch parts of the Field (which buffer holds u^n, the
+// seismogram row, the injection row) follow from the member's step, which the
+// device keeps in BatchState and advances after each chunk of steps, so one
+// captured graph runs every chunk and survives members joining and leaving.
+template <typename T>
+struct BatchMember {
+    Field<T> F;            // uc, un, dline, inject_next, seis_row are set per launch
+    Geo<T> G;
+    T* U[2];               // displacement buffers; step it reads U[(it-1)&1], writes U[it&1]
+    const T* dl;           // line increments of the chunk, [chunk+1][nline][3]
+    float* seis;           // whole-run seismograms, [nst][3][ntrace]
+    int nt_sem;            // steps that inject
+    int nline;
+};
+
+// per member: step at the chunk's start, steps in this chunk, step to stop at
+struct BatchState {
+    int it0, n, target, pad;
+};
+
+// header of a batch's device tables
+struct BatchHeader {
+    int nitems;            // tiles in the item table
+    int nmem;              // members
+    int chunk;             // steps per chunk
+    int pad;
+};
+
+// Persistent CTAs stride over the batch's tiles (item = member, cx | cz<<16,
+// ez0, ez1); launch j of a chunk advances each member with j < n by one step.
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP>
+__global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
+k_step_batch(const BatchMember<T>* __restrict__ mem, const BatchState* __restrict__ state,
+             const int4* __restrict__ items, const BatchHeader* __restrict__ hdr, int j,
+             const __grid_constant__ Coef<T> k)
+{
+    __shared__ TileShared<T, NW> sh;
+    __shared__ __align__(16) Field<T> sF;
+    __shared__ __align__(16) Geo<T> sG;
+    __shared__ int s_go;
+    const int nitems = hdr->nitems;
+    int cur = -1;
+    for (int i = blockIdx.x; i < nitems; i += gridDim.x) {
+        const int4 it = items[i];
+        if (it.x != cur) {
+            // descriptor of a new member: copy it, then set the per-launch fields
+            cur = it.x;
+            const BatchMember<T>* M = mem + cur;
+            constexpr int FW = (int)(sizeof(Field<T>) / 4), GW = (int)(sizeof(Geo<T>) / 4);
+            for (int q = threadIdx.x; q < FW + GW; q += blockDim.x) {
+                if (q < FW) reinterpret_cast<int*>(&sF)[q] = __ldg(reinterpret_cast<const int*>(&M->F) + q);
+                else reinterpret_cast<int*>(&sG)[q - FW] = __ldg(reinterpret_cast<const int*>(&M->G) + q - FW);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                const BatchState st = state[cur];
+                const int step = st.it0 + j;
+                const int go = j < st.n && step >= 1;
+                s_go = go;
+                if (go) {
+                    sF.uc = M->U[(step - 1) & 1];
+                    sF.un = M->U[step & 1];
+                    sF.dline = M->dl + (size_t)j * M->nline * 3;
+                    sF.inject_next = step + 1 < M->nt_sem ? 1 : 0;
+                    sF.seis_row = M->seis + (size_t)step * 3 * sF.ntrace;
+                }
+            }
+            __syncthreads();
+        }
+        if (s_go)
+            step_tile<T, ANISO, LF, NW, ZS>(sF, sG, k, it.y & 0xffff, it.y >> 16, it.z, it.w, sh);
+        __syncthreads();
+    }
+}
+
 }  // namespace sks
 
 namespace sks {
@@ -563,6 +662,14 @@ cudaError_t launch_step_f32(const StepVariant& v, bool aniso, int blocks, cudaSt
                             const Field<float>& F, const Geo<float>& G, const Coef<float>& k);
 cudaError_t launch_step_f64(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
                             const Field<double>& F, const Geo<double>& G, const Coef<double>& k);
+cudaError_t launch_batch_f32(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const BatchMember<float>* mem,
+                             const BatchState* state, const int4* items, const BatchHeader* hdr, int j,
+                             const Coef<float>& k);
+cudaError_t launch_batch_f64(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const BatchMember<double>* mem,
+                             const BatchState* state, const int4* items, const BatchHeader* hdr, int j,
+                             const Coef<double>& k);
+int batch_occupancy_f32(const StepVariant& v, bool aniso);
+int batch_occupancy_f64(const StepVariant& v, bool aniso);
 // resident CTAs per SM of a variant (cudaOccupancyMaxActiveBlocksPerMultiprocessor)
 int step_occupancy_f32(const StepVariant& v, bool aniso);
 int step_occupancy_f64(const StepVariant& v, bool aniso);

@@ -1,9 +1,7 @@
 // C ABI of the GB300 SEM time-stepping library (include/sks.h): device state,
 // step scheduling, and the entry points that replace main() and the time loop
 // of semsyn/src/sem2d_psvsh.c.
-#include "sks.h"
-#include "sks_model.h"
-#include "sks_kernels.cuh"
+#include "sks_internal.h"
 #include "sks_aux_kernels.cuh"
 
 #include <cuda_runtime.h>
@@ -15,10 +13,11 @@
 #include <algorithm>
 
 using namespace sks;
+using namespace sksi;
 
 static thread_local char g_err[1024];
 
-static int set_err(int code, const char* fmt, ...)
+int sks_err(int code, const char* fmt, ...)
 {
     va_list ap;
     va_start(ap, fmt);
@@ -26,14 +25,6 @@ static int set_err(int code, const char* fmt, ...)
     va_end(ap);
     return code;
 }
-
-#define CK(call)                                                                              \
-    do {                                                                                      \
-        cudaError_t e_ = (call);                                                              \
-        if (e_ != cudaSuccess)                                                                \
-            return set_err(SKS_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
-                           __FILE__, __LINE__);                                               \
-    } while (0)
 
 extern "C" const char* sks_last_error(void) { return g_err; }
 
@@ -43,65 +34,6 @@ extern "C" __attribute__((visibility("hidden"))) int sks_internal_set_error(int 
     if (e != cudaSuccess) return set_err(code, "%s: %s", msg, cudaGetErrorString(e));
     return set_err(code, "%s", msg);
 }
-
-struct sks_solver {
-    sks_model m;
-    int precision, device;
-    int step;                  // next step to take
-    int64_t launches;
-    cudaStream_t stream;
-    // geometry: CTA grid of the step kernel (tunable)
-    int NW, ncx, ncz, HZ, nblocks, ZS, CAP, WAVES;
-    int4* items;               // balanced band table (grow-only)
-    size_t items_n;
-    void* seam_lo;             // band-seam partial forces (grow-only)
-    void* seam_hi;
-    int* seam_cnt;
-    size_t seam_bytes, seam_cnt_n;
-    int sms;
-    int nbl;
-    // device buffers
-    void* U[2];                // displacement buffers, [3][np] each
-    void* Dv;                  // FP32 form: increment d
-    void* Cc;                  // FP32 form: Kahan compensation
-    uint16_t* mid;
-    void* mat;                 // [nmat][16] in the form's type
-    void* stc;                 // Stacey coefficients
-    int64_t* rec_off;          // per trace (step-0 recording)
-    uint32_t* recbits;         // receiver bitmap over points
-    int64_t* rec_sorted;       // receiver offsets, sorted
-    int32_t* rec_idx;          // trace index of each sorted offset
-    int nrec_in;               // receivers inside the mesh (offset < np)
-    int rec_iz0, rec_iz1;      // rows holding them (empty range when none)
-    float* seis;               // [chunk][3][ntrace], the slot in use
-    float* seisbuf[2];         // two slots: one filled by kernels while the other is copied out
-    cudaStream_t copy_stream;
-    cudaEvent_t chunk_done[2], copy_done[2];
-    bool slot_busy[2];
-    double* G;                 // [(chunk+2)][mtotal+shtotal]
-    void* Dl;                  // [chunk+1][nline][3] line increments in the form's type
-    float* rec_psv;            // boundary records
-    float* rec_sh;
-    int32_t* tap_psv;
-    int32_t* tap_sh;
-    double* w_psv;
-    double* w_sh;
-    int nrec_psv_loaded, nrec_sh_loaded;
-    int cur;                   // index of the buffer holding u^n
-    int g_last;                // row of G holding the last interpolated step
-    int chunk;
-    int64_t device_bytes;
-    bool boundary_ready;
-    // instrumentation: whole-run events, per-kernel-class event pairs
-    cudaEvent_t run_ev[2];
-    double last_run_ms;
-    int timing;
-    std::vector<cudaEvent_t> kev;     // pool of event pairs for one chunk
-    std::vector<int> kcls;            // class of each recorded pair
-    int kused;
-    double kms[SKS_KERNEL_CLASSES];
-    int64_t kcount[SKS_KERNEL_CLASSES];
-};
 
 struct sks_setup {
     sks_model m;
@@ -186,7 +118,7 @@ extern "C" void sks_setup_close(sks_setup* su)
     delete su;
 }
 
-namespace {
+namespace sksi {
 
 template <typename T>
 int dmalloc(sks_solver* s, T** p, size_t n)
@@ -203,7 +135,7 @@ void free_device(sks_solver* s)
 {
     void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc,
                   s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seisbuf[0], s->seisbuf[1], s->G, s->Dl, s->rec_psv, s->rec_sh,
-                  s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt, s->items};
+                  s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt, s->items, s->seis_full};
     for (void* p : ps)
         if (p) cudaFree(p);
     s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = nullptr;
@@ -212,6 +144,7 @@ void free_device(sks_solver* s)
     s->rec_psv = s->rec_sh = nullptr; s->tap_psv = s->tap_sh = nullptr; s->w_psv = s->w_sh = nullptr;
     s->seam_lo = s->seam_hi = nullptr; s->seam_cnt = nullptr; s->seam_bytes = 0; s->seam_cnt_n = 0;
     s->items = nullptr; s->items_n = 0;
+    s->seis_full = nullptr;
 }
 
 // per-kernel-class timing: an event pair around each launch when enabled
@@ -316,58 +249,6 @@ int upload_tables(sks_solver* s)
         s->Cc = nullptr;
     }
     return SKS_OK;
-}
-
-template <typename T>
-Coef<T> make_coef(const sks_model& m)
-{
-    Coef<T> k;
-    for (int j = 0; j < NP; j++)
-        for (int i = 0; i < NP; i++) {
-            k.D[j * NP + i] = (T)(m.dlagP[j * NP + i] * m.JeI);
-            k.DWs[j * NP + i] = (T)(m.dlagP[j * NP + i] * m.gllw[j] * (m.JeI * m.Je));
-        }
-    for (int i = 0; i < NP; i++) { k.w[i] = (T)m.gllw[i]; k.winv[i] = (T)(1.0 / m.gllw[i]); }
-    k.winv2 = (T)(1.0 / (2.0 * m.gllw[0]));
-    k.dt2_Je = (T)(m.sdt * m.sdt / m.Je);
-    return k;
-}
-
-template <typename T>
-Field<T> make_field(sks_solver* s)
-{
-    Field<T> F;
-    memset(&F, 0, sizeof F);
-    F.uc = (const T*)s->U[s->cur];
-    F.un = (T*)s->U[1 - s->cur];
-    F.dv = (T*)s->Dv;
-    F.cc = (T*)s->Cc;
-    F.mid = s->mid;
-    F.mat = (const T*)s->mat;
-    F.stc = (const T*)s->stc;
-    F.recbits = s->recbits;
-    F.rec_off = s->rec_sorted;
-    F.rec_idx = s->rec_idx;
-    F.nrec = s->nrec_in;
-    F.ntrace = s->m.ntrace;
-    F.rec_iz0 = s->rec_iz0;
-    F.rec_iz1 = s->rec_iz1;
-    F.seam_lo = (T*)s->seam_lo;
-    F.seam_hi = (T*)s->seam_hi;
-    F.seam_cnt = s->seam_cnt;
-    return F;
-}
-
-template <typename T>
-Geo<T> make_geo(const sks_solver* s)
-{
-    Geo<T> G;
-    G.nex = s->m.nex; G.nez = s->m.nez; G.nx = s->m.nx; G.nz = s->m.nz;
-    G.ncx = s->ncx; G.ncz = s->ncz; G.HZ = s->HZ; G.nblocks = s->nblocks;
-    G.items = s->WAVES > 0 ? s->items : nullptr;
-    G.nbl = s->nbl;
-    G.np = (int64_t)s->m.nx * s->m.nz;
-    return G;
 }
 
 // CTA grid for a tuning: NW warps (6*NW-1 owned elements) by bands of rows.
@@ -553,7 +434,7 @@ int run_chunk(sks_solver* s, int it0, int n)
     return SKS_OK;
 }
 
-}  // namespace
+}  // namespace sksi
 
 extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solver** out)
 {
@@ -837,6 +718,7 @@ extern "C" void sks_destroy(sks_solver* s)
 {
     if (!s) return;
     cudaSetDevice(s->device);
+    if (s->batch) batch_detach(s);
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_device(s);
     for (cudaEvent_t e : s->kev) cudaEventDestroy(e);
@@ -881,6 +763,7 @@ extern "C" int sks_set_tuning(sks_solver* s, const sks_tuning_t* t)
         return set_err(SKS_ERR_ARG, "register_cap=%d: 0, 1 or 2", t->register_cap);
     if (t->waves == 0 && t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
     if (t->waves < 0 || t->waves > 64) return set_err(SKS_ERR_ARG, "waves=%d: 0..64", t->waves);
+    if (s->batch) return set_err(SKS_ERR_STATE, "the solver is a member of a batch: tune the batch");
     return set_grid(s, t->warps_per_block, t->band_rows, t->zseam ? 1 : 0, t->register_cap, t->waves);
 }
 
@@ -897,14 +780,7 @@ extern "C" int sks_get_tuning(const sks_solver* s, sks_tuning_t* t)
     return SKS_OK;
 }
 
-namespace {
-
-struct Snapshot {
-    std::vector<void*> dev;
-    std::vector<size_t> bytes;
-    std::vector<void*> src;
-    int step, cur, g_last;
-};
+namespace sksi {
 
 int snap_take(sks_solver* s, Snapshot& S)
 {
@@ -937,13 +813,22 @@ int snap_restore(sks_solver* s, const Snapshot& S)
     return SKS_OK;
 }
 
-}  // namespace
+void snap_free(Snapshot& S)
+{
+    for (void* p : S.dev) cudaFree(p);
+    S.dev.clear();
+    S.bytes.clear();
+    S.src.clear();
+}
+
+}  // namespace sksi
 
 extern "C" int sks_autotune(sks_solver* s, int32_t steps, sks_tuning_t* best)
 {
     if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
     const sks_model& m = s->m;
     if (steps < 1) steps = 8;
+    if (s->batch) return set_err(SKS_ERR_STATE, "the solver is a member of a batch: tune the batch");
     if (s->step < m.nt_sem && !s->boundary_ready) return set_err(SKS_ERR_STATE, "boundary records not set");
     if (s->step + 1 + steps > m.nst) return set_err(SKS_ERR_STATE, "autotune needs %d more steps than the run has left", steps + 1);
     cudaSetDevice(s->device);

@@ -32,6 +32,9 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_kernel_launches", "sks_last_run_ms", "sks_enable_kernel_timing", "sks_kernel_timing",
            "sks_set_tuning", "sks_get_tuning", "sks_autotune", "sks_line_increments",
            "sks_line_increments_noalloc",
+           "sks_batch_create", "sks_batch_add", "sks_batch_remove", "sks_batch_size", "sks_batch_run",
+           "sks_batch_set_tuning", "sks_batch_get_tuning", "sks_batch_autotune", "sks_batch_last_run_ms",
+           "sks_batch_kernel_launches", "sks_batch_destroy",
            "sks_destroy", "sks_last_error"]
 
 KERNEL_CLASSES = ["element", "seam", "inject", "record", "interp"]
@@ -103,6 +106,21 @@ def lib() -> C.CDLL:
                                                   C.c_int32, vp, vp]
         L.sks_destroy.argtypes = [vp]
         L.sks_destroy.restype = None
+        fpp = C.POINTER(C.POINTER(C.c_float))
+        L.sks_batch_create.argtypes = [C.c_int, C.c_int, C.POINTER(vp)]
+        L.sks_batch_add.argtypes = [vp, vp]
+        L.sks_batch_remove.argtypes = [vp, vp]
+        L.sks_batch_size.argtypes = [vp]
+        L.sks_batch_run.argtypes = [vp, C.c_int32, fpp, fpp, fpp]
+        L.sks_batch_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+        L.sks_batch_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
+        L.sks_batch_autotune.argtypes = [vp, C.c_int32, C.POINTER(Tuning)]
+        L.sks_batch_last_run_ms.argtypes = [vp]
+        L.sks_batch_last_run_ms.restype = C.c_double
+        L.sks_batch_kernel_launches.argtypes = [vp]
+        L.sks_batch_kernel_launches.restype = C.c_int64
+        L.sks_batch_destroy.argtypes = [vp]
+        L.sks_batch_destroy.restype = None
         L.sks_last_error.restype = C.c_char_p
         _lib = L
     return _lib
@@ -186,12 +204,17 @@ class Setup:
 
 
 class Solver:
-    """Device solver of one par file (sks_open_par)."""
+    """Device solver of one par file (sks_open_par), or of an open Setup
+    (sks_open_setup, which takes the set-up over)."""
 
-    def __init__(self, words, precision: int = FP64, device: int = 0):
+    def __init__(self, words=None, precision: int = FP64, device: int = 0, setup: "Setup | None" = None):
         self.h = C.c_void_p()
-        n, arr = _argv(words)
-        _check(lib().sks_open_par(n, arr, precision, device, C.byref(self.h)))
+        if setup is not None:
+            h, setup.h = setup.h, C.c_void_p()
+            _check(lib().sks_open_setup(h, precision, device, C.byref(self.h)))
+        else:
+            n, arr = _argv(words)
+            _check(lib().sks_open_par(n, arr, precision, device, C.byref(self.h)))
 
     def info(self) -> dict:
         i = Info()
@@ -268,6 +291,79 @@ class Solver:
         if self.h:
             lib().sks_destroy(self.h)
             self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Solvers of one form advanced together (sks_batch_*)."""
+
+    def __init__(self, precision: int = FP32C, device: int = 0):
+        self.h = C.c_void_p()
+        _check(lib().sks_batch_create(precision, device, C.byref(self.h)))
+        self.members: list[Solver] = []
+
+    def add(self, s: Solver):
+        _check(lib().sks_batch_add(self.h, s.h))
+        self.members.append(s)
+
+    def remove(self, s: Solver):
+        _check(lib().sks_batch_remove(self.h, s.h))
+        self.members.remove(s)
+
+    def __len__(self) -> int:
+        return _check(lib().sks_batch_size(self.h))
+
+    def run(self, nsteps: int, want: bool = True):
+        """Advance every member; returns per member (u, v, w) of the rows it took."""
+        infos = [m.info() for m in self.members]
+        n = len(self.members)
+        fpp = C.POINTER(C.c_float) * max(1, n)
+        outs, arrs = [], [fpp(), fpp(), fpp()]
+        for i, inf in enumerate(infos):
+            rows = max(0, min(inf["nst"], inf["step"] + nsteps) - inf["step"])
+            o = tuple(np.zeros((rows, max(inf["ntrace"], 0)), np.float32) for _ in range(3))
+            outs.append(o)
+            for c in range(3):
+                arrs[c][i] = _f32(o[c]) if want and o[c].size else None
+        _check(lib().sks_batch_run(self.h, nsteps, arrs[0], arrs[1], arrs[2]))
+        return outs
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        _check(lib().sks_batch_get_tuning(self.h, C.byref(t)))
+        return t.asdict()
+
+    def set_tuning(self, warps_per_block: int, band_rows: int, zseam: int = 0, register_cap: int = 1):
+        t = Tuning(warps_per_block, band_rows, zseam, register_cap, 0, 0, 0.0)
+        _check(lib().sks_batch_set_tuning(self.h, C.byref(t)))
+
+    def autotune(self, steps: int = 4) -> dict:
+        t = Tuning()
+        _check(lib().sks_batch_autotune(self.h, steps, C.byref(t)))
+        return t.asdict()
+
+    def last_run_ms(self) -> float:
+        return lib().sks_batch_last_run_ms(self.h)
+
+    def launches(self) -> int:
+        return lib().sks_batch_kernel_launches(self.h)
+
+    def close(self):
+        if self.h:
+            lib().sks_batch_destroy(self.h)
+            self.h = C.c_void_p()
+        self.members = []
 
     def __enter__(self):
         return self

@@ -42,13 +42,15 @@ def _stale(target: str, deps: list[str]) -> bool:
 def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
-    hdrs = [os.path.join(INC, "sks.h"), os.path.join(CSRC, "sks_model.h"), os.path.join(CSRC, "sks_kernels.cuh"),
-            os.path.join(CSRC, "sks_aux_kernels.cuh")]
+    hdrs = [os.path.join(INC, "sks.h")] + [os.path.join(CSRC, h) for h in (
+        "sks_model.h", "sks_internal.h", "sks_kernels.cuh", "sks_aux_kernels.cuh", "sks_variants.cuh",
+        "sks_step_inst.cuh", "sks_batch_inst.cuh")]
     units = [
         (os.path.join(CSRC, "sks_model.c"), os.path.join(OUT, "sks_model.o"),
          ["gcc", "-O2", "-std=gnu11", "-fPIC", "-Wall", "-I" + INC, "-c"]),
     ]
-    for cu in ("sks_solver", "sks_step_f32", "sks_step_f64", "sks_noalloc"):
+    for cu in ("sks_solver", "sks_batch", "sks_step_f32", "sks_step_f64", "sks_batch_f32", "sks_batch_f64",
+               "sks_noalloc"):
         units.append((os.path.join(CSRC, cu + ".cu"), os.path.join(OUT, cu + ".o"),
                       [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC,
                        "-c"]))
