@@ -239,6 +239,95 @@ def run_e2e(d: str, precision: int, steps: int, warmup: int, gpu: int, tuning=No
 
 
 # ---------------------------------------------------------------- CPU side
+def _open_instances(inst, precision: int, gpu: int, base: str) -> list:
+    """Solvers of the batched workload's instances; boundary records generated on the device."""
+    import sks
+    import synth
+    sol = []
+    for k, i in enumerate(inst):
+        d = os.path.join(base, f"i{k:02d}")
+        synth.write_case(i["case"], d)
+        cwd = os.getcwd()
+        os.chdir(d)
+        try:
+            s = sks.Solver(["par=run.par"], precision=precision, device=gpu)
+        finally:
+            os.chdir(cwd)
+        s.set_boundary_plane_wave(i["vs_bottom"], i["p"], i["f0"], 1.0, 0.0)
+        sol.append(s)
+    return sol
+
+
+def run_batch(gpu: int, steps: int, warmup: int, fp64_steps: int = 8) -> dict:
+    """The batched workload (64 seeded uneven instances, FP32C): autotuned
+    batch, a timed window with every member active, then all 64 full solves
+    from step 0 to the end with the seismograms read back, wall-clock timed.
+    An FP64 batch of the same instances is timed over a short window."""
+    import sks
+    import synth
+    inst = synth.config_batch()
+    base = tempfile.mkdtemp(prefix="sks_batch_")
+    out = {}
+    try:
+        t0 = time.perf_counter()
+        sol = _open_instances(inst, sks.FP32C, gpu, base)
+        open_s = time.perf_counter() - t0
+        infos = [s.info() for s in sol]
+        pts = [i["nx"] * i["nz"] for i in infos]
+        work = sum(p * i["nst"] for p, i in zip(pts, infos))
+        b = sks.Batch(sks.FP32C, gpu)
+        for s in sol:
+            b.add(s)
+        b.run(warmup, want=False)
+        tun = b.autotune(4)
+        k = max(1, min(steps, min(i["nst"] for i in infos) - warmup - 8))
+        l0 = b.launches()
+        b.run(k, want=False)
+        ms = b.last_run_ms()
+        launches = b.launches() - l0
+        rate = sum(pts) * k / (ms / 1e3)
+        # the full solves, from step 0, seismograms into host arrays
+        for s in sol:
+            s.reset()
+        t0 = time.perf_counter()
+        res = b.run(10 ** 7, want=True)
+        wall = time.perf_counter() - t0
+        full_dev_ms = b.last_run_ms()
+        assert all(r[0].shape[0] == i["nst"] for r, i in zip(res, infos))
+        finite = all(np.isfinite(r[c]).all() for r in res for c in range(3))
+        b.close()
+        for s in sol:
+            s.close()
+        mem = sum(i["device_bytes"] for i in infos)
+        out["fp32c"] = {"updates_per_s": rate, "ms_per_batch_step": ms / k, "timed_steps": k,
+                        "launches_in_window": launches, "tuning": tun,
+                        "full_solves": {"solves": len(sol), "wall_s": wall, "device_s": full_dev_ms / 1e3,
+                                        "updates_per_s": work / wall, "solves_per_hour": len(sol) * 3600.0 / wall,
+                                        "seismograms_finite": finite}}
+        # FP64: same instances, short timed window
+        sol = _open_instances(inst, sks.FP64, gpu, base)
+        b = sks.Batch(sks.FP64, gpu)
+        for s in sol:
+            b.add(s)
+        b.set_tuning(4, 8, 1, 0)
+        b.run(3, want=False)
+        b.run(fp64_steps, want=False)
+        ms64 = b.last_run_ms()
+        b.close()
+        for s in sol:
+            s.close()
+        rate64 = sum(pts) * fp64_steps / (ms64 / 1e3)
+        out["fp64"] = {"updates_per_s": rate64, "ms_per_batch_step": ms64 / fp64_steps, "timed_steps": fp64_steps,
+                       "solves_per_hour_at_this_rate": len(inst) * 3600.0 / (work / rate64),
+                       "tuning": {"warps_per_block": 4, "band_rows": 8, "zseam": 1, "register_cap": 0}}
+        out.update({"instances": len(inst), "points_per_step": sum(pts), "updates_per_full_batch": work,
+                    "steps_min_max": [min(i["nst"] for i in infos), max(i["nst"] for i in infos)],
+                    "open_s": open_s, "fp32c_device_bytes": mem})
+    finally:
+        shutil.rmtree(base, ignore_errors=True)
+    return out
+
+
 def _cpu_worker(args):
     d, nsteps, fp64 = args
     sys.path.insert(0, ROOT)
@@ -301,6 +390,8 @@ def main() -> None:
                     help="only the device-resident step loop of one form (profiling)")
     ap.add_argument("--form", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--tuning", default="", help="W,B,Z,C[,V]: warps per CTA, band rows, band seams, register cap, waves")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-instance workload")
+    ap.add_argument("--batch-only", action="store_true", help="only the batched workload (one JSON object)")
     a = ap.parse_args()
     a.warmup = max(3, a.warmup)
     dist, rank, world, local = _dist()
@@ -345,6 +436,9 @@ def main() -> None:
             shutil.rmtree(d, ignore_errors=True)
         print(json.dumps({"kernel_only": a.form, **r}))
         return
+    if a.batch_only:
+        print(json.dumps({"batch": run_batch(gpu, min(a.steps, 200), a.warmup)}))
+        return
     d = tempfile.mkdtemp(prefix="sks_bench_")
     try:
         nst = a.warmup + a.steps + 8
@@ -366,6 +460,9 @@ def main() -> None:
             cpu = cpu_rate(d, a.cpu_steps, 1)
     finally:
         shutil.rmtree(d, ignore_errors=True)
+    batch = None
+    if not a.no_batch:
+        batch = run_batch(gpu, min(a.steps, 200), a.warmup)
     if rank != 0:
         return
     npts = r32["points"]
@@ -413,6 +510,16 @@ def main() -> None:
         "kernel_ms": {k: v[0] for k, v in r32["kernels"].items()},
         "tuning": {"fp32c": r32["tuning"], "fp64": r64["tuning"]},
     }
+    if batch:
+        pb = batch["points_per_step"] * BYTES_PER_POINT["fp32c"] / (batch["fp32c"]["ms_per_batch_step"] / 1e3) / 1e9
+        batch["workload"] = ("64 seeded instances: nex U{200..1000}, nez U{100..400}, element 1-2 km, GLL degree 4, "
+                             "p U[0.038,0.052], anisotropy U[0,6]%, azimuth U[0,180), tilt U[0,30), Ricker "
+                             "U[0.2,0.5] Hz, dt = 0.4 h_min/vp_max, 60 s simulated, SV plane wave generated on the device")
+        batch["fp32c"]["roofline"] = {"achieved": pb, "peak": peak, "unit": "GB/s", "frac": pb / peak,
+                                      "bytes_per_point": BYTES_PER_POINT["fp32c"]}
+        batch["solves_per_hour_ratio_fp32c_full_over_fp64"] = (batch["fp32c"]["full_solves"]["solves_per_hour"] /
+                                                                batch["fp64"]["solves_per_hour_at_this_rate"])
+        line["batch"] = batch
     if cpu:
         line["cpu_baseline"] = {"value": cpu["value"], "unit": "GLL-pt updates/s", "cores": 1, "kind": "port",
                                 "sample": f"{a.cpu_steps} time steps of the same mesh, one thread, oracle float "

@@ -85,6 +85,20 @@ int sks_load_boundary_files(sks_solver *s);
 int sks_set_boundary(sks_solver *s, const float *psv, int32_t nrec_psv,
                      const float *sh, int32_t nrec_sh);
 
+/* Boundary records generated on the device instead of read: an upgoing plane
+ * P-SV (SV polarisation) and SH wave in the bottom layer, velocity vs (km/s),
+ * ray parameter p (s/km), Ricker pulse of dominant frequency f0 (Hz) centred
+ * at 1.5/f0 s, sampled every dp (the par file's) on the interface row and
+ * column, in the layout of greenfile/shgreenfile.  Stands in for the
+ * reference's boundary-trace producers (semsyn/src/aserpsv_sem.c:319-488 and
+ * the record splitting of demult.c:63-78) for plane-wave runs, with no file
+ * round trip; the records equal the host generator's (s-sks_gb300/synth.py)
+ * up to the rounding of exp. */
+typedef struct {
+    double vs, p, f0, sv_amp, sh_amp;
+} sks_plane_wave_t;
+int sks_set_boundary_plane_wave(sks_solver *s, const sks_plane_wave_t *pw);
+
 /* Replaces the time loop (sem2d_psvsh.c:418-513) for steps
  * [step, step+nsteps): each step writes ntrace floats to each of seis_u
  * (u_x), seis_w (-u_z) and seis_v (u_y), time-major, like kirrecord_zhl

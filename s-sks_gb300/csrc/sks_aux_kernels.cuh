@@ -259,4 +259,60 @@ __global__ void __launch_bounds__(128) k_record(const T* __restrict__ u, int64_t
     out[2 * ntrace + r] = vz;
 }
 
+// Analytic boundary records of an upgoing plane P-SV / SH wave with a Ricker
+// pulse in the bottom layer (velocity vs, ray parameter p, dominant frequency
+// f0), sampled every dp on the interface row (height nbl*h) and column
+// (x = nbl*h): record r, time r*dp, delay tau = p*x + eta*z, eta =
+// sqrt(1/vs^2 - p^2); SV polarisation (eta*vs, -p*vs), z up.  Layout as the
+// boundary files hold it: P-SV [u_bot(nx), w_bot(nx), u_left(nz), w_left(nz)],
+// SH [v_bot(nx), v_left(nz)].  Explicitly rounded FP64 operations, so only exp
+// may round differently from a host evaluation of the same formula.
+__device__ __forceinline__ double ricker_at(double t, double pf)
+{
+    const double x = __dmul_rn(pf, t);
+    const double a = __dmul_rn(x, x);
+    return __dmul_rn(__dsub_rn(1.0, __dmul_rn(2.0, a)), exp(-a));
+}
+
+static __global__ void __launch_bounds__(256) k_plane_wave(float* __restrict__ psv, float* __restrict__ sh, int nrec_psv,
+                                                    int nrec_sh, int nx, int nz, double h, int nbl, double vs,
+                                                    double p, double f0, double dp, double sv_amp, double sh_amp)
+{
+    const int mtotal = 2 * (nx + nz), shtotal = nx + nz;
+    const double eta = sqrt(fmax(__dsub_rn(__ddiv_rn(1.0, __dmul_rn(vs, vs)), __dmul_rn(p, p)), 0.0));
+    const double delay = __ddiv_rn(1.5, f0);
+    const double pf = __dmul_rn(3.141592653589793, f0);
+    const double zb = __dmul_rn(eta, __dmul_rn((double)nbl, h));   // eta * (nbl h)
+    const double xl = __dmul_rn(p, __dmul_rn((double)nbl, h));     // p * (nbl h)
+    const double ux = __dmul_rn(__dmul_rn(sv_amp, eta), vs), uz = __dmul_rn(__dmul_rn(-sv_amp, p), vs);
+    const int64_t n1 = (int64_t)nrec_psv * mtotal, n2 = (int64_t)nrec_sh * shtotal;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n1 + n2; i += (int64_t)gridDim.x * blockDim.x) {
+        const bool fam_sh = i >= n1;
+        const int64_t k = fam_sh ? i - n1 : i;
+        const int L = fam_sh ? shtotal : mtotal;
+        const int r = (int)(k / L), c = (int)(k - (int64_t)r * L);
+        const double t = __dmul_rn((double)r, dp);
+        double tau;
+        int part;                          // 0: bottom line, 1: left column
+        int j;
+        if (!fam_sh) {
+            part = (c >= 2 * nx) ? 1 : 0;
+            j = part ? (c - 2 * nx) % nz : c % nx;
+        } else {
+            part = c >= nx ? 1 : 0;
+            j = part ? c - nx : c;
+        }
+        if (!part) tau = __dadd_rn(__dmul_rn(p, __dmul_rn((double)j, h)), zb);
+        else tau = __dadd_rn(xl, __dmul_rn(eta, __dmul_rn((double)j, h)));
+        const double rk = ricker_at(__dsub_rn(__dsub_rn(t, delay), tau), pf);
+        if (fam_sh) {
+            sh[k] = (float)__dmul_rn(sh_amp, rk);
+        } else {
+            const bool vert = part ? (c - 2 * nx) >= nz : c >= nx;
+            psv[k] = (float)(vert ? __dmul_rn(-uz, rk) : __dmul_rn(ux, rk));
+        }
+    }
+}
+
 }  // namespace sks
+

@@ -566,15 +566,12 @@ extern "C" int sks_open_par(int argc, const char* const* argv, int precision, in
     return sks_open_setup(su, precision, device, out);
 }
 
-extern "C" int sks_set_boundary(sks_solver* s, const float* psv, int32_t nrec_psv, const float* sh, int32_t nrec_sh)
+namespace {
+
+// device buffers for the records the run reads
+int alloc_records(sks_solver* s)
 {
-    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
     const sks_model& m = s->m;
-    if (nrec_psv < m.nrec_psv) return set_err(SKS_ERR_BOUNDARY, "the run reads %d P-SV records, %d given", m.nrec_psv, nrec_psv);
-    if (!m.psv_only && nrec_sh < m.nrec_sh) return set_err(SKS_ERR_BOUNDARY, "the run reads %d SH records, %d given", m.nrec_sh, nrec_sh);
-    if (m.nrec_psv > 0 && !psv) return set_err(SKS_ERR_ARG, "psv records are NULL");
-    if (!m.psv_only && m.nrec_sh > 0 && !sh) return set_err(SKS_ERR_ARG, "sh records are NULL");
-    cudaSetDevice(s->device);
     const size_t npsv = (size_t)m.nrec_psv * m.mtotal, nsh = (size_t)m.nrec_sh * m.shtotal;
     if (s->nrec_psv_loaded < m.nrec_psv || !s->rec_psv) {
         if (s->rec_psv) { cudaFree(s->rec_psv); s->device_bytes -= (int64_t)(sizeof(float) * (size_t)s->nrec_psv_loaded * m.mtotal); s->rec_psv = nullptr; }
@@ -587,6 +584,46 @@ extern "C" int sks_set_boundary(sks_solver* s, const float* psv, int32_t nrec_ps
         int rc = dmalloc(s, &s->rec_sh, nsh);
         if (rc) return rc;
         s->nrec_sh_loaded = m.nrec_sh;
+    }
+    return SKS_OK;
+}
+
+}  // namespace
+
+extern "C" int sks_set_boundary_plane_wave(sks_solver* s, const sks_plane_wave_t* pw)
+{
+    if (!s || !pw) return set_err(SKS_ERR_ARG, "NULL argument");
+    if (!(pw->vs > 0.0) || !(pw->f0 > 0.0) || !(pw->p >= 0.0)) return set_err(SKS_ERR_ARG, "plane wave needs vs > 0, f0 > 0, p >= 0");
+    const sks_model& m = s->m;
+    cudaSetDevice(s->device);
+    int rc = alloc_records(s);
+    if (rc) return rc;
+    const double sh_amp = m.psv_only ? 0.0 : pw->sh_amp;
+    const int64_t tot = (int64_t)m.nrec_psv * m.mtotal + (int64_t)m.nrec_sh * m.shtotal;
+    if (tot > 0) {
+        const int blocks = (int)std::min<int64_t>((tot + 255) / 256, (int64_t)s->sms * 16);
+        k_plane_wave<<<blocks, 256, 0, s->stream>>>(s->rec_psv, s->rec_sh, m.nrec_psv, m.nrec_sh, m.nx, m.nz, m.h, s->nbl,
+                                                    pw->vs, pw->p, pw->f0, m.dp, pw->sv_amp, sh_amp);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    s->boundary_ready = true;
+    return SKS_OK;
+}
+
+extern "C" int sks_set_boundary(sks_solver* s, const float* psv, int32_t nrec_psv, const float* sh, int32_t nrec_sh)
+{
+    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    const sks_model& m = s->m;
+    if (nrec_psv < m.nrec_psv) return set_err(SKS_ERR_BOUNDARY, "the run reads %d P-SV records, %d given", m.nrec_psv, nrec_psv);
+    if (!m.psv_only && nrec_sh < m.nrec_sh) return set_err(SKS_ERR_BOUNDARY, "the run reads %d SH records, %d given", m.nrec_sh, nrec_sh);
+    if (m.nrec_psv > 0 && !psv) return set_err(SKS_ERR_ARG, "psv records are NULL");
+    if (!m.psv_only && m.nrec_sh > 0 && !sh) return set_err(SKS_ERR_ARG, "sh records are NULL");
+    cudaSetDevice(s->device);
+    const size_t npsv = (size_t)m.nrec_psv * m.mtotal, nsh = (size_t)m.nrec_sh * m.shtotal;
+    {
+        int rc = alloc_records(s);
+        if (rc) return rc;
     }
     if (npsv) CK(cudaMemcpyAsync(s->rec_psv, psv, npsv * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     if (nsh) {

@@ -31,7 +31,7 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_setup_receivers", "sks_setup_schedule", "sks_setup_close", "sks_open_setup",
            "sks_kernel_launches", "sks_last_run_ms", "sks_enable_kernel_timing", "sks_kernel_timing",
            "sks_set_tuning", "sks_get_tuning", "sks_autotune", "sks_line_increments",
-           "sks_line_increments_noalloc",
+           "sks_line_increments_noalloc", "sks_set_boundary_plane_wave",
            "sks_batch_create", "sks_batch_add", "sks_batch_remove", "sks_batch_size", "sks_batch_run",
            "sks_batch_set_tuning", "sks_batch_get_tuning", "sks_batch_autotune", "sks_batch_last_run_ms",
            "sks_batch_kernel_launches", "sks_batch_destroy",
@@ -55,6 +55,11 @@ class Info(C.Structure):
 
     def asdict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class PlaneWave(C.Structure):
+    _fields_ = [("vs", C.c_double), ("p", C.c_double), ("f0", C.c_double), ("sv_amp", C.c_double),
+                ("sh_amp", C.c_double)]
 
 
 class Tuning(C.Structure):
@@ -104,6 +109,7 @@ def lib() -> C.CDLL:
         L.sks_line_increments.argtypes = [vp, C.c_int32, C.c_int32, dp]
         L.sks_line_increments_noalloc.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp,
                                                   C.c_int32, vp, vp]
+        L.sks_set_boundary_plane_wave.argtypes = [vp, C.POINTER(PlaneWave)]
         L.sks_destroy.argtypes = [vp]
         L.sks_destroy.restype = None
         fpp = C.POINTER(C.POINTER(C.c_float))
@@ -234,6 +240,10 @@ class Solver:
         else:
             nsh = 0
         _check(lib().sks_set_boundary(self.h, _f32(psv), nps, _f32(sh), nsh))
+
+    def set_boundary_plane_wave(self, vs: float, p: float, f0: float, sv_amp: float = 1.0, sh_amp: float = 0.0):
+        pw = PlaneWave(vs, p, f0, sv_amp, sh_amp)
+        _check(lib().sks_set_boundary_plane_wave(self.h, C.byref(pw)))
 
     def run(self, nsteps: int, out=None):
         nt = self.info()["ntrace"]

@@ -128,6 +128,7 @@ class Case:
     semmodel_full: bool = False
     psv_only: bool = False
     flat: int = 1
+    write_records: bool = True     # False: no greenfile/shgreenfile (records generated on the device)
     extra: dict = field(default_factory=dict)
 
     @property
@@ -184,9 +185,10 @@ def write_case(case: Case, d: str) -> dict:
     h = float(eh_eff) / N
     nx, nz = case.nex * N + 1, case.nez * N + 1
     nbl = case.neh * N
-    write_plane_wave(os.path.join(d, "greenfile"), os.path.join(d, "shgreenfile"),
-                     nx=nx, nz=nz, h=h, nbl=nbl, vs=vs_b, p=case.p, f0=case.f0,
-                     dp=dp, nt=nt, sv_amp=case.sv_amp, sh_amp=case.sh_amp)
+    if case.write_records:
+        write_plane_wave(os.path.join(d, "greenfile"), os.path.join(d, "shgreenfile"),
+                         nx=nx, nz=nz, h=h, nbl=nbl, vs=vs_b, p=case.p, f0=case.f0,
+                         dp=dp, nt=nt, sv_amp=case.sv_amp, sh_amp=case.sh_amp)
     par = {
         "greenfile": "greenfile", "shgreenfile": "shgreenfile", "raymodel": "raymodel",
         "semmodel": "semmodel", "nt": nt, "dp": _fmt(dp), "nex": case.nex, "eh": _fmt(case.eh),
@@ -203,7 +205,7 @@ def write_case(case: Case, d: str) -> dict:
     with open(os.path.join(d, "run.par"), "w") as f:
         for k, v in par.items():
             f.write(f"{k}={v}\n")
-    return {"nx": nx, "nz": nz, "h": h, "nt": nt, "dp": dp}
+    return {"nx": nx, "nz": nz, "h": h, "nt": nt, "dp": dp, "vs": vs_b}
 
 
 def ricker(t: np.ndarray, f0: float) -> np.ndarray:
@@ -276,3 +278,69 @@ def config_large(nst=40000) -> Case:
     H = 250.0
     return Case(nex=4000, nez=1000, eh=0.25, sdt=0.0015, nst=nst, layers=layered_aniso(H),
                 p=0.045, f0=2.0, ntrace=1001, rec_x0=0.0, rec_dx=1.0, semmodel_full=True)
+
+
+GLL4_MIN_SPACING = (1.0 - math.sqrt(3.0 / 7.0)) / 2.0   # smallest GLL gap of degree 4, in element sizes
+
+
+def vp_max(layers) -> float:
+    """Largest diagonal P velocity sqrt(C_ii / rho) over the layers (i = 1..3)."""
+    return max(math.sqrt(max(L.C[0, 0], L.C[1, 1], L.C[2, 2]) / L.rho) for L in layers)
+
+
+def stable_dt(eh: float, layers, courant: float = 0.4) -> float:
+    """dt = courant * h_min / vp_max, h_min the smallest GLL spacing of an element of size eh."""
+    return courant * GLL4_MIN_SPACING * eh / vp_max(layers)
+
+
+def layered_aniso_box(H: float, strength: float, az: float, tilt: float, crust_km=35.0, aniso_km=100.0):
+    """Crust over a hexagonal layer over the mantle, for a box of height H;
+    layers that would lie below the box bottom are left out."""
+    out = [L for L in layered_aniso(H, crust_km, aniso_km, strength, az, tilt) if L.top > 0.0]
+    return out
+
+
+def draw_instance(rng: np.random.Generator, nex: int, nez: int, eh: float, seconds: float = 60.0,
+                  ntrace: int = 101) -> dict:
+    """One SKS solve with the draws of the batched and served workloads: ray
+    parameter U[0.038, 0.052] s/km, anisotropy U[0, 6] %, fast-axis azimuth
+    U[0, 180) deg, tilt U[0, 30) deg, Ricker U[0.2, 0.5] Hz; dt = 0.4 h_min /
+    vp_max and `seconds` of simulated time."""
+    p = float(rng.uniform(0.038, 0.052))
+    strength = float(rng.uniform(0.0, 0.06))
+    az = float(rng.uniform(0.0, 180.0))
+    tilt = float(rng.uniform(0.0, 30.0))
+    f0 = float(rng.uniform(0.2, 0.5))
+    H = nez * eh
+    layers = layered_aniso_box(H, strength, az, tilt)
+    dt = stable_dt(eh, layers)
+    nst = int(math.ceil(seconds / dt))
+    width = nex * eh
+    dx = width * 0.9 / max(1, ntrace - 1)
+    case = Case(nex=nex, nez=nez, eh=eh, sdt=dt, nst=nst, layers=layers, p=p, f0=f0, sv_amp=1.0, sh_amp=0.0,
+                ntrace=ntrace, rec_x0=0.05 * width, rec_dx=dx, semmodel_full=True, write_records=False)
+    return {"case": case, "p": p, "strength": strength, "az": az, "tilt": tilt, "f0": f0, "dt": dt, "nst": nst,
+            "vs_bottom": math.sqrt(layers[0].C[3, 3] / layers[0].rho)}
+
+
+def config_batch(n: int = 64, seed: int = 20240601, seconds: float = 60.0) -> list:
+    """The batched workload: n instances, nex U{200..1000}, nez U{100..400},
+    element size U[1, 2] km, the physics draws of draw_instance."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        nex = int(rng.integers(200, 1001))
+        nez = int(rng.integers(100, 401))
+        eh = float(rng.uniform(1.0, 2.0))
+        out.append(draw_instance(rng, nex, nez, eh, seconds))
+    return out
+
+
+def draw_served_size(rng: np.random.Generator) -> tuple:
+    """Served request mesh: lognormal element counts with median 400 x 200,
+    clipped to 100 x 50 .. 2000 x 600 (one shared log-normal factor keeps the
+    aspect near 2:1, plus a small independent spread)."""
+    g = rng.normal(0.0, 0.6)
+    nex = int(np.clip(round(400 * math.exp(g + rng.normal(0.0, 0.15))), 100, 2000))
+    nez = int(np.clip(round(200 * math.exp(g + rng.normal(0.0, 0.15))), 50, 600))
+    return nex, nez

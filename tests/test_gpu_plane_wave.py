@@ -1,0 +1,75 @@
+"""GPU: boundary records generated on the device equal the host generator's.
+
+sks_set_boundary_plane_wave() evaluates the plane-wave records of
+synth.plane_wave_records() on the device, with explicitly rounded FP64
+arithmetic; only exp may round differently, which moves a float32 record by
+at most one unit in the last place.  Both record sets drive the same FP64
+solve here: the interpolated boundary increments and the seismograms agree to
+that rounding.
+"""
+import numpy as np
+import pytest
+
+import sks
+import synth
+from util import chdir
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(tmp_path, psv_only=False, sh_amp=0.6):
+    H = 12.002
+    layers = [synth.SemLayer(H - 6, synth.iso_cij(8.1, 4.5, 3.4), 3.4),
+              synth.SemLayer(H - 3, synth.hexagonal_cij(8.1, 4.5, 3.4, 0.05, 30.0, 15.0), 3.4),
+              synth.SemLayer(H + 1, synth.iso_cij(6.4, 3.6, 2.8), 2.8)]
+    c = synth.Case(nex=29, nez=12, eh=1.0, sdt=0.005, nst=700, layers=layers, p=0.044, f0=1.3, sv_amp=1.0,
+                   sh_amp=sh_amp, ntrace=13, rec_dx=2.0, semmodel_full=True, write_records=False,
+                   psv_only=psv_only)
+    d = str(tmp_path)
+    synth.write_case(c, d)
+    return d, c, float(np.sqrt(layers[0].C[3, 3] / layers[0].rho))
+
+
+@pytest.mark.parametrize("psv_only", [False, True])
+def test_device_records_match_host_generator(tmp_path, psv_only):
+    d, c, vs = _case(tmp_path, psv_only)
+    sh_amp = 0.0 if psv_only else c.sh_amp
+    with chdir(d):
+        host = sks.Solver(["par=run.par"], precision=sks.FP64)
+        dev = sks.Solver(["par=run.par"], precision=sks.FP64)
+    i = host.info()
+    nbl = i["neh"] * i["hpn"]
+    nrec = max(i["nrec_psv"], i["nrec_sh"])
+    psv, sh = synth.plane_wave_records(i["nx"], i["nz"], i["h"], nbl, vs, c.p, c.f0, c.sdt, 0, nrec,
+                                       c.sv_amp, sh_amp)
+    host.set_boundary(psv[:i["nrec_psv"]], None if psv_only else sh[:i["nrec_sh"]])
+    dev.set_boundary_plane_wave(vs, c.p, c.f0, c.sv_amp, sh_amp)
+    # interpolated FP64 increments of the interface line: one float32 ulp of a record at most
+    scale = float(np.abs(psv).max())
+    a = host.line_increments(0, 400)
+    b = dev.line_increments(0, 400)
+    assert np.abs(a).max() > 1e-3 * scale
+    assert np.abs(a - b).max() <= 4 * np.finfo(np.float32).eps * scale
+    ua = host.run(c.nst)
+    ub = dev.run(c.nst)
+    assert np.linalg.norm(ua[0]) > 0 and np.linalg.norm(ua[2]) > 0
+    for k in range(3):
+        ref = np.linalg.norm(ua[k])
+        if ref == 0.0:
+            assert np.abs(ub[k]).max() == 0.0
+        else:
+            assert np.linalg.norm(ua[k] - ub[k]) <= 1e-6 * ref
+    host.close()
+    dev.close()
+
+
+def test_plane_wave_rejects_bad_parameters(tmp_path):
+    d, c, vs = _case(tmp_path)
+    with chdir(d):
+        s = sks.Solver(["par=run.par"], precision=sks.FP32C)
+    for bad in ((0.0, 0.04, 1.0), (4.5, 0.04, 0.0), (4.5, -0.01, 1.0)):
+        with pytest.raises(sks.SksError):
+            s.set_boundary_plane_wave(*bad)
+    with pytest.raises(sks.SksError):
+        s.run(5)                                   # still no boundary records
+    s.close()
