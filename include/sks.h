@@ -282,6 +282,61 @@ int64_t sks_batch_kernel_launches(const sks_batch *b);
 /* Destroys the batch; the members stay open and leave it. */
 void sks_batch_destroy(sks_batch *b);
 
+/* ---- serving ----------------------------------------------------------
+ * Solve requests that arrive at any time (continuous batching).  The
+ * reference has no counterpart: one solve is one process (sem2d_psvsh.c:82).
+ * A request is a host set-up (the par words, sks_setup_open) plus its form
+ * and boundary source; the server admits queued requests first-fit in
+ * arrival order while their device-memory footprint fits the budget (a
+ * request left waiting in 8 admission rounds blocks the queue behind it, so
+ * large requests are not starved), opens them on the device, and runs every
+ * admitted request of a form as a member of that form's batch, a quantum of
+ * steps per round, the FP32C and FP64 batches on their own streams.
+ * Requests join and leave between quanta; wavefields stay on the device; a
+ * finished request's seismograms are copied once into the caller's arrays
+ * and its device memory is freed.  Each result equals the same request run
+ * alone with the batch's tuning, bit for bit.  submit() may be called from
+ * another thread than step(). */
+typedef struct sks_server sks_server;
+
+#define SKS_REQ_QUEUED  0
+#define SKS_REQ_RUNNING 1
+#define SKS_REQ_DONE    2
+#define SKS_REQ_FAILED  3
+
+typedef struct {
+    int32_t state;          /* SKS_REQ_*                                      */
+    int32_t status;         /* the error status of a failed request           */
+    int32_t precision;
+    int32_t step, nst;      /* steps taken, steps of the run                  */
+    int32_t ntrace;
+    double  submit_s;       /* server clock (sks_server_clock), seconds;       */
+    double  admit_s;        /*   -1 until it happens                          */
+    double  done_s;
+    int64_t device_bytes;   /* held while running; the estimate while queued  */
+} sks_request_info_t;
+
+/* budget <= 0: 90 % of the device memory free at creation.  quantum_steps:
+ * steps per scheduling round (64 = one chunk). */
+int sks_server_create(int device, int64_t device_budget_bytes, int32_t quantum_steps, sks_server **out);
+int sks_server_set_tuning(sks_server *srv, int precision, const sks_tuning_t *t);
+/* Takes the set-up over (also on error).  pw: boundary records generated on
+ * the device; NULL: read at admission from the files the par words name
+ * (relative names resolved against the working directory at submission).
+ * seis_u/v/w: nst*ntrace floats each, filled when the request is done (any
+ * may be NULL); they must stay valid until then. */
+int sks_server_submit(sks_server *srv, sks_setup *su, int precision, const sks_plane_wave_t *pw,
+                      float *seis_u, float *seis_v, float *seis_w, int64_t *id);
+/* One scheduling round: retire requests whose batch quantum finished,
+ * admit, launch the idle forms' next quantum.  Returns the requests queued or
+ * running (0 when all are done), or a negative status. */
+int sks_server_step(sks_server *srv);
+int sks_server_request_info(sks_server *srv, int64_t id, sks_request_info_t *info);
+int sks_server_release(sks_server *srv, int64_t id);     /* forget a finished request */
+double sks_server_clock(const sks_server *srv);          /* seconds since creation */
+int64_t sks_server_device_bytes(const sks_server *srv);  /* held by running requests */
+void sks_server_destroy(sks_server *srv);
+
 const char *sks_last_error(void);
 
 #ifdef __cplusplus

@@ -52,6 +52,9 @@ struct sks_batch {
     double last_ms = 0.0;
     int64_t launches = 0;
     int64_t device_bytes = 0;
+    // the run in flight (batch_launch .. batch_finish)
+    bool running = false;
+    std::vector<int> start, target;
 };
 
 namespace {
@@ -288,6 +291,7 @@ void batch_detach(sks_solver* s)
 {
     sks_batch* b = s->batch;
     if (!b) return;
+    if (b->running) batch_finish(b);
     cudaStreamSynchronize(b->stream);
     b->mem.erase(std::remove(b->mem.begin(), b->mem.end(), s), b->mem.end());
     b->tables_dirty = true;
@@ -325,6 +329,7 @@ extern "C" int sks_batch_add(sks_batch* b, sks_solver* s)
 {
     if (!b || !s) return set_err(SKS_ERR_ARG, "NULL argument");
     if (s->batch) return set_err(SKS_ERR_STATE, "the solver is already a member of a batch");
+    if (b->running) return set_err(SKS_ERR_STATE, "the batch is running");
     if (s->precision != b->precision) return set_err(SKS_ERR_ARG, "the solver's form differs from the batch's");
     if (s->device != b->device) return set_err(SKS_ERR_ARG, "the solver is on device %d, the batch on %d", s->device, b->device);
     cudaSetDevice(b->device);
@@ -357,68 +362,108 @@ extern "C" int sks_batch_remove(sks_batch* b, sks_solver* s)
 
 extern "C" int sks_batch_size(const sks_batch* b) { return b ? (int)b->mem.size() : -1; }
 
-extern "C" int sks_batch_run(sks_batch* b, int32_t nsteps, float* const* su, float* const* sv, float* const* sw)
+namespace sksi {
+
+// First half of a batch run: step 0 of new members, then every member's
+// chunks and (for non-NULL arrays) the copies of its new seismogram rows, all
+// enqueued on the batch's stream.  Copies to pageable host memory make the
+// call wait for the stream; the serving loop passes no arrays.
+int batch_launch(sks_batch* b, int32_t nsteps, float* const* su, float* const* sv, float* const* sw)
 {
     if (!b) return set_err(SKS_ERR_ARG, "batch is NULL");
     if (nsteps < 0) return set_err(SKS_ERR_ARG, "nsteps=%d", nsteps);
+    if (b->running) return set_err(SKS_ERR_STATE, "the batch's previous run has not finished");
     cudaSetDevice(b->device);
     const int n = (int)b->mem.size();
-    if (n == 0) return 0;
-    std::vector<int> start(n), target(n);
+    b->start.assign(n, 0);
+    b->target.assign(n, 0);
+    if (n == 0) return SKS_OK;
     int rc = SKS_OK;
     for (int i = 0; i < n; i++) {
         sks_solver* s = b->mem[i];
         if ((rc = check_member(b, s, i))) return rc;
-        start[i] = s->step;
-        target[i] = std::min(s->m.nst, s->step + nsteps);
+        b->start[i] = s->step;
+        b->target[i] = std::min(s->m.nst, s->step + nsteps);
     }
     CK(cudaEventRecord(b->ev[0], b->stream));
     for (int i = 0; i < n; i++) {
         sks_solver* s = b->mem[i];
-        if (s->step == 0 && target[i] > 0 && (rc = first_step(s))) return rc;
+        if (s->step == 0 && b->target[i] > 0 && (rc = first_step(s))) return rc;
     }
     if ((rc = prepare(b))) return rc;
     int most = 0;
     for (int i = 0; i < n; i++) {
         sks_solver* s = b->mem[i];
-        const int left = std::max(0, target[i] - s->step);
-        b->hstate[i] = BatchState{s->step, std::min(b->chunk, left), target[i], 0};
+        const int left = std::max(0, b->target[i] - s->step);
+        b->hstate[i] = BatchState{s->step, std::min(b->chunk, left), b->target[i], 0};
         most = std::max(most, left);
     }
-    if (n) CK(cudaMemcpyAsync(b->dstate, b->hstate, sizeof(BatchState) * n, cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(b->dstate, b->hstate, sizeof(BatchState) * n, cudaMemcpyHostToDevice, b->stream));
     const int nchunks = (most + b->chunk - 1) / b->chunk;
     for (int c = 0; c < nchunks; c++) {
         CK(cudaGraphLaunch(b->exec, b->stream));
         b->launches += b->graph_kernels;
     }
     CK(cudaEventRecord(b->ev[1], b->stream));
+    b->running = true;
     // the new seismogram rows of each member into the caller's arrays
     for (int i = 0; i < n; i++) {
         sks_solver* s = b->mem[i];
-        const int nt = s->m.ntrace, rows = target[i] - start[i];
+        const int nt = s->m.ntrace, rows = b->target[i] - b->start[i];
         if (nt <= 0 || rows <= 0) continue;
         float* dst[3] = {su ? su[i] : nullptr, sv ? sv[i] : nullptr, sw ? sw[i] : nullptr};
         const size_t w = sizeof(float) * (size_t)nt;
         for (int c = 0; c < 3; c++)
             if (dst[c])
-                CK(cudaMemcpy2DAsync(dst[c], w, s->seis_full + (size_t)start[i] * 3 * nt + (size_t)c * nt, 3 * w, w,
+                CK(cudaMemcpy2DAsync(dst[c], w, s->seis_full + (size_t)b->start[i] * 3 * nt + (size_t)c * nt, 3 * w, w,
                                      (size_t)rows, cudaMemcpyDeviceToHost, b->stream));
     }
+    return SKS_OK;
+}
+
+bool batch_done(const sks_batch* b)
+{
+    return !b->running || cudaEventQuery(b->ev[1]) != cudaErrorNotReady;
+}
+
+bool batch_running(const sks_batch* b) { return b->running; }
+
+// Second half: wait for the stream, then move every member's step on.
+// Returns the most steps any member took.
+int batch_finish(sks_batch* b)
+{
+    if (!b->running) return 0;
+    cudaSetDevice(b->device);
+    b->running = false;
     CK(cudaStreamSynchronize(b->stream));
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
     b->last_ms = ms;
     int adv = 0;
-    for (int i = 0; i < n; i++) {
+    for (size_t i = 0; i < b->mem.size() && i < b->target.size(); i++) {
         sks_solver* s = b->mem[i];
-        if (target[i] > s->step) {
-            s->step = target[i];
-            s->cur = (target[i] - 1) & 1;
+        if (b->target[i] > s->step) {
+            s->step = b->target[i];
+            s->cur = (b->target[i] - 1) & 1;
             s->g_last = 0;
         }
-        adv = std::max(adv, target[i] - start[i]);
+        adv = std::max(adv, b->target[i] - b->start[i]);
     }
     return adv;
+}
+
+std::vector<sks_solver*>& batch_members(sks_batch* b) { return b->mem; }
+
+}  // namespace sksi
+
+extern "C" int sks_batch_run(sks_batch* b, int32_t nsteps, float* const* su, float* const* sv, float* const* sw)
+{
+    int rc = batch_launch(b, nsteps, su, sv, sw);
+    if (rc) {
+        if (b && b->running) { cudaStreamSynchronize(b->stream); b->running = false; }
+        return rc;
+    }
+    return batch_finish(b);
 }
 
 extern "C" int sks_batch_set_tuning(sks_batch* b, const sks_tuning_t* t)
@@ -429,6 +474,7 @@ extern "C" int sks_batch_set_tuning(sks_batch* b, const sks_tuning_t* t)
     if (t->register_cap < 0 || t->register_cap > 2) return set_err(SKS_ERR_ARG, "register_cap=%d: 0, 1 or 2", t->register_cap);
     if (t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
     if (t->waves != 0) return set_err(SKS_ERR_ARG, "a batch uses plain bands (waves=0)");
+    if (b->running) return set_err(SKS_ERR_STATE, "the batch is running");
     cudaSetDevice(b->device);
     cudaStreamSynchronize(b->stream);
     b->NW = t->warps_per_block;
@@ -465,6 +511,7 @@ extern "C" int sks_batch_autotune(sks_batch* b, int32_t steps, sks_tuning_t* bes
     if (steps < 1) steps = 4;
     const int n = (int)b->mem.size();
     if (n == 0) return set_err(SKS_ERR_STATE, "the batch is empty");
+    if (b->running) return set_err(SKS_ERR_STATE, "the batch is running");
     cudaSetDevice(b->device);
     for (int i = 0; i < n; i++) {
         sks_solver* s = b->mem[i];
@@ -540,6 +587,7 @@ extern "C" void sks_batch_destroy(sks_batch* b)
 {
     if (!b) return;
     cudaSetDevice(b->device);
+    if (b->running) batch_finish(b);
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (sks_solver* s : b->mem) s->batch = nullptr;
     b->mem.clear();

@@ -25,6 +25,11 @@ SKS_HIDDEN int sks_err(int code, const char* fmt, ...);
 
 struct sks_batch;
 
+// a host set-up (sks_setup_open): the model, before any device state
+struct sks_setup {
+    sks_model m;
+};
+
 struct sks_solver {
     sks_model m;
     int precision, device;
@@ -105,6 +110,12 @@ SKS_HIDDEN int snap_take(sks_solver* s, Snapshot& S);
 SKS_HIDDEN int snap_restore(sks_solver* s, const Snapshot& S);
 SKS_HIDDEN void snap_free(Snapshot& S);
 SKS_HIDDEN void batch_detach(sks_solver* s);   // sks_batch.cu: leave the batch (on destroy)
+// a batch run in two halves (sks_batch.cu), for the serving loop
+SKS_HIDDEN int batch_launch(sks_batch* b, int32_t nsteps, float* const* su, float* const* sv, float* const* sw);
+SKS_HIDDEN int batch_finish(sks_batch* b);
+SKS_HIDDEN bool batch_done(const sks_batch* b);
+SKS_HIDDEN bool batch_running(const sks_batch* b);
+SKS_HIDDEN std::vector<sks_solver*>& batch_members(sks_batch* b);
 
 template <typename T>
 Coef<T> make_coef(const sks_model& m)

@@ -1,0 +1,357 @@
+// The serving loop: solve requests arrive at any time and are admitted by
+// their device-memory footprint; admitted requests join the batch of their
+// form (FP32C or FP64), keep their wavefields on the device and advance one
+// quantum of steps per scheduling round together with every other admitted
+// request of that form (continuous batching: requests join and leave between
+// quanta, never waiting for a batch to drain).  The two forms' batches run on
+// their own streams and overlap on the device.  A finished request's whole
+// seismogram is copied once into the caller's arrays and its device memory
+// is released.
+//
+// The reference has no serving path: one solve is one process
+// (sem2d_psvsh.c:82), started per event by the driver scripts
+// (applications/test/prem_epi83.pl:81-82).  A request here is that process's
+// par words (as an sks_setup) plus its boundary records.
+#include "sks_internal.h"
+
+#include <unistd.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+
+using namespace sks;
+using namespace sksi;
+
+namespace {
+
+struct Request {
+    int64_t id = 0;
+    sks_setup* su = nullptr;           // owned until admission
+    int precision = SKS_FP32C;
+    bool has_pw = false;
+    sks_plane_wave_t pw{};
+    float* out[3] = {nullptr, nullptr, nullptr};
+    sks_solver* s = nullptr;           // while running
+    int64_t est_bytes = 0, bytes = 0;
+    double t_submit = -1, t_admit = -1, t_done = -1;
+    int state = SKS_REQ_QUEUED;
+    int status = SKS_OK;
+    int nst = 0, ntrace = 0;
+    int passed = 0;                    // later requests admitted ahead of it
+};
+
+// device bytes a request will hold, from its model (an upper bound of what
+// the solver, its boundary records and its whole-run seismograms allocate)
+int64_t estimate_bytes(const sks_model& m, int precision)
+{
+    const int64_t np = (int64_t)m.nx * m.nz;
+    const int64_t el = precision == SKS_FP64 ? 8 : 4;
+    const int64_t L = (int64_t)m.mtotal + m.shtotal;
+    const int64_t nline = (int64_t)m.nx + m.nz;
+    const int64_t nb = (int64_t)2 * m.nz + m.nx + 3 * m.hpn + 1;
+    int64_t b = 0;
+    b += 2 * 3 * np * el;                                   // two displacement buffers
+    if (precision == SKS_FP32C) b += 6 * np * 4;            // (d, c) pairs
+    b += 2 * np + np / 8 + 64;                              // material index, receiver bitmap
+    b += nb * 9 * el + (int64_t)m.nmat * 16 * el;           // Stacey coefficients, material table
+    b += ((int64_t)m.nrec_psv * m.mtotal + (int64_t)m.nrec_sh * m.shtotal) * 4;   // boundary records
+    b += (int64_t)std::max(1, m.nst) * 3 * std::max(1, m.ntrace) * 4;          // whole-run seismograms
+    b += (int64_t)2 * 64 * 3 * std::max(1, m.ntrace) * 4;                        // chunk seismograms
+    b += (int64_t)66 * L * 8 + (int64_t)65 * nline * 3 * el;                     // interpolation rows, increments
+    b += (int64_t)m.nt_sem * 48 * 2;                                             // schedule
+    b += (int64_t)m.ntrace * 20;                                                 // receiver tables
+    b += 2 * ((int64_t)m.nez + 1) * m.nx * 6 * el + (int64_t)(m.nez + 1) * (m.nex + 1) * 4;  // band seams
+    return b + b / 50 + ((int64_t)1 << 20);
+}
+
+// boundary files named relative to the submitter's working directory, made
+// absolute at submission (they are read at admission, on the serving thread)
+int absolute_path(char* path, size_t cap)
+{
+    if (!path[0] || path[0] == '/') return SKS_OK;
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd)) return set_err(SKS_ERR_IO, "getcwd failed");
+    char buf[4096 + 512 + 2];
+    const int n = snprintf(buf, sizeof buf, "%s/%s", cwd, path);
+    if (n < 0 || (size_t)n >= cap) return set_err(SKS_ERR_IO, "boundary file path too long: %s/%s", cwd, path);
+    memcpy(path, buf, (size_t)n + 1);
+    return SKS_OK;
+}
+
+}  // namespace
+
+struct sks_server {
+    int device = 0;
+    int64_t budget = 0;
+    int64_t in_use = 0;
+    int quantum = 64;
+    int max_active = 1024;
+    sks_batch* batch[2] = {nullptr, nullptr};      // by precision
+    std::mutex mu;                                 // guards queue, reqs, next_id
+    std::deque<Request*> queue;
+    std::unordered_map<int64_t, Request*> reqs;
+    std::vector<Request*> active[2];
+    int64_t next_id = 1;
+    std::chrono::steady_clock::time_point t0;
+    double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
+namespace {
+
+// A finished request: its seismograms to the caller, its device memory freed.
+void retire(sks_server* v, Request* r)
+{
+    sks_solver* s = r->s;
+    int rc = SKS_OK;
+    const int nt = s->m.ntrace;
+    if (nt > 0 && s->seis_full) {
+        const size_t w = sizeof(float) * (size_t)nt;
+        for (int c = 0; c < 3 && !rc; c++)
+            if (r->out[c] &&
+                cudaMemcpy2DAsync(r->out[c], w, s->seis_full + (size_t)c * nt, 3 * w, w, (size_t)s->m.nst,
+                                  cudaMemcpyDeviceToHost, s->stream) != cudaSuccess)
+                rc = set_err(SKS_ERR_CUDA, "copy of the seismograms of request %lld", (long long)r->id);
+        if (!rc && cudaStreamSynchronize(s->stream) != cudaSuccess)
+            rc = set_err(SKS_ERR_CUDA, "copy of the seismograms of request %lld", (long long)r->id);
+    }
+    sks_batch_remove(v->batch[r->precision], s);
+    sks_destroy(s);
+    r->s = nullptr;
+    v->in_use -= r->bytes;
+    r->t_done = v->now();
+    std::lock_guard<std::mutex> lk(v->mu);
+    r->state = rc ? SKS_REQ_FAILED : SKS_REQ_DONE;
+    r->status = rc;
+}
+
+// open the request's solver and make it a member of its form's batch
+int admit_one(sks_server* v, Request* r)
+{
+    sks_solver* s = nullptr;
+    sks_setup* su = r->su;
+    r->su = nullptr;
+    int rc = sks_open_setup(su, r->precision, v->device, &s);   // takes the set-up over
+    if (!rc) rc = r->has_pw ? sks_set_boundary_plane_wave(s, &r->pw) : sks_load_boundary_files(s);
+    if (!rc) rc = sks_batch_add(v->batch[r->precision], s);
+    if (rc) {
+        if (s) sks_destroy(s);
+        std::lock_guard<std::mutex> lk(v->mu);
+        r->state = SKS_REQ_FAILED;
+        r->status = rc;
+        r->t_done = v->now();
+        return rc;
+    }
+    r->s = s;
+    r->bytes = s->device_bytes;
+    v->in_use += r->bytes;
+    r->t_admit = v->now();
+    v->active[r->precision].push_back(r);
+    std::lock_guard<std::mutex> lk(v->mu);
+    r->state = SKS_REQ_RUNNING;
+    return SKS_OK;
+}
+
+// First fit in arrival order for the forms whose batch is idle; a queued
+// request left waiting in 8 admission rounds blocks the queue behind it, so
+// large requests are not starved.
+void admit(sks_server* v, const bool idle[2])
+{
+    std::vector<Request*> take;
+    {
+        std::lock_guard<std::mutex> lk(v->mu);
+        int64_t room = v->budget - v->in_use;
+        int nact = (int)(v->active[0].size() + v->active[1].size());
+        for (auto it = v->queue.begin(); it != v->queue.end();) {
+            Request* r = *it;
+            if (!idle[r->precision]) { ++it; continue; }
+            if (nact < v->max_active && r->est_bytes <= room) {
+                room -= r->est_bytes;
+                nact++;
+                take.push_back(r);
+                it = v->queue.erase(it);
+                continue;
+            }
+            r->passed++;
+            if (r->passed > 8) break;
+            ++it;
+        }
+    }
+    for (Request* r : take) admit_one(v, r);
+}
+
+}  // namespace
+
+extern "C" int sks_server_create(int device, int64_t budget, int32_t quantum, sks_server** out)
+{
+    if (!out) return set_err(SKS_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (quantum < 1) return set_err(SKS_ERR_ARG, "quantum_steps=%d", quantum);
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return set_err(SKS_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+    if (budget <= 0) {
+        size_t fr = 0, tot = 0;
+        e = cudaMemGetInfo(&fr, &tot);
+        if (e != cudaSuccess) return set_err(SKS_ERR_CUDA, "cudaMemGetInfo: %s", cudaGetErrorString(e));
+        budget = (int64_t)(fr / 10 * 9);
+    }
+    sks_server* v = new (std::nothrow) sks_server();
+    if (!v) return set_err(SKS_ERR_NOMEM, "cannot allocate the server");
+    v->device = device;
+    v->budget = budget;
+    v->quantum = quantum;
+    v->t0 = std::chrono::steady_clock::now();
+    int rc = sks_batch_create(SKS_FP64, device, &v->batch[SKS_FP64]);
+    if (!rc) rc = sks_batch_create(SKS_FP32C, device, &v->batch[SKS_FP32C]);
+    if (rc) {
+        sks_batch_destroy(v->batch[0]);
+        sks_batch_destroy(v->batch[1]);
+        delete v;
+        return rc;
+    }
+    *out = v;
+    return SKS_OK;
+}
+
+extern "C" int sks_server_set_tuning(sks_server* v, int precision, const sks_tuning_t* t)
+{
+    if (!v || !t) return set_err(SKS_ERR_ARG, "NULL argument");
+    if (precision != SKS_FP64 && precision != SKS_FP32C) return set_err(SKS_ERR_ARG, "unknown precision %d", precision);
+    if (batch_running(v->batch[precision])) batch_finish(v->batch[precision]);
+    return sks_batch_set_tuning(v->batch[precision], t);
+}
+
+extern "C" int sks_server_submit(sks_server* v, sks_setup* su, int precision, const sks_plane_wave_t* pw, float* su_out,
+                                 float* sv_out, float* sw_out, int64_t* id)
+{
+    if (!v || !su || !id) {
+        if (su) sks_setup_close(su);
+        return set_err(SKS_ERR_ARG, "NULL argument");
+    }
+    if (precision != SKS_FP64 && precision != SKS_FP32C) {
+        sks_setup_close(su);
+        return set_err(SKS_ERR_ARG, "unknown precision %d", precision);
+    }
+    if (!pw) {
+        int rc = absolute_path(su->m.greenfile, sizeof su->m.greenfile);
+        if (!rc && !su->m.psv_only) rc = absolute_path(su->m.shgreenfile, sizeof su->m.shgreenfile);
+        if (rc) { sks_setup_close(su); return rc; }
+    }
+    Request* r = new (std::nothrow) Request();
+    if (!r) { sks_setup_close(su); return set_err(SKS_ERR_NOMEM, "cannot allocate the request"); }
+    r->su = su;
+    r->precision = precision;
+    if (pw) { r->has_pw = true; r->pw = *pw; }
+    r->out[0] = su_out; r->out[1] = sv_out; r->out[2] = sw_out;
+    r->est_bytes = estimate_bytes(su->m, precision);
+    r->nst = su->m.nst;
+    r->ntrace = su->m.ntrace;
+    r->t_submit = v->now();
+    std::lock_guard<std::mutex> lk(v->mu);
+    r->id = v->next_id++;
+    v->reqs[r->id] = r;
+    if (r->est_bytes > v->budget) {
+        r->state = SKS_REQ_FAILED;
+        r->status = SKS_ERR_NOMEM;
+        r->t_done = r->t_submit;
+        sks_setup_close(r->su);
+        r->su = nullptr;
+    } else {
+        v->queue.push_back(r);
+    }
+    *id = r->id;
+    return SKS_OK;
+}
+
+extern "C" int sks_server_step(sks_server* v)
+{
+    if (!v) return set_err(SKS_ERR_ARG, "server is NULL");
+    cudaSetDevice(v->device);
+    bool progressed = false;
+    // finished quanta: move steps on, retire the requests that reached their end
+    for (int f = 0; f < 2; f++) {
+        sks_batch* b = v->batch[f];
+        if (!batch_running(b) || !batch_done(b)) continue;
+        const int rc = batch_finish(b);
+        if (rc < 0) return rc;
+        progressed = true;
+        std::vector<Request*> keep;
+        for (Request* r : v->active[f]) {
+            if (r->s->step >= r->s->m.nst) retire(v, r);
+            else keep.push_back(r);
+        }
+        v->active[f].swap(keep);
+    }
+    // admission into the idle forms, then their next quantum
+    bool idle[2] = {!batch_running(v->batch[0]), !batch_running(v->batch[1])};
+    admit(v, idle);
+    for (int f = 0; f < 2; f++) {
+        if (!idle[f] || v->active[f].empty()) continue;
+        const int rc = batch_launch(v->batch[f], v->quantum, nullptr, nullptr, nullptr);
+        if (rc < 0) return rc;
+        progressed = true;
+    }
+    if (!progressed && (batch_running(v->batch[0]) || batch_running(v->batch[1])))
+        std::this_thread::sleep_for(std::chrono::microseconds(100));
+    std::lock_guard<std::mutex> lk(v->mu);
+    return (int)(v->queue.size() + v->active[0].size() + v->active[1].size());
+}
+
+extern "C" int sks_server_request_info(sks_server* v, int64_t id, sks_request_info_t* info)
+{
+    if (!v || !info) return set_err(SKS_ERR_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(v->mu);
+    auto it = v->reqs.find(id);
+    if (it == v->reqs.end()) return set_err(SKS_ERR_ARG, "no request %lld", (long long)id);
+    const Request* r = it->second;
+    info->state = r->state;
+    info->status = r->status;
+    info->precision = r->precision;
+    info->step = r->s ? r->s->step : (r->state == SKS_REQ_DONE ? r->nst : 0);
+    info->nst = r->nst;
+    info->ntrace = r->ntrace;
+    info->submit_s = r->t_submit;
+    info->admit_s = r->t_admit;
+    info->done_s = r->t_done;
+    info->device_bytes = r->s ? r->bytes : r->est_bytes;
+    return SKS_OK;
+}
+
+extern "C" int sks_server_release(sks_server* v, int64_t id)
+{
+    if (!v) return set_err(SKS_ERR_ARG, "server is NULL");
+    std::lock_guard<std::mutex> lk(v->mu);
+    auto it = v->reqs.find(id);
+    if (it == v->reqs.end()) return set_err(SKS_ERR_ARG, "no request %lld", (long long)id);
+    if (it->second->state != SKS_REQ_DONE && it->second->state != SKS_REQ_FAILED)
+        return set_err(SKS_ERR_STATE, "request %lld has not finished", (long long)id);
+    delete it->second;
+    v->reqs.erase(it);
+    return SKS_OK;
+}
+
+extern "C" double sks_server_clock(const sks_server* v) { return v ? v->now() : -1.0; }
+
+extern "C" int64_t sks_server_device_bytes(const sks_server* v) { return v ? v->in_use : -1; }
+
+extern "C" void sks_server_destroy(sks_server* v)
+{
+    if (!v) return;
+    cudaSetDevice(v->device);
+    for (int f = 0; f < 2; f++)
+        if (v->batch[f] && batch_running(v->batch[f])) batch_finish(v->batch[f]);
+    for (int f = 0; f < 2; f++)
+        for (Request* r : v->active[f])
+            if (r->s) { sks_batch_remove(v->batch[f], r->s); sks_destroy(r->s); r->s = nullptr; }
+    sks_batch_destroy(v->batch[0]);
+    sks_batch_destroy(v->batch[1]);
+    for (auto& kv : v->reqs) {
+        if (kv.second->su) sks_setup_close(kv.second->su);
+        delete kv.second;
+    }
+    delete v;
+}

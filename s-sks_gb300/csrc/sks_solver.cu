@@ -35,9 +35,6 @@ extern "C" __attribute__((visibility("hidden"))) int sks_internal_set_error(int 
     return set_err(code, "%s", msg);
 }
 
-struct sks_setup {
-    sks_model m;
-};
 
 static void fill_info(const sks_model& m, sks_info_t* info)
 {

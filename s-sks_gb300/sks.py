@@ -35,6 +35,9 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_batch_create", "sks_batch_add", "sks_batch_remove", "sks_batch_size", "sks_batch_run",
            "sks_batch_set_tuning", "sks_batch_get_tuning", "sks_batch_autotune", "sks_batch_last_run_ms",
            "sks_batch_kernel_launches", "sks_batch_destroy",
+           "sks_server_create", "sks_server_set_tuning", "sks_server_submit", "sks_server_step",
+           "sks_server_request_info", "sks_server_release", "sks_server_clock", "sks_server_device_bytes",
+           "sks_server_destroy",
            "sks_destroy", "sks_last_error"]
 
 KERNEL_CLASSES = ["element", "seam", "inject", "record", "interp"]
@@ -55,6 +58,18 @@ class Info(C.Structure):
 
     def asdict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("precision", C.c_int32), ("step", C.c_int32),
+                ("nst", C.c_int32), ("ntrace", C.c_int32), ("submit_s", C.c_double), ("admit_s", C.c_double),
+                ("done_s", C.c_double), ("device_bytes", C.c_int64)]
+
+    def asdict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class PlaneWave(C.Structure):
@@ -127,6 +142,18 @@ def lib() -> C.CDLL:
         L.sks_batch_kernel_launches.restype = C.c_int64
         L.sks_batch_destroy.argtypes = [vp]
         L.sks_batch_destroy.restype = None
+        L.sks_server_create.argtypes = [C.c_int, C.c_int64, C.c_int32, C.POINTER(vp)]
+        L.sks_server_set_tuning.argtypes = [vp, C.c_int, C.POINTER(Tuning)]
+        L.sks_server_submit.argtypes = [vp, vp, C.c_int, C.POINTER(PlaneWave), fp, fp, fp, C.POINTER(C.c_int64)]
+        L.sks_server_step.argtypes = [vp]
+        L.sks_server_request_info.argtypes = [vp, C.c_int64, C.POINTER(RequestInfo)]
+        L.sks_server_release.argtypes = [vp, C.c_int64]
+        L.sks_server_clock.argtypes = [vp]
+        L.sks_server_clock.restype = C.c_double
+        L.sks_server_device_bytes.argtypes = [vp]
+        L.sks_server_device_bytes.restype = C.c_int64
+        L.sks_server_destroy.argtypes = [vp]
+        L.sks_server_destroy.restype = None
         L.sks_last_error.restype = C.c_char_p
         _lib = L
     return _lib
@@ -374,6 +401,69 @@ class Batch:
             lib().sks_batch_destroy(self.h)
             self.h = C.c_void_p()
         self.members = []
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """The serving loop (sks_server_*): submit() from any thread, step() in a loop."""
+
+    def __init__(self, device: int = 0, budget: int = 0, quantum: int = 64):
+        self.h = C.c_void_p()
+        _check(lib().sks_server_create(device, budget, quantum, C.byref(self.h)))
+        self.outputs: dict[int, tuple] = {}
+
+    def set_tuning(self, precision: int, warps_per_block: int, band_rows: int, zseam: int, register_cap: int):
+        t = Tuning(warps_per_block, band_rows, zseam, register_cap, 0, 0, 0.0)
+        _check(lib().sks_server_set_tuning(self.h, precision, C.byref(t)))
+
+    def submit(self, setup: "Setup", precision: int, plane_wave: tuple | None = None, want: bool = True) -> int:
+        """plane_wave = (vs, p, f0, sv_amp, sh_amp) or None (the par's boundary files)."""
+        i = setup.info()
+        out = tuple(np.zeros((i["nst"], max(i["ntrace"], 0)), np.float32) for _ in range(3)) if want else None
+        pw = C.byref(PlaneWave(*plane_wave)) if plane_wave is not None else None
+        h, setup.h = setup.h, C.c_void_p()
+        rid = C.c_int64()
+        ptrs = [_f32(o) for o in out] if out else [None, None, None]
+        _check(lib().sks_server_submit(self.h, h, precision, pw, ptrs[0], ptrs[1], ptrs[2], C.byref(rid)))
+        self.outputs[rid.value] = out
+        return rid.value
+
+    def step(self) -> int:
+        return _check(lib().sks_server_step(self.h))
+
+    def info(self, rid: int) -> dict:
+        r = RequestInfo()
+        _check(lib().sks_server_request_info(self.h, rid, C.byref(r)))
+        return r.asdict()
+
+    def result(self, rid: int):
+        return self.outputs[rid]
+
+    def release(self, rid: int):
+        _check(lib().sks_server_release(self.h, rid))
+        self.outputs.pop(rid, None)
+
+    def clock(self) -> float:
+        return lib().sks_server_clock(self.h)
+
+    def device_bytes(self) -> int:
+        return lib().sks_server_device_bytes(self.h)
+
+    def close(self):
+        if self.h:
+            lib().sks_server_destroy(self.h)
+            self.h = C.c_void_p()
 
     def __enter__(self):
         return self

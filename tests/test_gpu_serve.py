@@ -1,0 +1,141 @@
+"""GPU: the serving loop (continuous batching).
+
+Requests of both forms, uneven sizes and boundary sources arrive while others
+run; each result equals the same request run alone with the batch's tuning,
+bit for bit; admission never lets the running requests hold more device
+memory than the budget; a request that can never fit fails cleanly.
+"""
+import numpy as np
+import pytest
+
+import sks
+import synth
+from util import chdir
+
+pytestmark = pytest.mark.gpu
+
+T32 = (4, 3, 0, 1)
+T64 = (4, 4, 1, 0)
+
+
+def _layers(H, aniso):
+    mid = synth.hexagonal_cij(8.1, 4.5, 3.4, 0.05, 60.0, 20.0) if aniso else synth.iso_cij(8.0, 4.45, 3.35)
+    return [synth.SemLayer(H - 6, synth.iso_cij(8.1, 4.5, 3.4), 3.4),
+            synth.SemLayer(H - 3, mid, 3.4),
+            synth.SemLayer(H + 1, synth.iso_cij(6.4, 3.6, 2.8), 2.8)]
+
+
+REQS = [  # nex, nez, eh, dt, nst, p, f0, aniso, form, device records
+    (31, 10, 1.0, 0.005, 850, 0.045, 1.5, True, sks.FP32C, True),
+    (17, 6, 2.0, 0.01, 620, 0.05, 0.8, False, sks.FP64, False),
+    (45, 12, 1.0, 0.004, 1100, 0.038, 1.2, True, sks.FP32C, False),
+    (24, 10, 1.5, 0.006, 960, 0.042, 1.0, True, sks.FP64, True),
+    (20, 8, 1.0, 0.005, 700, 0.048, 1.4, True, sks.FP32C, True),
+    (38, 9, 1.0, 0.005, 800, 0.040, 1.1, False, sks.FP32C, False),
+]
+
+
+@pytest.fixture(scope="module")
+def reqs(tmp_path_factory):
+    out = []
+    for i, (nex, nez, eh, dt, nst, p, f0, aniso, form, dev) in enumerate(REQS):
+        d = str(tmp_path_factory.mktemp(f"req{i}"))
+        H = nez * eh + 0.002
+        layers = _layers(H, aniso)
+        c = synth.Case(nex=nex, nez=nez, eh=eh, sdt=dt, nst=nst, layers=layers, p=p, f0=f0, sv_amp=1.0, sh_amp=0.3,
+                       ntrace=7, rec_dx=nex * eh / 8, semmodel_full=True, write_records=not dev)
+        synth.write_case(c, d)
+        pw = (float(np.sqrt(layers[0].C[3, 3] / layers[0].rho)), p, f0, 1.0, 0.3) if dev else None
+        out.append((d, form, pw, nst))
+    return out
+
+
+def _alone(d, form, pw, nst):
+    with chdir(d):
+        s = sks.Solver(["par=run.par"], precision=form)
+        if pw is None:
+            s.load_boundary_files()
+    if pw is not None:
+        s.set_boundary_plane_wave(*pw)
+    s.set_tuning(*(T32 if form == sks.FP32C else T64), 0)
+    out = s.run(nst)
+    s.close()
+    return out
+
+
+def _setup(d):
+    with chdir(d):
+        return sks.Setup(["par=run.par"])
+
+
+def _serve(reqs, budget, arrivals, check_budget=None):
+    """arrivals[i]: scheduling round at which request i is submitted."""
+    srv = sks.Server(0, budget, 64)
+    srv.set_tuning(sks.FP32C, *T32)
+    srv.set_tuning(sks.FP64, *T64)
+    ids = {}
+    rnd = 0
+    saw_queue_while_running = False
+    while True:
+        for i, (d, form, pw, nst) in enumerate(reqs):
+            if arrivals[i] == rnd:
+                with chdir(d):                       # relative boundary file names resolve here
+                    ids[i] = srv.submit(_setup(d), form, pw)
+        left = srv.step()
+        if check_budget is not None:
+            assert srv.device_bytes() <= check_budget
+            st = [srv.info(r)["state"] for r in ids.values()]
+            if sks.REQ_QUEUED in st and sks.REQ_RUNNING in st:
+                saw_queue_while_running = True
+        rnd += 1
+        if left == 0 and len(ids) == len(reqs):
+            break
+        assert rnd < 100000
+    return srv, ids, saw_queue_while_running
+
+
+def test_each_result_is_the_same_alone_and_in_the_mix(reqs):
+    alone = [_alone(*r) for r in reqs]
+    assert all(max(np.abs(x).max() for x in a) > 0.05 for a in alone)
+    srv, ids, _ = _serve(reqs, 0, arrivals=[0, 0, 3, 5, 9, 14])
+    for i, rid in ids.items():
+        info = srv.info(rid)
+        assert info["state"] == sks.REQ_DONE, info
+        assert info["step"] == reqs[i][3]
+        assert 0 <= info["submit_s"] <= info["admit_s"] <= info["done_s"]
+        got = srv.result(rid)
+        for c in range(3):
+            assert np.array_equal(got[c], alone[i][c]), f"request {i} component {c}"
+        srv.release(rid)
+    assert srv.device_bytes() == 0
+    srv.close()
+
+
+def test_admission_respects_the_device_budget(reqs):
+    # the server's own footprint estimates (reported while queued), then room
+    # for about two requests at a time
+    est = []
+    with sks.Server(0, 1 << 40, 64) as probe:
+        for d, form, pw, nst in reqs:
+            with chdir(d):
+                est.append(probe.info(probe.submit(_setup(d), form, pw))["device_bytes"])
+    budget = int(2.2 * max(est))
+    alone = [_alone(*r) for r in reqs]
+    srv, ids, queued_while_running = _serve(reqs, budget, arrivals=[0] * len(reqs), check_budget=budget)
+    assert queued_while_running
+    for k, rid in ids.items():
+        assert srv.info(rid)["state"] == sks.REQ_DONE
+        got = srv.result(rid)
+        for c in range(3):
+            assert np.array_equal(got[c], alone[k][c])
+    srv.close()
+
+
+def test_request_larger_than_the_budget_fails(reqs):
+    srv = sks.Server(0, 1 << 20, 64)
+    d, form, pw, nst = reqs[2]
+    rid = srv.submit(_setup(d), form, pw)
+    assert srv.step() == 0
+    info = srv.info(rid)
+    assert info["state"] == sks.REQ_FAILED and info["status"] == -6
+    srv.close()
