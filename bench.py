@@ -328,6 +328,103 @@ def run_batch(gpu: int, steps: int, warmup: int, fp64_steps: int = 8) -> dict:
     return out
 
 
+def run_serve(gpu: int, rate: float, nreq: int = 24, seed: int = 7, fp64_frac: float = 0.1,
+              prep_threads: int = 8, quantum: int = 64) -> dict:
+    """The served workload: seeded Poisson arrivals of `nreq` SKS solve
+    requests at `rate` per second (mesh sizes lognormal, median 400 x 200
+    elements, clipped to 100 x 50 .. 2000 x 600, element 1-2 km; physics as in
+    the batched workload; FP64 with probability fp64_frac).  Each request's
+    host set-up is built at its arrival by a pool of threads and submitted;
+    the main thread runs the serving loop.  Latency runs from the scheduled
+    arrival to the moment the seismograms are in host memory."""
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+    import sks
+    import synth
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, nreq)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    specs = []
+    for _ in range(nreq):
+        nex, nez = synth.draw_served_size(rng)
+        eh = float(rng.uniform(1.0, 2.0))
+        inst = synth.draw_instance(rng, nex, nez, eh)
+        form = sks.FP64 if rng.random() < fp64_frac else sks.FP32C
+        specs.append((inst, form))
+    base = tempfile.mkdtemp(prefix="sks_serve_")
+    srv = sks.Server(gpu, 0, quantum)
+    srv.set_tuning(sks.FP32C, 4, 6, 0, 1)
+    srv.set_tuning(sks.FP64, 4, 8, 1, 0)
+    lock = threading.Lock()
+    ids, errors = {}, []
+    t_start = srv.clock() + 1.0
+
+    def prepare(k):
+        inst, form = specs[k]
+        wait = t_start + arrivals[k] - srv.clock()
+        if wait > 0:
+            time.sleep(wait)
+        try:
+            d = os.path.join(base, f"r{k:03d}")
+            synth.write_case(inst["case"], d, absolute=True)
+            su = sks.Setup([f"par={os.path.join(d, 'run.par')}"])
+            rid = srv.submit(su, form, (inst["vs_bottom"], inst["p"], inst["f0"], 1.0, 0.0))
+            with lock:
+                ids[k] = rid
+        except Exception as e:  # reported in the result
+            with lock:
+                errors.append(f"request {k}: {e}")
+                ids[k] = None
+
+    done = {}
+    work = {}
+    try:
+        with ThreadPoolExecutor(prep_threads) as pool:
+            futs = [pool.submit(prepare, k) for k in range(nreq)]
+            while len(done) < nreq:
+                srv.step()
+                with lock:
+                    items = list(ids.items())
+                for k, rid in items:
+                    if k in done:
+                        continue
+                    if rid is None:
+                        done[k] = None
+                        continue
+                    inf = srv.info(rid)
+                    if inf["state"] in (sks.REQ_DONE, sks.REQ_FAILED):
+                        out = srv.result(rid)
+                        ok = inf["state"] == sks.REQ_DONE and all(np.isfinite(o).all() for o in out)
+                        inf["finite"] = bool(ok)
+                        done[k] = inf
+                        c = specs[k][0]["case"]
+                        work[k] = (c.nex * 4 + 1) * (c.nez * 4 + 1) * inf["nst"]
+                        srv.release(rid)
+            for f in futs:
+                f.result()
+    finally:
+        srv.close()
+        shutil.rmtree(base, ignore_errors=True)
+    ok = {k: v for k, v in done.items() if v is not None and v["state"] == sks.REQ_DONE}
+    lat = {k: v["done_s"] - (t_start + arrivals[k]) for k, v in ok.items()}
+    def pct(xs, q):
+        return float(np.percentile(np.array(xs), q)) if xs else None
+    by_form = {}
+    for name, f in (("fp32c", sks.FP32C), ("fp64", sks.FP64)):
+        xs = [lat[k] for k in lat if specs[k][1] == f]
+        by_form[name] = {"requests": sum(1 for s in specs if s[1] == f), "completed": len(xs),
+                         "p50_s": pct(xs, 50), "p99_s": pct(xs, 99)}
+    span = max(v["done_s"] for v in ok.values()) - t_start if ok else None
+    return {"rate_per_s": rate, "requests": nreq, "completed": len(ok), "failed": nreq - len(ok),
+            "errors": errors[:3], "fp64_fraction": fp64_frac,
+            "latency_s": {"p50": pct(list(lat.values()), 50), "p99": pct(list(lat.values()), 99), **by_form},
+            "queue_wait_s_p50": pct([v["admit_s"] - (t_start + arrivals[k]) for k, v in ok.items()], 50),
+            "span_s": span, "solves_per_hour": len(ok) * 3600.0 / span if span else None,
+            "updates_per_s": sum(work[k] for k in ok) / span if span else None,
+            "all_finite": all(v["finite"] for v in ok.values()),
+            "arrival_window_s": float(arrivals[-1]), "quantum_steps": quantum}
+
+
 def _cpu_worker(args):
     d, nsteps, fp64 = args
     sys.path.insert(0, ROOT)
@@ -392,6 +489,10 @@ def main() -> None:
     ap.add_argument("--tuning", default="", help="W,B,Z,C[,V]: warps per CTA, band rows, band seams, register cap, waves")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-instance workload")
     ap.add_argument("--batch-only", action="store_true", help="only the batched workload (one JSON object)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served workload")
+    ap.add_argument("--serve-rates", default="", help="only the served workload at these arrival rates (req/s), "
+                    "one JSON object per rate, e.g. 2,5,10,20")
+    ap.add_argument("--serve-requests", type=int, default=24)
     a = ap.parse_args()
     a.warmup = max(3, a.warmup)
     dist, rank, world, local = _dist()
@@ -439,6 +540,10 @@ def main() -> None:
     if a.batch_only:
         print(json.dumps({"batch": run_batch(gpu, min(a.steps, 200), a.warmup)}))
         return
+    if a.serve_rates:
+        for r in a.serve_rates.split(","):
+            print(json.dumps({"serve": run_serve(gpu, float(r), a.serve_requests)}), flush=True)
+        return
     d = tempfile.mkdtemp(prefix="sks_bench_")
     try:
         nst = a.warmup + a.steps + 8
@@ -463,6 +568,9 @@ def main() -> None:
     batch = None
     if not a.no_batch:
         batch = run_batch(gpu, min(a.steps, 200), a.warmup)
+    serve = None
+    if not a.no_serve:
+        serve = run_serve(gpu, 2.0, a.serve_requests)
     if rank != 0:
         return
     npts = r32["points"]
@@ -520,6 +628,11 @@ def main() -> None:
         batch["solves_per_hour_ratio_fp32c_full_over_fp64"] = (batch["fp32c"]["full_solves"]["solves_per_hour"] /
                                                                 batch["fp64"]["solves_per_hour_at_this_rate"])
         line["batch"] = batch
+    if serve:
+        serve["workload"] = ("seeded Poisson arrivals of SKS solve requests; meshes lognormal, median 400x200 "
+                             "elements, clipped 100x50..2000x600, element 1-2 km, GLL degree 4; physics drawn as "
+                             "in the batched workload; 10 % FP64 requests; 60 s simulated each")
+        line["serve"] = serve
     if cpu:
         line["cpu_baseline"] = {"value": cpu["value"], "unit": "GLL-pt updates/s", "cores": 1, "kind": "port",
                                 "sample": f"{a.cpu_steps} time steps of the same mesh, one thread, oracle float "

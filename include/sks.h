@@ -286,12 +286,13 @@ void sks_batch_destroy(sks_batch *b);
  * Solve requests that arrive at any time (continuous batching).  The
  * reference has no counterpart: one solve is one process (sem2d_psvsh.c:82).
  * A request is a host set-up (the par words, sks_setup_open) plus its form
- * and boundary source; the server admits queued requests first-fit in
- * arrival order while their device-memory footprint fits the budget (a
- * request left waiting in 8 admission rounds blocks the queue behind it, so
- * large requests are not starved), opens them on the device, and runs every
- * admitted request of a form as a member of that form's batch, a quantum of
- * steps per round, the FP32C and FP64 batches on their own streams.
+ * and boundary source.  The server admits queued requests first come first
+ * served within each form, while their device-memory footprint fits the
+ * budget and the form's running grid points stay within its cap (by default
+ * 8 Mi points FP64, 24 Mi FP32C, about twice what fills the GPU; a larger
+ * request runs alone), opens them on the device, and runs every admitted
+ * request of a form as a member of that form's batch, a quantum of steps per
+ * round, the FP32C and FP64 batches on their own streams.
  * Requests join and leave between quanta; wavefields stay on the device; a
  * finished request's seismograms are copied once into the caller's arrays
  * and its device memory is freed.  Each result equals the same request run
@@ -320,6 +321,7 @@ typedef struct {
  * steps per scheduling round (64 = one chunk). */
 int sks_server_create(int device, int64_t device_budget_bytes, int32_t quantum_steps, sks_server **out);
 int sks_server_set_tuning(sks_server *srv, int precision, const sks_tuning_t *t);
+int sks_server_set_active_points(sks_server *srv, int precision, int64_t max_points);
 /* Takes the set-up over (also on error).  pw: boundary records generated on
  * the device; NULL: read at admission from the files the par words name
  * (relative names resolved against the working directory at submission).

@@ -42,7 +42,7 @@ struct Request {
     int state = SKS_REQ_QUEUED;
     int status = SKS_OK;
     int nst = 0, ntrace = 0;
-    int passed = 0;                    // later requests admitted ahead of it
+    int64_t points = 0;                // grid points of the mesh
 };
 
 // device bytes a request will hold, from its model (an upper bound of what
@@ -90,7 +90,11 @@ struct sks_server {
     int64_t budget = 0;
     int64_t in_use = 0;
     int quantum = 64;
-    int max_active = 1024;
+    // active grid points per form (index = precision): a cap of about twice
+    // what fills the GPU, so admitted requests finish in arrival order instead
+    // of all sharing the device
+    int64_t max_points[2] = {(int64_t)8 << 20, (int64_t)24 << 20};
+    int64_t active_points[2] = {0, 0};
     sks_batch* batch[2] = {nullptr, nullptr};      // by precision
     std::mutex mu;                                 // guards queue, reqs, next_id
     std::deque<Request*> queue;
@@ -123,6 +127,7 @@ void retire(sks_server* v, Request* r)
     sks_destroy(s);
     r->s = nullptr;
     v->in_use -= r->bytes;
+    v->active_points[r->precision] -= r->points;
     r->t_done = v->now();
     std::lock_guard<std::mutex> lk(v->mu);
     r->state = rc ? SKS_REQ_FAILED : SKS_REQ_DONE;
@@ -149,6 +154,7 @@ int admit_one(sks_server* v, Request* r)
     r->s = s;
     r->bytes = s->device_bytes;
     v->in_use += r->bytes;
+    v->active_points[r->precision] += r->points;
     r->t_admit = v->now();
     v->active[r->precision].push_back(r);
     std::lock_guard<std::mutex> lk(v->mu);
@@ -156,28 +162,32 @@ int admit_one(sks_server* v, Request* r)
     return SKS_OK;
 }
 
-// First fit in arrival order for the forms whose batch is idle; a queued
-// request left waiting in 8 admission rounds blocks the queue behind it, so
-// large requests are not starved.
+// Admission, first come first served within each form: the oldest queued
+// request of a form is admitted when its footprint fits the device budget and
+// the form's active grid points stay within its cap (a request larger than
+// the cap is admitted when the form has nothing running); later requests of
+// that form wait behind it.  Only forms whose batch is between quanta admit.
 void admit(sks_server* v, const bool idle[2])
 {
     std::vector<Request*> take;
     {
         std::lock_guard<std::mutex> lk(v->mu);
         int64_t room = v->budget - v->in_use;
-        int nact = (int)(v->active[0].size() + v->active[1].size());
-        for (auto it = v->queue.begin(); it != v->queue.end();) {
+        int64_t pts[2] = {v->active_points[0], v->active_points[1]};
+        bool blocked[2] = {!idle[0], !idle[1]};
+        for (auto it = v->queue.begin(); it != v->queue.end() && !(blocked[0] && blocked[1]);) {
             Request* r = *it;
-            if (!idle[r->precision]) { ++it; continue; }
-            if (nact < v->max_active && r->est_bytes <= room) {
+            const int f = r->precision;
+            if (blocked[f]) { ++it; continue; }
+            const bool fits_work = pts[f] == 0 || pts[f] + r->points <= v->max_points[f];
+            if (r->est_bytes <= room && fits_work) {
                 room -= r->est_bytes;
-                nact++;
+                pts[f] += r->points;
                 take.push_back(r);
                 it = v->queue.erase(it);
                 continue;
             }
-            r->passed++;
-            if (r->passed > 8) break;
+            blocked[f] = true;
             ++it;
         }
     }
@@ -225,6 +235,16 @@ extern "C" int sks_server_set_tuning(sks_server* v, int precision, const sks_tun
     return sks_batch_set_tuning(v->batch[precision], t);
 }
 
+extern "C" int sks_server_set_active_points(sks_server* v, int precision, int64_t max_points)
+{
+    if (!v) return set_err(SKS_ERR_ARG, "server is NULL");
+    if (precision != SKS_FP64 && precision != SKS_FP32C) return set_err(SKS_ERR_ARG, "unknown precision %d", precision);
+    if (max_points < 1) return set_err(SKS_ERR_ARG, "max_points=%lld", (long long)max_points);
+    std::lock_guard<std::mutex> lk(v->mu);
+    v->max_points[precision] = max_points;
+    return SKS_OK;
+}
+
 extern "C" int sks_server_submit(sks_server* v, sks_setup* su, int precision, const sks_plane_wave_t* pw, float* su_out,
                                  float* sv_out, float* sw_out, int64_t* id)
 {
@@ -250,6 +270,7 @@ extern "C" int sks_server_submit(sks_server* v, sks_setup* su, int precision, co
     r->est_bytes = estimate_bytes(su->m, precision);
     r->nst = su->m.nst;
     r->ntrace = su->m.ntrace;
+    r->points = (int64_t)su->m.nx * su->m.nz;
     r->t_submit = v->now();
     std::lock_guard<std::mutex> lk(v->mu);
     r->id = v->next_id++;

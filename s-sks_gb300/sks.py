@@ -35,7 +35,7 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_batch_create", "sks_batch_add", "sks_batch_remove", "sks_batch_size", "sks_batch_run",
            "sks_batch_set_tuning", "sks_batch_get_tuning", "sks_batch_autotune", "sks_batch_last_run_ms",
            "sks_batch_kernel_launches", "sks_batch_destroy",
-           "sks_server_create", "sks_server_set_tuning", "sks_server_submit", "sks_server_step",
+           "sks_server_create", "sks_server_set_tuning", "sks_server_set_active_points", "sks_server_submit", "sks_server_step",
            "sks_server_request_info", "sks_server_release", "sks_server_clock", "sks_server_device_bytes",
            "sks_server_destroy",
            "sks_destroy", "sks_last_error"]
@@ -144,6 +144,7 @@ def lib() -> C.CDLL:
         L.sks_batch_destroy.restype = None
         L.sks_server_create.argtypes = [C.c_int, C.c_int64, C.c_int32, C.POINTER(vp)]
         L.sks_server_set_tuning.argtypes = [vp, C.c_int, C.POINTER(Tuning)]
+        L.sks_server_set_active_points.argtypes = [vp, C.c_int, C.c_int64]
         L.sks_server_submit.argtypes = [vp, vp, C.c_int, C.POINTER(PlaneWave), fp, fp, fp, C.POINTER(C.c_int64)]
         L.sks_server_step.argtypes = [vp]
         L.sks_server_request_info.argtypes = [vp, C.c_int64, C.POINTER(RequestInfo)]
@@ -426,6 +427,9 @@ class Server:
     def set_tuning(self, precision: int, warps_per_block: int, band_rows: int, zseam: int, register_cap: int):
         t = Tuning(warps_per_block, band_rows, zseam, register_cap, 0, 0, 0.0)
         _check(lib().sks_server_set_tuning(self.h, precision, C.byref(t)))
+
+    def set_active_points(self, precision: int, max_points: int):
+        _check(lib().sks_server_set_active_points(self.h, precision, max_points))
 
     def submit(self, setup: "Setup", precision: int, plane_wave: tuple | None = None, want: bool = True) -> int:
         """plane_wave = (vs, p, f0, sv_amp, sh_amp) or None (the par's boundary files)."""

@@ -140,8 +140,10 @@ def _fmt(v: float) -> str:
     return repr(float(v))
 
 
-def write_case(case: Case, d: str) -> dict:
-    """Write the input files of ``case`` into directory ``d``; returns a summary."""
+def write_case(case: Case, d: str, absolute: bool = False) -> dict:
+    """Write the input files of ``case`` into directory ``d``; returns a summary.
+    absolute: the par file names its inputs by absolute path (readable from
+    any working directory)."""
     os.makedirs(d, exist_ok=True)
     N = case.hpn
     H = case.thickness
@@ -189,12 +191,13 @@ def write_case(case: Case, d: str) -> dict:
         write_plane_wave(os.path.join(d, "greenfile"), os.path.join(d, "shgreenfile"),
                          nx=nx, nz=nz, h=h, nbl=nbl, vs=vs_b, p=case.p, f0=case.f0,
                          dp=dp, nt=nt, sv_amp=case.sv_amp, sh_amp=case.sh_amp)
+    name = (lambda f: os.path.join(os.path.abspath(d), f)) if absolute else (lambda f: f)
     par = {
-        "greenfile": "greenfile", "shgreenfile": "shgreenfile", "raymodel": "raymodel",
-        "semmodel": "semmodel", "nt": nt, "dp": _fmt(dp), "nex": case.nex, "eh": _fmt(case.eh),
+        "greenfile": name("greenfile"), "shgreenfile": name("shgreenfile"), "raymodel": name("raymodel"),
+        "semmodel": name("semmodel"), "nt": nt, "dp": _fmt(dp), "nex": case.nex, "eh": _fmt(case.eh),
         "xmin": "0.0", "nst": case.nst, "sdt": _fmt(case.sdt), "hpn": N, "neh": case.neh,
         "absorb": case.absorb, "readpars": case.readpars, "xbeg": "0.0", "idxplot": 8,
-        "xtrace": case.ntrace, "get_rec": case.get_rec, "rec_file": "rec_file", "plot_trace": 1,
+        "xtrace": case.ntrace, "get_rec": case.get_rec, "rec_file": name("rec_file"), "plot_trace": 1,
         "msource": 0, "check": 0, "flat": case.flat, "nfil": 1,
     }
     if case.semmodel_full:

@@ -139,3 +139,29 @@ def test_request_larger_than_the_budget_fails(reqs):
     info = srv.info(rid)
     assert info["state"] == sks.REQ_FAILED and info["status"] == -6
     srv.close()
+
+
+def test_points_cap_runs_each_form_first_come_first_served(reqs):
+    alone = [_alone(*r) for r in reqs]
+    srv = sks.Server(0, 0, 64)
+    srv.set_tuning(sks.FP32C, *T32)
+    srv.set_tuning(sks.FP64, *T64)
+    srv.set_active_points(sks.FP32C, 1)        # one request of a form at a time
+    srv.set_active_points(sks.FP64, 1)
+    ids = []
+    for d, form, pw, nst in reqs:
+        with chdir(d):
+            ids.append(srv.submit(_setup(d), form, pw))
+    while srv.step():
+        running = [k for k, r in enumerate(ids) if srv.info(r)["state"] == sks.REQ_RUNNING]
+        for f in (sks.FP32C, sks.FP64):
+            assert sum(1 for k in running if reqs[k][1] == f) <= 1
+    for f in (sks.FP32C, sks.FP64):
+        ks = [k for k in range(len(reqs)) if reqs[k][1] == f]
+        done = [srv.info(ids[k])["done_s"] for k in ks]
+        assert done == sorted(done)            # completions in arrival order
+    for k, rid in enumerate(ids):
+        got = srv.result(rid)
+        for c in range(3):
+            assert np.array_equal(got[c], alone[k][c])
+    srv.close()
