@@ -425,6 +425,102 @@ def run_serve(gpu: int, rate: float, nreq: int = 24, seed: int = 7, fp64_frac: f
             "arrival_window_s": float(arrivals[-1]), "quantum_steps": quantum}
 
 
+def run_accuracy(gpu: int, nst: int = FULL_STEPS) -> dict:
+    """The whole anisotropic 3-component solve (24000 steps) in both forms:
+    relative L2 of the FP32C seismograms against the FP64 ones, per
+    component, and the Silver-Chan splitting of both at five interior
+    receivers.  The FP64 form stands in for the FP64 oracle at this size (it
+    matches the oracle to relative L2 <= 1e-10 on the parity cases; the CPU
+    oracle would need hours here).  Boundary records are generated on the
+    device."""
+    import sks
+    import splitting
+    import synth
+    c = synth.config_aniso_3c(nst=nst)
+    c.write_records = False
+    d = tempfile.mkdtemp(prefix="sks_acc_")
+    out = {}
+    try:
+        summ = synth.write_case(c, d)
+        seis = {}
+        for name, prec in (("fp64", sks.FP64), ("fp32c", sks.FP32C)):
+            cwd = os.getcwd()
+            os.chdir(d)
+            try:
+                s = sks.Solver(["par=run.par"], precision=prec, device=gpu)
+            finally:
+                os.chdir(cwd)
+            s.set_boundary_plane_wave(summ["vs"], c.p, c.f0, c.sv_amp, c.sh_amp)
+            t0 = time.perf_counter()
+            seis[name] = s.run(nst)
+            out[f"{name}_solve_s"] = time.perf_counter() - t0
+            s.close()
+        a, b = seis["fp64"], seis["fp32c"]
+        out["rel_l2"] = {k: float(np.linalg.norm(b[i].astype(np.float64) - a[i]) / max(np.linalg.norm(a[i]), 1e-300))
+                         for i, k in enumerate(("u_x", "u_y", "minus_u_z"))}
+        sp = []
+        for r in (50, 75, 100, 125, 150):
+            w = splitting.sks_window(a[0][:, r], c.sdt, 5.0)
+            e64 = splitting.splitting(a[0][:, r], a[1][:, r], c.sdt, w, max_delay=3.0, dphi=0.25)
+            e32 = splitting.splitting(b[0][:, r], b[1][:, r], c.sdt, w, max_delay=3.0, dphi=0.25)
+            sp.append({"receiver": r, "x_km": c.rec_x0 + r * c.rec_dx, "fp64": e64, "fp32c": e32,
+                       "dphi_deg": abs(e32["phi_deg"] - e64["phi_deg"]),
+                       "ddelay_s": abs(e32["delay_s"] - e64["delay_s"])})
+        out.update({"splitting": sp, "max_dphi_deg": max(x["dphi_deg"] for x in sp),
+                    "max_ddelay_s": max(x["ddelay_s"] for x in sp), "steps": nst,
+                    "reference_form": "FP64 form (matches the FP64 oracle to rel L2 <= 1e-10 on the parity cases)",
+                    "splitting_grid": {"dphi_deg": 0.25, "ddelay_s": c.sdt}})
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return out
+
+
+def run_large(gpu: int, steps: int, warmup: int) -> dict:
+    """The single large solve: 1000 x 250 km as 4000 x 1000 elements of 250 m
+    (64,020,001 points), the anisotropic layer of the 3-component case, SV
+    plane wave p = 0.045 s/km, Ricker 2 Hz, dt 1.5 ms, 1001 receivers; FP32C,
+    autotuned, device-resident, boundary records generated on the device.
+    A timed window of `steps` steps (the whole solve is 40000)."""
+    import sks
+    import synth
+    c = synth.config_large()
+    c.write_records = False
+    d = tempfile.mkdtemp(prefix="sks_large_")
+    try:
+        summ = synth.write_case(c, d)
+        cwd = os.getcwd()
+        os.chdir(d)
+        try:
+            t0 = time.perf_counter()
+            s = sks.Solver(["par=run.par"], precision=sks.FP32C, device=gpu)
+            open_s = time.perf_counter() - t0
+        finally:
+            os.chdir(cwd)
+        s.set_boundary_plane_wave(summ["vs"], c.p, c.f0, c.sv_amp, c.sh_amp)
+        info = s.info()
+        lib_run_noout(s, warmup)
+        tun = s.autotune(6)
+        n = lib_run_noout(s, steps)
+        ms = s.last_run_ms()
+        s.reset()
+        lib_run_noout(s, warmup)
+        s.enable_kernel_timing(True)
+        lib_run_noout(s, steps)
+        kt = s.kernel_timing()
+        s.close()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    npts = info["nx"] * info["nz"]
+    km, kc = kt["element"]
+    t_launch = km / max(1, kc) / 1e3
+    return {"points": npts, "steps": n, "ms_per_step": ms / n, "updates_per_s": npts * n / (ms / 1e3),
+            "kernel_ms_per_launch": t_launch * 1e3,
+            "kernel_gbs": npts * BYTES_PER_POINT["fp32c"] / t_launch / 1e9,
+            "kernel_gbs_layout_bytes": npts * LAYOUT_BYTES_PER_POINT["fp32c"] / t_launch / 1e9,
+            "tuning": tun, "device_bytes": info["device_bytes"], "open_s": open_s,
+            "full_solve_s_at_this_rate": 40000 * ms / n / 1e3}
+
+
 def _cpu_worker(args):
     d, nsteps, fp64 = args
     sys.path.insert(0, ROOT)
@@ -490,6 +586,10 @@ def main() -> None:
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-instance workload")
     ap.add_argument("--batch-only", action="store_true", help="only the batched workload (one JSON object)")
     ap.add_argument("--no-serve", action="store_true", help="skip the served workload")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the whole-solve FP32C-vs-FP64 accuracy run")
+    ap.add_argument("--accuracy-only", action="store_true")
+    ap.add_argument("--no-large", action="store_true", help="skip the 64 M-point single solve")
+    ap.add_argument("--large-only", action="store_true")
     ap.add_argument("--serve-rates", default="", help="only the served workload at these arrival rates (req/s), "
                     "one JSON object per rate, e.g. 2,5,10,20")
     ap.add_argument("--serve-requests", type=int, default=24)
@@ -540,6 +640,12 @@ def main() -> None:
     if a.batch_only:
         print(json.dumps({"batch": run_batch(gpu, min(a.steps, 200), a.warmup)}))
         return
+    if a.accuracy_only:
+        print(json.dumps({"accuracy": run_accuracy(gpu)}))
+        return
+    if a.large_only:
+        print(json.dumps({"large": run_large(gpu, min(a.steps, 300), a.warmup)}))
+        return
     if a.serve_rates:
         for r in a.serve_rates.split(","):
             print(json.dumps({"serve": run_serve(gpu, float(r), a.serve_requests)}), flush=True)
@@ -571,6 +677,12 @@ def main() -> None:
     serve = None
     if not a.no_serve:
         serve = run_serve(gpu, 2.0, a.serve_requests)
+    accuracy = None
+    if not a.no_accuracy:
+        accuracy = run_accuracy(gpu)
+    large = None
+    if not a.no_large:
+        large = run_large(gpu, min(a.steps, 300), a.warmup)
     if rank != 0:
         return
     npts = r32["points"]
@@ -633,6 +745,14 @@ def main() -> None:
                              "elements, clipped 100x50..2000x600, element 1-2 km, GLL degree 4; physics drawn as "
                              "in the batched workload; 10 % FP64 requests; 60 s simulated each")
         line["serve"] = serve
+    if accuracy:
+        line["accuracy"] = accuracy
+    if large:
+        large["workload"] = ("single large solve: 4000x1000 elements of 250 m, 64,020,001 points, anisotropic layer "
+                             "(4 %, azimuth 45, tilt 20), Ricker 2 Hz, dt 1.5 ms, 1001 receivers, FP32C")
+        large["roofline"] = {"achieved": large["kernel_gbs"], "peak": peak, "unit": "GB/s",
+                             "frac": large["kernel_gbs"] / peak, "bytes_per_point": BYTES_PER_POINT["fp32c"]}
+        line["large"] = large
     if cpu:
         line["cpu_baseline"] = {"value": cpu["value"], "unit": "GLL-pt updates/s", "cores": 1, "kind": "port",
                                 "sample": f"{a.cpu_steps} time steps of the same mesh, one thread, oracle float "
