@@ -208,6 +208,12 @@ typedef struct {
                                      columns split into near-equal bands   */
     int32_t blocks;               /* CTAs per step (output)                 */
     float   ms_per_step;          /* measured by sks_autotune (output)      */
+    int32_t pipeline;             /* 1: each 64-step chunk is one launch of
+                                     persistent CTAs that take (step, tile)
+                                     pairs in order, a tile starting once its
+                                     neighbours finished the previous step
+                                     (needs zseam = 0, waves = 0); 0: one
+                                     launch per step                        */
 } sks_tuning_t;
 
 int sks_set_tuning(sks_solver *s, const sks_tuning_t *t);

@@ -474,6 +474,7 @@ extern "C" int sks_batch_set_tuning(sks_batch* b, const sks_tuning_t* t)
     if (t->register_cap < 0 || t->register_cap > 2) return set_err(SKS_ERR_ARG, "register_cap=%d: 0, 1 or 2", t->register_cap);
     if (t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
     if (t->waves != 0) return set_err(SKS_ERR_ARG, "a batch uses plain bands (waves=0)");
+    if (t->pipeline != 0) return set_err(SKS_ERR_ARG, "a batch is launched per step (pipeline=0)");
     if (b->running) return set_err(SKS_ERR_STATE, "the batch is running");
     cudaSetDevice(b->device);
     cudaStreamSynchronize(b->stream);
@@ -500,6 +501,7 @@ extern "C" int sks_batch_get_tuning(const sks_batch* b, sks_tuning_t* t)
     t->waves = 0;
     t->blocks = b->grid;
     t->ms_per_step = 0.f;
+    t->pipeline = 0;
     return SKS_OK;
 }
 

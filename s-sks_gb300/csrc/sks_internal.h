@@ -37,7 +37,10 @@ struct sks_solver {
     int64_t launches;
     cudaStream_t stream;
     // geometry: CTA grid of the step kernel (tunable)
-    int NW, ncx, ncz, HZ, nblocks, ZS, CAP, WAVES;
+    int NW, ncx, ncz, HZ, nblocks, ZS, CAP, WAVES, PIPE;
+    int* pipe_ctl;             // pipelined chunks: [claim, error, done[ncx*ncz]] (grow-only)
+    size_t pipe_ctl_n;
+    int pipe_blocks;           // persistent CTAs of a pipelined launch
     int4* items;               // balanced band table (grow-only)
     size_t items_n;
     void* seam_lo;             // band-seam partial forces (grow-only)
@@ -104,7 +107,7 @@ struct Snapshot {
     int step, cur, g_last;
 };
 
-SKS_HIDDEN int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES);
+SKS_HIDDEN int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES, int PIPE = 0);
 SKS_HIDDEN int run_chunk(sks_solver* s, int it0, int n);
 SKS_HIDDEN int snap_take(sks_solver* s, Snapshot& S);
 SKS_HIDDEN int snap_restore(sks_solver* s, const Snapshot& S);

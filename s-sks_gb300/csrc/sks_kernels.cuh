@@ -108,14 +108,23 @@ __device__ __forceinline__ int64_t ucomp(int c, int64_t g, int64_t np)
     return c == 1 ? 2 * np + g : 2 * g + (c == 2 ? 1 : 0);
 }
 
-template <typename T>
+// loads of values other CTAs of the same launch may have written (CG: through
+// L2 only, never a stale L1 line) or that no one writes during the launch
+template <bool CG, typename X>
+__device__ __forceinline__ X ldv(const X* p)
+{
+    if constexpr (CG) return __ldcg(p);
+    else return *p;
+}
+
+template <typename T, bool CG = false>
 __device__ __forceinline__ void load_u(const T* __restrict__ U, int np, int g, T out[3])
 {
     using V = typename Pair<T>::type;
-    const V p = reinterpret_cast<const V*>(U)[g];
+    const V p = ldv<CG>(reinterpret_cast<const V*>(U) + g);
     out[0] = p.x;
     out[2] = p.y;
-    out[1] = U[2 * np + g];
+    out[1] = ldv<CG>(U + 2 * np + g);
 }
 
 template <typename T>
@@ -198,15 +207,15 @@ struct Aux {
     T b[LF ? 3 : 1];   // FP32: Kahan compensation
 };
 
-template <typename T, bool LF>
+template <typename T, bool LF, bool CG = false>
 __device__ __forceinline__ void load_aux(const Field<T>& F, int64_t np, int64_t g, Aux<T, LF>& x)
 {
     if constexpr (!LF) {
-        load_u<T>(F.un, (int)np, (int)g, x.a);
+        load_u<T, CG>(F.un, (int)np, (int)g, x.a);
     } else {
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            const float2 v = reinterpret_cast<const float2*>(F.dv)[c * np + g];
+            const float2 v = ldv<CG>(reinterpret_cast<const float2*>(F.dv) + c * np + g);
             x.a[c] = v.x;
             x.b[c] = v.y;
         }
@@ -328,7 +337,7 @@ struct TileShared {
 
 // One CTA tile: element column cx (S = 6*NW-1 owned elements), band cz of
 // element rows [ez0, ez1).
-template <typename T, bool ANISO, bool LF, int NW, bool ZS>
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, bool CG = false>
 __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, const Coef<T>& k, int cx, int cz,
                                           int ez0, int ez1, TileShared<T, NW>& sh)
 {
@@ -374,7 +383,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
 #pragma unroll
         for (int b = 0; b < NP; b++) {
             const int g = o + b * nx;
-            load_u<T>(F.uc, np, g, u[b]);
+            load_u<T, CG>(F.uc, np, g, u[b]);
             m[b] = F.mid[g];
         }
     }
@@ -389,14 +398,14 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
 #pragma unroll
             for (int b = 1; b < NP; b++) {
                 const int g = o + b * nx;
-                load_u<T>(F.uc, np, g, u[b]);
+                load_u<T, CG>(F.uc, np, g, u[b]);
                 m[b] = F.mid[g];
             }
         }
         Aux<T, LF> aux[N];
         if (!halo && own_x) {
 #pragma unroll
-            for (int b = 0; b < N; b++) load_aux<T, LF>(F, G.np, (int64_t)(ez * N + b) * nx + ix, aux[b]);
+            for (int b = 0; b < N; b++) load_aux<T, LF, CG>(F, G.np, (int64_t)(ez * N + b) * nx + ix, aux[b]);
         }
         T kk[NP][3];
 #pragma unroll
@@ -528,7 +537,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
         if (ez1 == G.nez) {
             if (own_x) {
                 Aux<T, LF> x;
-                load_aux<T, LF>(F, G.np, (int64_t)iz * nx + ix, x);
+                load_aux<T, LF, CG>(F, G.np, (int64_t)iz * nx + ix, x);
                 finish_point<T, LF>(F, G, k, ix, iz, u[N], kt, rinvN, wxi, k.winv[0], x, pfl);
             }
         } else {
@@ -550,7 +559,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
                     for (int c = 0; c < 3; c++)
                         K[c] = (lft[c] + __ldcg(hi + c)) + (kc[c] + __ldcg(hi + 3 + c));
                     Aux<T, LF> x;
-                    load_aux<T, LF>(F, G.np, (int64_t)iz * nx + ix, x);
+                    load_aux<T, LF, CG>(F, G.np, (int64_t)iz * nx + ix, x);
                     finish_point<T, LF>(F, G, k, ix, iz, u[N], K, rinvN, wxi, k.winv2, x, pfl);
                 }
             }
@@ -654,6 +663,108 @@ k_step_batch(const BatchMember<T>* __restrict__ mem, const BatchState* __restric
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined chunk: the steps of a chunk of one mesh in one launch.  Persistent
+// CTAs claim (step, tile) pairs in step-major order from a counter; tile t of
+// step s waits until the tiles around it (its 3 x 3 neighbourhood of the band
+// grid, all the tiles whose points it reads or whose reads of its points it
+// would overwrite) have finished step s-1, then runs the same step_tile as a
+// single-step launch, loading the wavefield through L2.  A CTA only waits on
+// tiles claimed before its own, by CTAs that were running then, so the waits
+// end; each wait is still bounded, and a wait that runs out sets the error
+// flag, which stops every CTA.  One launch replaces a chunk of step launches:
+// the per-launch ramp and tail of a small mesh are paid once per chunk.
+struct PipeCtl {
+    int* claim;            // next (step, tile) index
+    int* done;             // per tile: steps of the chunk it has finished
+    int* error;            // set when a wait ran out
+};
+
+struct PipeChunk {
+    const void* U[2];      // displacement buffers; step it reads U[(it-1)&1]
+    int it0, n;            // the chunk's first step (>= 1) and its length
+    int nt_sem;            // steps that inject
+    int nline;
+    const void* dl;        // [n+1][nline][3] increments of the chunk (row s: step it0+s)
+    float* seis;           // [n][3][ntrace] seismogram rows of the chunk
+};
+
+__device__ __forceinline__ int ld_acquire(const int* p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(int* p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+constexpr int PIPE_SPIN_LIMIT = 1 << 22;   // polls of one wait (with 128 ns sleeps: about a second)
+
+template <typename T, bool ANISO, bool LF, int NW, int CAP>
+__global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
+k_step_pipe(Field<T> F, Geo<T> G, Coef<T> k, PipeChunk C, PipeCtl ctl)
+{
+    __shared__ TileShared<T, NW> sh;
+    __shared__ __align__(16) Field<T> sF;
+    __shared__ int s_claim, s_step, s_next, s_fail;
+    const int ntiles = G.ncx * G.ncz;
+    const int total = C.n * ntiles;
+    if (threadIdx.x == 0) { sF = F; s_step = -1; s_claim = atomicAdd(ctl.claim, 1); }
+    __syncthreads();
+    for (;;) {
+        const int c = s_claim;
+        if (c >= total) break;
+        const int st = c / ntiles, t = c - st * ntiles;
+        const int cz = t / G.ncx, cx = t - cz * G.ncx;
+        if (threadIdx.x < 32) {
+            // lanes 0..8 wait, each for one tile of the 3 x 3 neighbourhood to
+            // finish step st-1; lane 0 claims the next pair meanwhile (this CTA
+            // takes it up after the current one)
+            int next = 0;
+            if (threadIdx.x == 0) { next = atomicAdd(ctl.claim, 1); s_fail = 0; }
+            int fail = 0;
+            if (st > 0 && threadIdx.x < 9) {
+                const int z = cz + (int)threadIdx.x / 3 - 1, x = cx + (int)threadIdx.x % 3 - 1;
+                if (z >= 0 && z < G.ncz && x >= 0 && x < G.ncx) {
+                    const int* f = ctl.done + z * G.ncx + x;
+                    int spins = 0;
+                    while (ld_acquire(f) < st) {
+                        if (++spins > PIPE_SPIN_LIMIT || ld_acquire(ctl.error)) { fail = 1; break; }
+                        __nanosleep(128);
+                    }
+                }
+            }
+            fail = __any_sync(0xffffffffu, fail);
+            if (threadIdx.x == 0) {
+                s_next = next;
+                if (fail) { atomicExch(ctl.error, 1); s_fail = 1; }
+                else if (st != s_step) {
+                    const int it = C.it0 + st;
+                    sF.uc = (const T*)C.U[(it - 1) & 1];
+                    sF.un = (T*)C.U[it & 1];
+                    sF.dline = (const T*)C.dl + (size_t)st * C.nline * 3;
+                    sF.inject_next = it + 1 < C.nt_sem ? 1 : 0;
+                    sF.seis_row = C.seis + (size_t)st * 3 * F.ntrace;
+                    s_step = st;
+                }
+            }
+        }
+        __syncthreads();
+        if (s_fail) break;
+        step_tile<T, ANISO, LF, NW, false, true>(sF, G, k, cx, cz, cz * G.HZ, min(cz * G.HZ + G.HZ, G.nez), sh);
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            st_release(ctl.done + t, st + 1);
+            s_claim = ld_acquire(ctl.error) ? total : s_next;
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace sks
 
 namespace sks {
@@ -669,6 +780,12 @@ cudaError_t launch_batch_f64(const StepVariant& v, bool aniso, int blocks, cudaS
                              const BatchState* state, const int4* items, const BatchHeader* hdr, int j,
                              const Coef<double>& k);
 int batch_occupancy_f32(const StepVariant& v, bool aniso);
+cudaError_t launch_pipe_f32(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<float>& F,
+                            const Geo<float>& G, const Coef<float>& k, const PipeChunk& C, const PipeCtl& ctl);
+cudaError_t launch_pipe_f64(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<double>& F,
+                            const Geo<double>& G, const Coef<double>& k, const PipeChunk& C, const PipeCtl& ctl);
+int pipe_occupancy_f32(const StepVariant& v, bool aniso);
+int pipe_occupancy_f64(const StepVariant& v, bool aniso);
 int batch_occupancy_f64(const StepVariant& v, bool aniso);
 // resident CTAs per SM of a variant (cudaOccupancyMaxActiveBlocksPerMultiprocessor)
 int step_occupancy_f32(const StepVariant& v, bool aniso);

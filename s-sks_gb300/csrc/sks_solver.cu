@@ -132,7 +132,8 @@ void free_device(sks_solver* s)
 {
     void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc,
                   s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seisbuf[0], s->seisbuf[1], s->G, s->Dl, s->rec_psv, s->rec_sh,
-                  s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt, s->items, s->seis_full};
+                  s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt, s->items, s->seis_full,
+                  s->pipe_ctl};
     for (void* p : ps)
         if (p) cudaFree(p);
     s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = nullptr;
@@ -142,6 +143,8 @@ void free_device(sks_solver* s)
     s->seam_lo = s->seam_hi = nullptr; s->seam_cnt = nullptr; s->seam_bytes = 0; s->seam_cnt_n = 0;
     s->items = nullptr; s->items_n = 0;
     s->seis_full = nullptr;
+    s->pipe_ctl = nullptr;
+    s->pipe_ctl_n = 0;
 }
 
 // per-kernel-class timing: an event pair around each launch when enabled
@@ -253,12 +256,14 @@ int upload_tables(sks_solver* s)
 // waves CTAs, each column split into bands of near-equal height, so every
 // SM carries the same work (no partly filled last wave).  The band-seam
 // buffers grow to fit and their counters restart at 0.
-int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES)
+int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES, int PIPE)
 {
+    if (PIPE && (ZS || WAVES)) return set_err(SKS_ERR_ARG, "pipeline=1 needs zseam=0 and waves=0");
     s->NW = NW;
     s->ZS = ZS;
     s->CAP = CAP;
     s->WAVES = WAVES;
+    s->PIPE = PIPE;
     s->ncx = (s->m.nex + (TEX * NW - 1) - 1) / (TEX * NW - 1);
     const int nez = s->m.nez;
     if (WAVES <= 0) {
@@ -296,6 +301,22 @@ int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES)
         s->ncz = maxb;
         s->HZ = (nez + maxb - 1) / maxb;
         s->nblocks = (int)it.size();
+    }
+    if (PIPE) {
+        const StepVariant pv{NW, 0, CAP};
+        const int occ = s->precision == SKS_FP64 ? pipe_occupancy_f64(pv, s->m.anisotropic != 0)
+                                                 : pipe_occupancy_f32(pv, s->m.anisotropic != 0);
+        s->pipe_blocks = std::max(1, std::min(s->sms * occ, s->ncx * s->ncz));
+        const size_t need = 2 + (size_t)s->ncx * s->ncz;
+        if (need > s->pipe_ctl_n) {
+            if (s->pipe_ctl) { cudaFree(s->pipe_ctl); s->device_bytes -= 4 * (int64_t)s->pipe_ctl_n; }
+            s->pipe_ctl = nullptr;
+            s->pipe_ctl_n = 0;
+            CK(cudaMalloc(&s->pipe_ctl, need * sizeof(int)));
+            s->pipe_ctl_n = need;
+            s->device_bytes += 4 * (int64_t)need;
+        }
+        CK(cudaMemsetAsync(s->pipe_ctl, 0, need * sizeof(int), s->stream));
     }
     if (!ZS) return SKS_OK;
     const size_t el = s->precision == SKS_FP64 ? sizeof(double) : sizeof(float);
@@ -379,6 +400,46 @@ int step0_impl(sks_solver* s, const double* G0, const double* G1, float* seis_ro
     return SKS_OK;
 }
 
+// steps it1 .. it1+cnt-1 (it1 >= 1) of the chunk in one pipelined launch;
+// i0 = the first of them within the chunk (its row of Dl and of the seismograms)
+template <typename T, bool LF>
+int pipe_impl(sks_solver* s, int it1, int cnt, int i0)
+{
+    const sks_model& m = s->m;
+    const size_t nline = (size_t)(m.nx - s->nbl) + (m.nz - s->nbl - 1);
+    Field<T> F = make_field<T>(s);
+    Geo<T> G = make_geo<T>(s);
+    static thread_local Coef<T> k;
+    k = make_coef<T>(m);
+    PipeChunk C;
+    C.U[0] = s->U[0];
+    C.U[1] = s->U[1];
+    C.it0 = it1;
+    C.n = cnt;
+    C.nt_sem = m.nt_sem;
+    C.nline = (int)nline;
+    C.dl = (const T*)s->Dl + (size_t)i0 * nline * 3;
+    C.seis = s->seis + (size_t)i0 * 3 * m.ntrace;
+    const PipeCtl ctl{s->pipe_ctl, s->pipe_ctl + 2, s->pipe_ctl + 1};
+    const int ntiles = s->ncx * s->ncz;
+    CK(cudaMemsetAsync(ctl.claim, 0, sizeof(int), s->stream));
+    CK(cudaMemsetAsync(ctl.done, 0, sizeof(int) * (size_t)ntiles, s->stream));
+    {
+        KTimer t(s, SKS_KC_ELEMENT);
+        const StepVariant v{s->NW, 0, s->CAP};
+        cudaError_t e;
+        if (sizeof(T) == 4)
+            e = launch_pipe_f32(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<float>*)&F,
+                                *(const Geo<float>*)&G, *(const Coef<float>*)&k, C, ctl);
+        else
+            e = launch_pipe_f64(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<double>*)&F,
+                                *(const Geo<double>*)&G, *(const Coef<double>*)&k, C, ctl);
+        CK(e);
+    }
+    s->cur = (it1 + cnt - 1) & 1;
+    return SKS_OK;
+}
+
 int run_chunk(sks_solver* s, int it0, int n)
 {
     const sks_model& m = s->m;
@@ -413,6 +474,12 @@ int run_chunk(sks_solver* s, int it0, int n)
     if (m.ntrace > 0) CK(cudaMemsetAsync(s->seis, 0, sizeof(float) * (size_t)n * 3 * m.ntrace, st));
     for (int i = 0; i < n; i++) {
         const int it = it0 + i;
+        if (s->PIPE && it > 0) {        // the rest of the chunk as one pipelined launch
+            const int rc = s->precision == SKS_FP64 ? pipe_impl<double, false>(s, it, n - i, i)
+                                                    : pipe_impl<float, true>(s, it, n - i, i);
+            if (rc) return rc;
+            break;
+        }
         const double* Gcur = s->G + (size_t)(i + 1) * L;
         const double* Gnext = s->G + (size_t)(i + 2) * L;
         const size_t nline = (size_t)(m.nx - s->nbl) + (m.nz - s->nbl - 1);
@@ -689,6 +756,7 @@ extern "C" int sks_run(sks_solver* s, int32_t nsteps, float* su, float* sv, floa
         CK(cudaEventCreate(&s->run_ev[0]));
         CK(cudaEventCreate(&s->run_ev[1]));
     }
+    if (s->PIPE) CK(cudaMemsetAsync(s->pipe_ctl + 1, 0, sizeof(int), s->stream));
     CK(cudaEventRecord(s->run_ev[0], s->stream));
     while (s->step < end) {
         const int n = std::min(s->chunk, end - s->step);
@@ -717,6 +785,11 @@ extern "C" int sks_run(sks_solver* s, int32_t nsteps, float* su, float* sv, floa
     CK(cudaStreamSynchronize(s->stream));
     CK(cudaStreamSynchronize(s->copy_stream));
     s->slot_busy[0] = s->slot_busy[1] = false;
+    if (s->PIPE) {
+        int err = 0;
+        CK(cudaMemcpy(&err, s->pipe_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) return set_err(SKS_ERR_CUDA, "pipelined step: a wait for neighbouring tiles ran out");
+    }
     {
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, s->run_ev[0], s->run_ev[1]));
@@ -798,7 +871,8 @@ extern "C" int sks_set_tuning(sks_solver* s, const sks_tuning_t* t)
     if (t->waves == 0 && t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
     if (t->waves < 0 || t->waves > 64) return set_err(SKS_ERR_ARG, "waves=%d: 0..64", t->waves);
     if (s->batch) return set_err(SKS_ERR_STATE, "the solver is a member of a batch: tune the batch");
-    return set_grid(s, t->warps_per_block, t->band_rows, t->zseam ? 1 : 0, t->register_cap, t->waves);
+    if (t->pipeline != 0 && t->pipeline != 1) return set_err(SKS_ERR_ARG, "pipeline=%d: 0 or 1", t->pipeline);
+    return set_grid(s, t->warps_per_block, t->band_rows, t->zseam ? 1 : 0, t->register_cap, t->waves, t->pipeline);
 }
 
 extern "C" int sks_get_tuning(const sks_solver* s, sks_tuning_t* t)
@@ -809,8 +883,9 @@ extern "C" int sks_get_tuning(const sks_solver* s, sks_tuning_t* t)
     t->zseam = s->ZS;
     t->waves = s->WAVES;
     t->register_cap = s->CAP;
-    t->blocks = s->nblocks;
+    t->blocks = s->PIPE ? s->pipe_blocks : s->nblocks;
     t->ms_per_step = 0.f;
+    t->pipeline = s->PIPE;
     return SKS_OK;
 }
 
@@ -873,31 +948,34 @@ extern "C" int sks_autotune(sks_solver* s, int32_t steps, sks_tuning_t* best)
     s->timing = 0;
     const int nws[] = {2, 4};
     const int hzs[] = {4, 6, 8, 12};
-    sks_tuning_t b = {s->NW, s->HZ, s->ZS, s->CAP, s->WAVES, s->nblocks, 1e30f};
-    // fixed band heights, then balanced partitions of 1..3 waves
+    sks_tuning_t b = {s->NW, s->HZ, s->ZS, s->CAP, s->WAVES, s->nblocks, 1e30f, s->PIPE};
+    // fixed band heights, then balanced partitions of 1..3 waves; pipelined
+    // chunks with fixed band heights
     const int nhz = (int)(sizeof hzs / sizeof hzs[0]);
+    for (int pipe = 0; pipe < 2; pipe++)
     for (int nw : nws)
         for (int zs = 0; zs < 2; zs++)
           for (int cap = 0; cap < 3; cap++)
             for (int cand = 0; cand < nhz + 3; cand++) {
                 const int hz = cand < nhz ? hzs[cand] : 0, wv = cand < nhz ? 0 : cand - nhz + 1;
                 if (wv == 0 && hz > m.nez && hz != hzs[0]) continue;
+                if (pipe && (zs || wv)) continue;
                 if ((rc = snap_restore(s, snap))) break;
-                if ((rc = set_grid(s, nw, hz, zs, cap, wv))) break;
+                if ((rc = set_grid(s, nw, hz, zs, cap, wv, pipe))) break;
                 // one untimed step, then the timed ones
                 rc = sks_run(s, 1, nullptr, nullptr, nullptr);
                 if (rc < 0) break;
                 rc = sks_run(s, steps, nullptr, nullptr, nullptr);
                 if (rc < 0) break;
                 const float ms = (float)(s->last_run_ms / rc);
-                if (ms < b.ms_per_step) b = {nw, s->HZ, zs, cap, wv, s->nblocks, ms};
+                if (ms < b.ms_per_step) b = {nw, s->HZ, zs, cap, wv, pipe ? s->pipe_blocks : s->nblocks, ms, pipe};
                 rc = SKS_OK;
             }
     const int rc2 = snap_restore(s, snap);
     cudaStreamSynchronize(s->stream);
     for (void* p : snap.dev) cudaFree(p);
     s->timing = old_timing;
-    const int rc3 = set_grid(s, b.warps_per_block, b.band_rows, b.zseam, b.register_cap, b.waves);
+    const int rc3 = set_grid(s, b.warps_per_block, b.band_rows, b.zseam, b.register_cap, b.waves, b.pipeline);
     if (rc < 0) return rc;
     if (rc3) return rc3;
     if (rc2) return rc2;

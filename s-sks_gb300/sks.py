@@ -80,7 +80,7 @@ class PlaneWave(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("warps_per_block", C.c_int32), ("band_rows", C.c_int32), ("zseam", C.c_int32),
                 ("register_cap", C.c_int32), ("waves", C.c_int32), ("blocks", C.c_int32),
-                ("ms_per_step", C.c_float)]
+                ("ms_per_step", C.c_float), ("pipeline", C.c_int32)]
 
     def asdict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -301,8 +301,8 @@ class Solver:
         return t.asdict()
 
     def set_tuning(self, warps_per_block: int, band_rows: int, zseam: int = 1, register_cap: int = 0,
-                   waves: int = 0):
-        t = Tuning(warps_per_block, band_rows, zseam, register_cap, waves, 0, 0.0)
+                   waves: int = 0, pipeline: int = 0):
+        t = Tuning(warps_per_block, band_rows, zseam, register_cap, waves, 0, 0.0, pipeline)
         _check(lib().sks_set_tuning(self.h, C.byref(t)))
 
     def autotune(self, steps: int = 8) -> dict:

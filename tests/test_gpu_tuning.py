@@ -1,9 +1,10 @@
 """GPU: every tuning of the step kernel gives bit-identical seismograms, and the
 autotuner leaves the solve where it found it.
 
-The CTA grid (warps per CTA, band height, band-seam method, register cap) changes which CTA computes
-an element, never the arithmetic: a halo element is recomputed with the same
-inputs and code, and each point's force is summed in the same order.
+The CTA grid (warps per CTA, band height, band-seam method, register cap,
+pipelined chunks) changes which CTA computes an element and when, never the
+arithmetic: a halo element is recomputed with the same inputs and code, and
+each point's force is summed in the same order.
 """
 import numpy as np
 import pytest
@@ -48,19 +49,20 @@ def _run(d, prec, nst, tuning=None, autotune=False):
         return out, got, s.tuning()
 
 
-TUNINGS = [(nw, hz, zs, cap, wv) for nw in (2, 4) for hz in (1, 3, 23) for zs in (0, 1) for cap in (0, 1, 2)
-           for wv in (0,)] + [(nw, 4, zs, 1, wv) for nw in (2, 4) for zs in (0, 1) for wv in (1, 2, 5)]
+TUNINGS = ([(nw, hz, zs, cap, wv, 0) for nw in (2, 4) for hz in (1, 3, 23) for zs in (0, 1) for cap in (0, 1, 2)
+            for wv in (0,)] + [(nw, 4, zs, 1, wv, 0) for nw in (2, 4) for zs in (0, 1) for wv in (1, 2, 5)]
+           + [(nw, hz, 0, cap, 0, 1) for nw in (2, 4) for hz in (1, 3, 23) for cap in (0, 1, 2)])
 
 
 @pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])
 def test_all_tunings_bit_identical(case, prec):
     d, c = case
-    ref, _, _ = _run(d, prec, c.nst, tuning=(4, 8, 1, 0, 0))
+    ref, _, _ = _run(d, prec, c.nst, tuning=(4, 8, 1, 0, 0, 0))
     assert max(np.abs(x).max() for x in ref) > 0.1
     for t in TUNINGS:
         out, _, used = _run(d, prec, c.nst, tuning=t)
-        got = (used["warps_per_block"], used["zseam"], used["register_cap"], used["waves"])
-        assert got == (t[0], t[2], t[3], t[4])
+        got = (used["warps_per_block"], used["zseam"], used["register_cap"], used["waves"], used["pipeline"])
+        assert got == (t[0], t[2], t[3], t[4], t[5])
         if t[4] == 0:
             assert used["band_rows"] == t[1]
         for i in range(3):
