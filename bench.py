@@ -161,7 +161,7 @@ def run_form(d: str, precision: int, steps: int, warmup: int, gpu: int, clocks: 
         s.load_boundary_files()
         info = s.info()
         lib_run_noout(s, warmup)
-        tuning = s.autotune(8)
+        tuning = s.autotune(16)
         l0 = s.launches()
         ck = Clocks(gpu) if clocks else None
         if ck:
