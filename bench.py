@@ -554,21 +554,33 @@ def cpu_rate(d: str, nsteps: int, procs: int) -> dict:
 
 # ---------------------------------------------------------------- main
 def _dist():
+    """Replicas: one process per GPU under torchrun (NCCL), or gloo without GPUs."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws > 1:
+        import torch
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
         return dist, int(os.environ["RANK"]), ws, int(os.environ.get("LOCAL_RANK", "0"))
     return None, 0, 1, 0
 
 
 def _max_over_ranks(dist, v: float) -> float:
+    """The largest of the ranks' values (every rank gets it)."""
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_rate(dist, world: int, units_per_rank: float, ms: float) -> tuple[float, float]:
+    """Whole-job rate of N independent replicas (weak scaling): every rank did
+    units_per_rank units; the job took the slowest rank's time.  Returns
+    (max ms over ranks, units per second of the whole job)."""
+    ms_max = _max_over_ranks(dist, ms)
+    return ms_max, world * units_per_rank / (ms_max / 1e3)
 
 
 def main() -> None:
@@ -687,7 +699,7 @@ def main() -> None:
     if rank != 0:
         return
     npts = r32["points"]
-    value = world * npts * r32["steps"] / (ms32 / 1e3)
+    value = world * npts * r32["steps"] / (ms32 / 1e3)      # ms32: max over ranks (replica_rate)
     v64 = world * npts * r64["steps"] / (ms64 / 1e3)
     peak, peak_kind = _peaks()
     # roofline of the dominant kernel (the fused step kernel): algorithmic
