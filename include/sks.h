@@ -106,6 +106,17 @@ int sks_set_boundary_plane_wave(sks_solver *s, const sks_plane_wave_t *pw);
  * NULL.  Returns the number of steps taken (>= 0) or a negative status. */
 int sks_run(sks_solver *s, int32_t nsteps, float *seis_u, float *seis_v, float *seis_w);
 
+/* Snapshots (plot_snap=1 with startsnap / incresnap in the par words, as in
+ * sem2d_psvsh.c:149-150,202-204,483-510): the step startsnap + k*incresnap
+ * (k < 26) records (u_x, u_y) of every second grid point, the field the
+ * receivers see (after the update, before the next injection), like the
+ * reference's snapshot() (sem2d.c:1667-1683), which writes them as text file
+ * out<k+1>.  out receives dims[0]*dims[1]*2 floats, [ix/2][iz/2][2] (ix outer,
+ * iz inner, as the file lists them); dims = {(nx+1)/2, (nz+1)/2}.  Returns
+ * the snapshot's step, or SKS_ERR_STATE when the run has not taken it (or
+ * plot_snap=0).  sks_run takes snapshots; batch members cannot have them. */
+int sks_snapshot(const sks_solver *s, int32_t k, float *out, int32_t *dims);
+
 /* The boundary increments the time loop injects, as GRT_Interface4 adds them
  * (sem2d_psvsh.c:2076-2111) from the interpolated traces of interpl()
  * (interpl.c:16-54): for each step it in [it0, it0+nsteps), the FP64
@@ -298,7 +309,8 @@ void sks_batch_destroy(sks_batch *b);
  * 8 Mi points FP64, 24 Mi FP32C, about twice what fills the GPU; a larger
  * request runs alone), opens them on the device, and runs every admitted
  * request of a form as a member of that form's batch, a quantum of steps per
- * round, the FP32C and FP64 batches on their own streams.
+ * round, the FP32C and FP64 batches on their own streams (FP32C at the higher
+ * stream priority: its quanta are short, FP64's long).
  * Requests join and leave between quanta; wavefields stay on the device; a
  * finished request's seismograms are copied once into the caller's arrays
  * and its device memory is freed.  Each result equals the same request run

@@ -47,6 +47,7 @@ def _lib(fp64: bool) -> C.CDLL:
         L.oracle_material.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.oracle_mass.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.oracle_receivers.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+        L.oracle_snapshot.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_int)]
         L.oracle_destroy.argtypes = [C.c_void_p]
         L.oracle_destroy.restype = None
         L.oracle_last_error.restype = C.c_char_p
@@ -90,6 +91,14 @@ class Oracle:
         off = np.zeros(max(1, self.ntrace), np.int64)
         self.L.oracle_receivers(self.h, off.ctypes.data_as(C.POINTER(C.c_longlong)))
         return off[: self.ntrace]
+
+    def snapshot(self, k: int):
+        """(step, [nx/2][nz/2][2] float32) of snapshot k (plot_snap), or None."""
+        dims = (C.c_int * 2)()
+        self.L.oracle_snapshot(self.h, k, None, dims)
+        out = np.zeros((dims[0], dims[1], 2), np.float32)
+        st = self.L.oracle_snapshot(self.h, k, out.ctypes.data_as(C.POINTER(C.c_float)), dims)
+        return None if st < 0 else (st, out)
 
     def close(self):
         if self.h:

@@ -177,7 +177,14 @@ typedef struct {
     FILE *gf, *shf;
     /* wavefield */
     Vec3 *u, *u0, *u1, *K;
+    /* snapshots (plot_snap, sem2d_psvsh.c:483-510): every second point of
+     * (u[0], u[1]) at steps ist + k*incre, k < NSNAP */
+    int plot_snap, ist, incre, nxs, nzs;
+    float *snaps;               /* [NSNAP][nxs][nzs][2] */
+    int snap_taken[32];
 } Oracle;
+
+#define NSNAP 26
 
 /* ---------------- ray model (semsyn/src/readmodel.c:43-109) ------------- */
 typedef struct {
@@ -803,7 +810,11 @@ static int oracle_setup(Oracle *o, int argc, char **argv)
     memset(o, 0, sizeof *o);
     o->flat = 1; o->nfil = 1; o->hpn = 5; o->absorb = 1; o->readpars = 1; o->neh = 1;
     o->xtrace = 20; o->idxplot = 20;
+    o->ist = 100; o->incre = 50;
     if (par_parse(&pl, argc, argv)) { free(pl.e); return ORC_ERR; }
+    GETI("plot_snap", o->plot_snap, 0);
+    GETI("startsnap", o->ist, 0);
+    GETI("incresnap", o->incre, 0);
     GETI("flat", o->flat, 0);
     GETI("psv_only", o->psv_only, 0);
     GETI("semmodel_full", o->semmodel_full, 0);
@@ -917,7 +928,23 @@ static void oracle_free(Oracle *o)
     free(o->mesh); free(o->Mass); free(o->Mass_dt2); free(o->Ab);
     free(o->u); free(o->u0); free(o->u1); free(o->K); free(o->rec_off);
     free(o->grtuw); free(o->grtuw0); free(o->grtv); free(o->grtv0); free(o->sy); free(o->sy_sh);
+    free(o->snaps);
     memset(o, 0, sizeof *o);
+}
+
+/* snapshot (sem2d.c:1667-1683): ix = 0, 2, ... outer, iz = 0, 2, ... inner */
+static void take_snapshot(Oracle *o, int k)
+{
+    int ix, iz;
+    float *out = o->snaps + (size_t)k * o->nxs * o->nzs * 2;
+    for (ix = 0; ix < o->nx; ix += 2)
+        for (iz = 0; iz < o->nz; iz += 2) {
+            const Vec3 *p = &o->u[(size_t)iz * o->nx + ix];
+            float *q = out + ((size_t)(ix / 2) * o->nzs + iz / 2) * 2;
+            q[0] = (float)p->u[0];
+            q[1] = (float)p->u[1];
+        }
+    o->snap_taken[k] = 1;
 }
 
 static void record(const Oracle *o, float *su, float *sv, float *sw)
@@ -958,6 +985,16 @@ static int oracle_steps(Oracle *o, int it_begin, int it_end, float *su, float *s
             size_t off = (size_t)(it - it_begin) * o->ntrace;
             record(o, su + off, sv + off, sw + off);
         }
+        if (o->plot_snap && o->incre != 0 && it >= o->ist && (it - o->ist) % o->incre == 0 &&
+            (it - o->ist) / o->incre < NSNAP) {
+            if (!o->snaps) {
+                o->nxs = (o->nx + 1) / 2;
+                o->nzs = (o->nz + 1) / 2;
+                o->snaps = (float *)calloc((size_t)NSNAP * o->nxs * o->nzs * 2, sizeof(float));
+                if (!o->snaps) { free(tmp); return fail("cannot allocate snapshots", NULL); }
+            }
+            take_snapshot(o, (it - o->ist) / o->incre);
+        }
     }
     free(tmp);
     return ORC_OK;
@@ -992,6 +1029,19 @@ int oracle_run(void *hv, int nsteps, float *su, float *sv, float *sw)
     h->it = e;
     return nsteps;
 }
+/* snapshot k (the step ist + k*incre) as [nxs][nzs][2]; returns its step, or
+ * -1 when it was not taken; dims = {nxs, nzs} */
+int oracle_snapshot(void *hv, int k, float *out, int *dims)
+{
+    OracleHandle *h = (OracleHandle *)hv;
+    const Oracle *o = &h->o;
+    dims[0] = (o->nx + 1) / 2;
+    dims[1] = (o->nz + 1) / 2;
+    if (k < 0 || k >= NSNAP || !o->snaps || !o->snap_taken[k]) return -1;
+    if (out) memcpy(out, o->snaps + (size_t)k * o->nxs * o->nzs * 2, sizeof(float) * (size_t)o->nxs * o->nzs * 2);
+    return o->ist + k * o->incre;
+}
+
 /* per-point material as 15 coefficients + rho and the Stacey/mass arrays, for set-up checks */
 int oracle_material(void *hv, double *out16)
 {
@@ -1061,6 +1111,21 @@ int main(int argc, char **argv)
         }
     }
     if (fu) { fclose(fu); fclose(fw); fclose(fv); }
+    for (it = 0; it < NSNAP && o.snaps; it++) {
+        /* the reference's text snapshot: "%d %d %e %e\n" (sem2d.c:1677-1681) */
+        char name[16];
+        FILE *f;
+        int ix, iz;
+        if (!o.snap_taken[it]) continue;
+        snprintf(name, sizeof name, "out%d", it + 1);
+        if (!(f = fopen(name, "wt"))) { fprintf(stderr, "oracle: cannot open %s\n", name); return 1; }
+        for (ix = 0; ix < o.nx; ix += 2)
+            for (iz = 0; iz < o.nz; iz += 2) {
+                const float *q = o.snaps + (((size_t)it * o.nxs + ix / 2) * o.nzs + iz / 2) * 2;
+                fprintf(f, "%d %d %e %e\n", ix, iz, q[0], q[1]);
+            }
+        fclose(f);
+    }
     free(su); free(sv); free(sw);
     oracle_free(&o);
     return 0;

@@ -70,6 +70,29 @@ int main(int argc, char **argv)
         step += n;
     }
     if (fu) { fclose(fu); fclose(fw); fclose(fv); }
+    {
+        /* snapshots as the reference's snapshot() writes them (sem2d.c:1667-1683) */
+        int32_t dims[2] = {0, 0};
+        float *buf;
+        int k;
+        sks_snapshot(s, 0, NULL, dims);
+        buf = (float *)malloc(sizeof(float) * 2 * ((size_t)dims[0] * dims[1] + 1));
+        for (k = 0; k < 26 && buf; k++) {
+            char name[16];
+            FILE *f;
+            int ix, iz;
+            if (sks_snapshot(s, k, buf, dims) < 0) continue;
+            snprintf(name, sizeof name, "out%d", k + 1);
+            if (!(f = fopen(name, "wt"))) { fprintf(stderr, "%s: cannot open %s\n", prog, name); return 1; }
+            for (ix = 0; ix < dims[0]; ix++)
+                for (iz = 0; iz < dims[1]; iz++) {
+                    const float *q = buf + ((size_t)ix * dims[1] + iz) * 2;
+                    fprintf(f, "%d %d %e %e\n", 2 * ix, 2 * iz, q[0], q[1]);
+                }
+            fclose(f);
+        }
+        free(buf);
+    }
     printf("%s: SEM calculation finished, %d steps\n", prog, step);
     free(su); free(sv); free(sw); free(args);
     sks_destroy(s);

@@ -243,6 +243,21 @@ __global__ void __launch_bounds__(256) k_init_line(T* __restrict__ u, T* __restr
     }
 }
 
+// snapshot (sem2d.c:1667-1683) of the field in u: (u_x, u_y) of every second
+// point, [ix/2][iz/2][2]
+template <typename T>
+__global__ void __launch_bounds__(256) k_snap(const T* __restrict__ u, int64_t np, int nx, int nz,
+                                              float* __restrict__ out, int nzs)
+{
+    const int nxs = (nx + 1) / 2;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)nxs * nzs) return;
+    const int ix = 2 * (int)(i / nzs), iz = 2 * (int)(i - (i / nzs) * nzs);
+    const int64_t g = (int64_t)iz * nx + ix;
+    out[2 * i] = (float)u[2 * g];
+    out[2 * i + 1] = (float)u[2 * np + g];
+}
+
 // kirrecord_zhl (sem2d_psvsh.c:2116-2160): u_x, u_y, -u_z at the receivers;
 // offset np addresses the reference's never-written extra point (reads 0)
 template <typename T>

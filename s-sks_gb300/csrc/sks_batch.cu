@@ -332,6 +332,7 @@ extern "C" int sks_batch_add(sks_batch* b, sks_solver* s)
     if (b->running) return set_err(SKS_ERR_STATE, "the batch is running");
     if (s->precision != b->precision) return set_err(SKS_ERR_ARG, "the solver's form differs from the batch's");
     if (s->device != b->device) return set_err(SKS_ERR_ARG, "the solver is on device %d, the batch on %d", s->device, b->device);
+    if (s->snaps) return set_err(SKS_ERR_UNSUPPORTED, "snapshots (plot_snap=1) are taken by sks_run, not in batches");
     cudaSetDevice(b->device);
     const sks_model& m = s->m;
     if (!s->seis_full) {
@@ -453,6 +454,23 @@ int batch_finish(sks_batch* b)
 }
 
 std::vector<sks_solver*>& batch_members(sks_batch* b) { return b->mem; }
+
+// the batch's stream at the device's highest (high = true) or lowest stream
+// priority: where two batches share the GPU, the scheduler starts the
+// high-priority batch's CTAs first.  Only between runs.
+int batch_set_priority(sks_batch* b, bool high)
+{
+    if (b->running) return set_err(SKS_ERR_STATE, "the batch is running");
+    cudaSetDevice(b->device);
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    cudaStream_t st = nullptr;
+    CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, high ? greatest : least));
+    CK(cudaStreamSynchronize(b->stream));
+    cudaStreamDestroy(b->stream);
+    b->stream = st;
+    return SKS_OK;
+}
 
 }  // namespace sksi
 

@@ -94,6 +94,12 @@ struct sks_solver {
     // whole-run seismograms its launches write ([nst][3][ntrace])
     sks_batch* batch;
     float* seis_full;
+    // snapshots (plot_snap): SKS_NSNAP buffers of snap_size floats, and which
+    // of them the run has taken
+    float* snaps;
+    size_t snap_size;
+    int nsnap;
+    bool snap_taken[SKS_NSNAP];
 };
 
 namespace sksi {
@@ -119,6 +125,7 @@ SKS_HIDDEN int batch_finish(sks_batch* b);
 SKS_HIDDEN bool batch_done(const sks_batch* b);
 SKS_HIDDEN bool batch_running(const sks_batch* b);
 SKS_HIDDEN std::vector<sks_solver*>& batch_members(sks_batch* b);
+SKS_HIDDEN int batch_set_priority(sks_batch* b, bool high);
 
 template <typename T>
 Coef<T> make_coef(const sks_model& m)
@@ -156,6 +163,8 @@ Field<T> make_field(sks_solver* s)
     F.seam_lo = (T*)s->seam_lo;
     F.seam_hi = (T*)s->seam_hi;
     F.seam_cnt = s->seam_cnt;
+    F.snap = nullptr;
+    F.snap_nzs = (s->m.nz + 1) / 2;
     return F;
 }
 

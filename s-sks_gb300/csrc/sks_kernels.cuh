@@ -95,6 +95,10 @@ struct Field {
     T* __restrict__ seam_lo;
     T* __restrict__ seam_hi;
     int* __restrict__ seam_cnt;
+    // snapshot of this step (plot_snap), or null: (u_x, u_y) of every second
+    // point, [ix/2][iz/2][2] with snap_nzs = (nz+1)/2 rows of iz per ix
+    float* __restrict__ snap;
+    int snap_nzs;
 };
 
 // Displacement layout: the P-SV pair (u_x, u_z) of every point as one 2-vector
@@ -279,6 +283,12 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
             F.seis_row[F.ntrace + t] = (float)un[1];
             F.seis_row[2 * F.ntrace + t] = (float)(-un[2]);
         }
+    }
+    // snapshot (sem2d.c:1667-1683): the same field as the receivers see
+    if (F.snap && !((ix | iz) & 1)) {
+        float* q = F.snap + ((size_t)(ix >> 1) * F.snap_nzs + (iz >> 1)) * 2;
+        q[0] = (float)un[0];
+        q[1] = (float)un[1];
     }
     // GRT_Interface4 of the next step (sem2d_psvsh.c:2076-2111)
     if (F.inject_next && ((iz == G.nbl && pf.row_ok) || (pf.on_col && iz > G.nbl))) {
@@ -687,7 +697,29 @@ struct PipeChunk {
     int nline;
     const void* dl;        // [n+1][nline][3] increments of the chunk (row s: step it0+s)
     float* seis;           // [n][3][ntrace] seismogram rows of the chunk
+    float* snaps;          // snapshot k of step snap_start + k*snap_incre (k < nsnap), or null
+    int snap_start, snap_incre, nsnap;
+    size_t snap_size;      // floats per snapshot
 };
+
+// which snapshot step it takes: the k < n with it == start + k*incre (the
+// reference tests the 26 candidates in turn; with incre == 0 they all name
+// the step `start`, whose snapshot is k = 0), or -1
+__host__ __device__ __forceinline__ int snap_index(int it, int start, int incre, int n)
+{
+    const int d = it - start;
+    if (incre == 0) return d == 0 && n > 0 ? 0 : -1;
+    if (d % incre) return -1;
+    const int k = d / incre;
+    return k >= 0 && k < n ? k : -1;
+}
+
+// the snapshot buffer of step it, or null
+__device__ __forceinline__ float* snap_of(float* snaps, int it, int start, int incre, int n, size_t size)
+{
+    const int k = snaps ? snap_index(it, start, incre, n) : -1;
+    return k >= 0 ? snaps + (size_t)k * size : nullptr;
+}
 
 __device__ __forceinline__ int ld_acquire(const int* p)
 {
@@ -748,6 +780,7 @@ k_step_pipe(Field<T> F, Geo<T> G, Coef<T> k, PipeChunk C, PipeCtl ctl)
                     sF.dline = (const T*)C.dl + (size_t)st * C.nline * 3;
                     sF.inject_next = it + 1 < C.nt_sem ? 1 : 0;
                     sF.seis_row = C.seis + (size_t)st * 3 * F.ntrace;
+                    sF.snap = snap_of(C.snaps, it, C.snap_start, C.snap_incre, C.nsnap, C.snap_size);
                     s_step = st;
                 }
             }

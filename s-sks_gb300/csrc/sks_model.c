@@ -628,6 +628,7 @@ int sks_model_from_par(sks_model *m, int argc, const char *const *argv, char *er
     /* defaults as in sem2d_psvsh.c:46-135 */
     m->flat = 1; m->nfil = 1; m->hpn = 5; m->absorb = 1; m->readpars = 1; m->neh = 1;
     m->xtrace = 20; m->idxplot = 20;
+    m->snap_start = 100; m->snap_incre = 50;
     for (i = 1; i < argc; i++) {
         const char *a = argv[i], *eq;
         while (*a == ' ' || *a == '\t') a++;
@@ -664,6 +665,9 @@ int sks_model_from_par(sks_model *m, int argc, const char *const *argv, char *er
     PGETF("zbeg", m->zbeg, m->zbeg_f, 0);
     PGETI("get_rec", m->get_rec, 0);
     PGETI("plot_trace", m->plot_trace, 0);
+    PGETI("plot_snap", m->plot_snap, 0);
+    PGETI("startsnap", m->snap_start, 0);
+    PGETI("incresnap", m->snap_incre, 0);
     if (m->get_rec == 1) PGETS("rec_file", m->rec_file, 1);
     PGETI("idxplot", m->idxplot, 1);
     PGETI("msource", m->msource, 1);

@@ -14,12 +14,16 @@ extern "C" {
 #endif
 
 #define SKS_MAX_N 6
+/* snapshots the reference writes with plot_snap=1: out1..out26 at steps
+ * startsnap + k*incresnap (sem2d_psvsh.c:483-510) */
+#define SKS_NSNAP 26
 #define SKS_MAT_STRIDE 16   /* 15 stiffness entries + rho per material */
 
 typedef struct {
     /* par words (sem2d_psvsh.c:154-205) */
     int flat, nt, nex, nst, nfil, hpn, absorb, readpars, neh, atten, xtrace;
     int get_rec, plot_trace, idxplot, msource, semmodel_full, psv_only;
+    int plot_snap, snap_start, snap_incre;   /* snapshots (sem2d_psvsh.c:149-150,202-204) */
     double dp, eh_par, sdt, xbeg, zbeg;
     float dp_f, eh_par_f, sdt_f, xbeg_f, zbeg_f;
     char greenfile[512], shgreenfile[512], raymodel[512], semmodel[512], rec_file[512];

@@ -217,6 +217,9 @@ extern "C" int sks_server_create(int device, int64_t budget, int32_t quantum, sk
     v->t0 = std::chrono::steady_clock::now();
     int rc = sks_batch_create(SKS_FP64, device, &v->batch[SKS_FP64]);
     if (!rc) rc = sks_batch_create(SKS_FP32C, device, &v->batch[SKS_FP32C]);
+    // FP32C quanta are short and many; FP64 quanta long: FP32C first
+    if (!rc) rc = batch_set_priority(v->batch[SKS_FP32C], true);
+    if (!rc) rc = batch_set_priority(v->batch[SKS_FP64], false);
     if (rc) {
         sks_batch_destroy(v->batch[0]);
         sks_batch_destroy(v->batch[1]);

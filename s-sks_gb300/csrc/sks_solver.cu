@@ -133,7 +133,7 @@ void free_device(sks_solver* s)
     void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc,
                   s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seisbuf[0], s->seisbuf[1], s->G, s->Dl, s->rec_psv, s->rec_sh,
                   s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt, s->items, s->seis_full,
-                  s->pipe_ctl};
+                  s->pipe_ctl, s->snaps};
     for (void* p : ps)
         if (p) cudaFree(p);
     s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = nullptr;
@@ -145,6 +145,7 @@ void free_device(sks_solver* s)
     s->seis_full = nullptr;
     s->pipe_ctl = nullptr;
     s->pipe_ctl_n = 0;
+    s->snaps = nullptr;
 }
 
 // per-kernel-class timing: an event pair around each launch when enabled
@@ -353,6 +354,10 @@ int step_impl(sks_solver* s, int it, const T* dline, float* seis_row)
     F.dline = dline;
     F.inject_next = (it + 1 < m.nt_sem) ? 1 : 0;
     F.seis_row = seis_row;
+    {
+        const int k = s->snaps ? snap_index(it, m.snap_start, m.snap_incre, s->nsnap) : -1;
+        F.snap = k >= 0 ? s->snaps + (size_t)k * s->snap_size : nullptr;
+    }
     Geo<T> G = make_geo<T>(s);
     static thread_local Coef<T> k;
     k = make_coef<T>(m);
@@ -391,6 +396,14 @@ int step0_impl(sks_solver* s, const double* G0, const double* G1, float* seis_ro
         KTimer t(s, SKS_KC_RECORD);
         k_record<T><<<(m.ntrace + 127) / 128, 128, 0, st>>>((const T*)s->U[0], np, s->rec_off, m.ntrace, seis_row);
     }
+    if (s->snaps) {
+        const int k = snap_index(0, m.snap_start, m.snap_incre, s->nsnap);
+        if (k >= 0) {
+            const int64_t n = (int64_t)((m.nx + 1) / 2) * ((m.nz + 1) / 2);
+            k_snap<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const T*)s->U[0], np, m.nx, m.nz,
+                                                                 s->snaps + (size_t)k * s->snap_size, (m.nz + 1) / 2);
+        }
+    }
     if (m.nt_sem > 1) {   // step 1's GRT_Interface4, applied to the step-0 field
         const int n = (m.nx - s->nbl) + (m.nz - s->nbl - 1);
         KTimer t(s, SKS_KC_INJECT);
@@ -420,6 +433,11 @@ int pipe_impl(sks_solver* s, int it1, int cnt, int i0)
     C.nline = (int)nline;
     C.dl = (const T*)s->Dl + (size_t)i0 * nline * 3;
     C.seis = s->seis + (size_t)i0 * 3 * m.ntrace;
+    C.snaps = s->snaps;
+    C.snap_start = m.snap_start;
+    C.snap_incre = m.snap_incre;
+    C.nsnap = s->nsnap;
+    C.snap_size = s->snap_size;
     const PipeCtl ctl{s->pipe_ctl, s->pipe_ctl + 2, s->pipe_ctl + 1};
     const int ntiles = s->ncx * s->ncz;
     CK(cudaMemsetAsync(ctl.claim, 0, sizeof(int), s->stream));
@@ -616,6 +634,21 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
             if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "upload of the boundary schedule: %s", cudaGetErrorString(ce));
         }
     }
+    if (!rc && m.plot_snap) {
+        // as many of the 26 candidate steps start + k*incre as fall in the run
+        s->nsnap = 0;
+        for (int k = 0; k < SKS_NSNAP; k++) {
+            const int64_t it = (int64_t)m.snap_start + (int64_t)k * m.snap_incre;
+            if (it >= 0 && it < m.nst) s->nsnap = k + 1;
+        }
+        if (m.snap_incre == 0) s->nsnap = (m.snap_start >= 0 && m.snap_start < m.nst) ? 1 : 0;
+        s->snap_size = (size_t)((m.nx + 1) / 2) * ((m.nz + 1) / 2) * 2;
+        if (s->nsnap > 0) {
+            rc = dmalloc(s, &s->snaps, (size_t)s->nsnap * s->snap_size);
+            if (!rc && cudaMemset(s->snaps, 0, sizeof(float) * (size_t)s->nsnap * s->snap_size) != cudaSuccess)
+                rc = set_err(SKS_ERR_CUDA, "snapshot buffers");
+        }
+    }
     if (rc) { free_device(s); cudaStreamDestroy(s->stream); sks_model_free(&s->m); delete s; return rc; }
     s->boundary_ready = (m.nt_sem == 0);
     *out = s;
@@ -773,6 +806,11 @@ extern "C" int sks_run(sks_solver* s, int32_t nsteps, float* su, float* sv, floa
         if (rc) return rc;
         if (want && pend.slot >= 0 && (rc = issue_copy(pend))) return rc;
         pend = want ? Pending{slot, n, done} : Pending{-1, 0, 0};
+        if (s->snaps)
+            for (int it = s->step; it < s->step + n; it++) {
+                const int k = snap_index(it, m.snap_start, m.snap_incre, s->nsnap);
+                if (k >= 0) s->snap_taken[k] = true;
+            }
         s->step += n;
         done += n;
         chunk_i++;
@@ -804,7 +842,25 @@ extern "C" int sks_reset(sks_solver* s)
     s->step = 0;
     s->cur = 0;
     s->g_last = 0;
+    for (bool& t : s->snap_taken) t = false;
     return SKS_OK;
+}
+
+extern "C" int sks_snapshot(const sks_solver* s, int32_t k, float* out, int32_t* dims)
+{
+    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    const sks_model& m = s->m;
+    if (dims) { dims[0] = (m.nx + 1) / 2; dims[1] = (m.nz + 1) / 2; }
+    if (!m.plot_snap) return set_err(SKS_ERR_STATE, "snapshots need plot_snap=1");
+    if (k < 0 || k >= SKS_NSNAP) return set_err(SKS_ERR_ARG, "snapshot %d: 0..%d", k, SKS_NSNAP - 1);
+    const int kk = m.snap_incre == 0 ? 0 : k;         // every candidate names the same step
+    if (kk >= s->nsnap || !s->snap_taken[kk]) return set_err(SKS_ERR_STATE, "snapshot %d has not been taken", k);
+    if (out) {
+        cudaSetDevice(s->device);
+        CK(cudaStreamSynchronize(s->stream));
+        CK(cudaMemcpy(out, s->snaps + (size_t)kk * s->snap_size, sizeof(float) * s->snap_size, cudaMemcpyDeviceToHost));
+    }
+    return m.snap_start + kk * m.snap_incre;
 }
 
 extern "C" int sks_get_info(const sks_solver* s, sks_info_t* info)

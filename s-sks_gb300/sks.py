@@ -31,7 +31,7 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_setup_receivers", "sks_setup_schedule", "sks_setup_close", "sks_open_setup",
            "sks_kernel_launches", "sks_last_run_ms", "sks_enable_kernel_timing", "sks_kernel_timing",
            "sks_set_tuning", "sks_get_tuning", "sks_autotune", "sks_line_increments",
-           "sks_line_increments_noalloc", "sks_set_boundary_plane_wave",
+           "sks_line_increments_noalloc", "sks_set_boundary_plane_wave", "sks_snapshot",
            "sks_batch_create", "sks_batch_add", "sks_batch_remove", "sks_batch_size", "sks_batch_run",
            "sks_batch_set_tuning", "sks_batch_get_tuning", "sks_batch_autotune", "sks_batch_last_run_ms",
            "sks_batch_kernel_launches", "sks_batch_destroy",
@@ -125,6 +125,7 @@ def lib() -> C.CDLL:
         L.sks_line_increments_noalloc.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp,
                                                   C.c_int32, vp, vp]
         L.sks_set_boundary_plane_wave.argtypes = [vp, C.POINTER(PlaneWave)]
+        L.sks_snapshot.argtypes = [vp, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_int32)]
         L.sks_destroy.argtypes = [vp]
         L.sks_destroy.restype = None
         fpp = C.POINTER(C.POINTER(C.c_float))
@@ -283,6 +284,14 @@ class Solver:
 
     def reset(self):
         _check(lib().sks_reset(self.h))
+
+    def snapshot(self, k: int):
+        """(step, [nx/2][nz/2][2] float32 of (u_x, u_y)) of snapshot k, or None when not taken."""
+        dims = (C.c_int32 * 2)()
+        lib().sks_snapshot(self.h, k, None, dims)
+        out = np.zeros((dims[0], dims[1], 2), np.float32)
+        st = lib().sks_snapshot(self.h, k, out.ctypes.data_as(C.POINTER(C.c_float)), dims)
+        return None if st < 0 else (st, out)
 
     def nline(self) -> int:
         i = self.info()

@@ -69,6 +69,11 @@ CASES = {
     "ratio_layers": dict(prog="sem2d_psvsh", semmodel=ratio_semmodel, case=lambda: synth.Case(
         nex=14, nez=8, eh=2.0, sdt=0.01, nst=640, layers=synth.layered_two(16.0, 5.0), p=0.05,
         f0=1.0, sh_amp=0.3, ntrace=8, rec_dx=3.3)),
+    # snapshots (plot_snap): the reference's text files out1..outK
+    "psvsh_snap": dict(prog="sem2d_psvsh", words=["plot_snap=1", "startsnap=40", "incresnap=60"],
+                       case=lambda: synth.Case(
+        nex=14, nez=9, eh=2.0, sdt=0.01, nst=720, layers=aniso_layers(18.0, 20.0), p=0.05, f0=1.0,
+        sv_amp=1.0, sh_amp=0.5, ntrace=7, rec_x0=1.0, rec_dx=4.0)),
 }
 
 
@@ -88,7 +93,7 @@ def make(name, spec):
         if "semmodel" in spec:
             spec["semmodel"](os.path.join(d, "semmodel"), c.thickness)
         quantize_traces(d)
-        r = subprocess.run([os.path.join(REFBIN, spec["prog"]), "par=run.par"], cwd=d,
+        r = subprocess.run([os.path.join(REFBIN, spec["prog"]), "par=run.par"] + spec.get("words", []), cwd=d,
                            capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"{name}: reference failed\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
@@ -101,6 +106,12 @@ def make(name, spec):
         out["ntrace"] = np.array(c.ntrace)
         out["nst"] = np.array(c.nst)
         out["prog"] = np.array(spec["prog"])
+        out["words"] = np.array(" ".join(spec.get("words", [])))
+        k = 1
+        while os.path.exists(os.path.join(d, f"out{k}")):
+            with open(os.path.join(d, f"out{k}"), "rb") as f:
+                out[f"snap_out{k}"] = np.frombuffer(f.read(), np.uint8)
+            k += 1
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print(name, {k: v.shape for k, v in out.items() if k.startswith("seis")})
 
@@ -118,4 +129,6 @@ if __name__ == "__main__":
     if not os.path.exists(os.path.join(REFBIN, "sem2d_psvsh")):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
     for n, s in CASES.items():
+        if len(sys.argv) > 1 and n not in sys.argv[1:]:
+            continue
         make(n, s)

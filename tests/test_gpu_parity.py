@@ -227,3 +227,76 @@ def test_line_increments_match_schedule(casedirs):
         # the injection window ends: the tail is zeros
         tail = s.line_increments(info["nt_inject"] - 2, 5)
         assert tail[0].any() and not tail[1:].any()
+
+
+SNAP_FIXTURES = [p for p in GOLDEN if "snap_out1" in np.load(p).files]
+
+
+def _parse_snapshot_text(b: bytes):
+    rows = np.array([line.split() for line in b.decode().splitlines()], dtype=np.float64)
+    return rows[:, :2].astype(int), rows[:, 2:]
+
+
+@pytest.mark.parametrize("path", SNAP_FIXTURES, ids=[os.path.basename(p)[:-4] for p in SNAP_FIXTURES])
+def test_snapshots_vs_oracle_and_reference_files(path, tmp_path):
+    """plot_snap: both forms, per-step and pipelined launches, against the
+    FP64 oracle's snapshots; the drop-in program's out files against the
+    reference's (same points, values within its FP32 rounding)."""
+    d = str(tmp_path)
+    z = extract(path, d)
+    nst = int(z["nst"])
+    words = ["par=run.par"] + str(z["words"]).split()
+    with chdir(d):
+        o = Oracle(words, fp64=True)
+        o.run(nst)
+        ref = []
+        k = 0
+        while True:
+            r = o.snapshot(k)
+            if r is None:
+                break
+            ref.append(r)
+            k += 1
+        o.close()
+        assert len(ref) >= 5 and max(np.abs(r[1]).max() for r in ref) > 0.05
+        for prec, tol in ((sks.FP64, FP64_TOL), (sks.FP32C, FP32C_TOL)):
+            for tuning in ((4, 3, 0, 1, 0, 0), (4, 3, 0, 1, 0, 1), (2, 2, 1, 0, 0, 0)):
+                with sks.Solver(words, precision=prec) as s:
+                    s.load_boundary_files()
+                    s.set_tuning(*tuning)
+                    s.run(nst // 3)
+                    s.run(nst)
+                    for k, (step, a) in enumerate(ref):
+                        got = s.snapshot(k)
+                        assert got is not None and got[0] == step
+                        na = np.linalg.norm(a)
+                        if na == 0.0:                  # before the wave arrives: exactly zero
+                            assert not np.any(got[1]), (prec, tuning, k)
+                            continue
+                        err = np.linalg.norm(got[1].astype(np.float64) - a) / na
+                        assert err <= tol, (prec, tuning, k, err)
+                    assert s.snapshot(len(ref)) is None
+        cli = os.path.join(os.path.dirname(sks.LIB_PATH), "sem2d_psvsh_gb300")
+        r = subprocess.run([cli] + words, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+    k = 1
+    while f"snap_out{k}" in z.files:
+        pos_ref, val_ref = _parse_snapshot_text(z[f"snap_out{k}"].tobytes())
+        with open(os.path.join(d, f"out{k}"), "rb") as f:
+            pos, val = _parse_snapshot_text(f.read())
+        assert np.array_equal(pos, pos_ref)
+        # the reference's %e text keeps 7 significant digits
+        assert np.linalg.norm(val - val_ref) <= 5e-5 * np.linalg.norm(val_ref) + 1e-30
+        k += 1
+    assert not os.path.exists(os.path.join(d, f"out{k}"))
+
+
+def test_snapshots_need_plot_snap(tmp_path):
+    d = str(tmp_path)
+    c = CASES["aniso_full_sh"]()
+    synth.write_case(c, d)
+    with chdir(d), sks.Solver(["par=run.par"], precision=sks.FP32C) as s:
+        s.load_boundary_files()
+        s.run(50)
+        assert s.snapshot(0) is None
+        assert "plot_snap" in sks.lib().sks_last_error().decode()

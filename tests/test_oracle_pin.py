@@ -106,3 +106,38 @@ def test_derivative_matrix_known_answers():
     assert np.allclose(D.sum(1), 0, atol=1e-13)
     for k in range(N + 1):
         assert np.allclose(D @ xi ** k, k * xi ** max(k - 1, 0) if k else 0, atol=1e-12)
+
+
+def _snap_fixtures():
+    out = []
+    for p in GOLDEN:
+        z = np.load(p)
+        if "snap_out1" in z.files:
+            out.append(p)
+    return out
+
+
+SNAP = _snap_fixtures()
+
+
+@pytest.mark.parametrize("path", SNAP, ids=[os.path.basename(p)[:-4] for p in SNAP])
+def test_float_oracle_snapshot_files_are_the_references(path):
+    """The oracle's program writes out1..outK byte for byte as the reference did."""
+    import subprocess
+    exe = os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_build", "oracle_sem2d_psvsh32")
+    with tempfile.TemporaryDirectory() as d:
+        z = extract(path, d)
+        words = ["par=run.par"] + str(z["words"]).split()
+        r = subprocess.run([exe] + words, cwd=d, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        k = 1
+        while f"snap_out{k}" in z.files:
+            with open(os.path.join(d, f"out{k}"), "rb") as f:
+                assert f.read() == z[f"snap_out{k}"].tobytes(), f"out{k} differs"
+            k += 1
+        assert k > 5
+        assert not os.path.exists(os.path.join(d, f"out{k}"))
+
+
+def test_snapshot_fixture_present():
+    assert SNAP
