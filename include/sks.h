@@ -117,6 +117,17 @@ int sks_run(sks_solver *s, int32_t nsteps, float *seis_u, float *seis_v, float *
  * plot_snap=0).  sks_run takes snapshots; batch members cannot have them. */
 int sks_snapshot(const sks_solver *s, int32_t k, float *out, int32_t *dims);
 
+/* Restart: a solve's state (both displacement buffers, the FP32C increment
+ * and compensation, the step, taken snapshots) copied to host memory and
+ * back, for checkpoints and for preempting a served solve.  A saved state
+ * loads into the same solve or into a new solver opened from the same par
+ * words and form (checked: form, mesh, step count); the run then continues
+ * exactly as if it had not stopped, under any tuning.  The reference has no
+ * restart (its snapshot files, sem2d.c:1667-1683, are for plotting). */
+int64_t sks_state_bytes(const sks_solver *s);
+int sks_state_save(sks_solver *s, void *host, int64_t bytes);
+int sks_state_load(sks_solver *s, const void *host, int64_t bytes);
+
 /* The boundary increments the time loop injects, as GRT_Interface4 adds them
  * (sem2d_psvsh.c:2076-2111) from the interpolated traces of interpl()
  * (interpl.c:16-54): for each step it in [it0, it0+nsteps), the FP64

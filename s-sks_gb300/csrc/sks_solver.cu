@@ -846,6 +846,106 @@ extern "C" int sks_reset(sks_solver* s)
     return SKS_OK;
 }
 
+// ---- state save / load -----------------------------------------------------
+namespace {
+
+struct StateHeader {
+    char magic[8];            // "SKSSTATE"
+    int32_t version, precision, nx, nz, nst, step, cur, nsnap;
+    int64_t field_bytes;      // bytes of the wavefield arrays that follow
+    int64_t snap_bytes;       // bytes of the snapshot buffers that follow
+    uint8_t snap_taken[SKS_NSNAP];
+    uint8_t pad[6];
+};
+
+// the device arrays of a solve's state, in save order
+int state_arrays(const sks_solver* s, void* const* ptrs[3], size_t sizes[3])
+{
+    const size_t np = (size_t)s->m.nx * s->m.nz;
+    const size_t el = s->precision == SKS_FP64 ? sizeof(double) : sizeof(float);
+    ptrs[0] = (void* const*)&s->U[0];
+    ptrs[1] = (void* const*)&s->U[1];
+    ptrs[2] = (void* const*)&s->Dv;
+    sizes[0] = sizes[1] = 3 * np * el;
+    sizes[2] = s->precision == SKS_FP32C ? 6 * np * el : 0;
+    return 3;
+}
+
+}  // namespace
+
+extern "C" int64_t sks_state_bytes(const sks_solver* s)
+{
+    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    void* const* p[3];
+    size_t sz[3];
+    state_arrays(s, p, sz);
+    return (int64_t)(sizeof(StateHeader) + sz[0] + sz[1] + sz[2] + (s->snaps ? s->nsnap * s->snap_size * sizeof(float) : 0));
+}
+
+extern "C" int sks_state_save(sks_solver* s, void* host, int64_t bytes)
+{
+    if (!s || !host) return set_err(SKS_ERR_ARG, "NULL argument");
+    if (bytes < sks_state_bytes(s)) return set_err(SKS_ERR_ARG, "state buffer of %lld bytes, %lld needed", (long long)bytes, (long long)sks_state_bytes(s));
+    cudaSetDevice(s->device);
+    void* const* p[3];
+    size_t sz[3];
+    state_arrays(s, p, sz);
+    StateHeader h;
+    memset(&h, 0, sizeof h);
+    memcpy(h.magic, "SKSSTATE", 8);
+    h.version = 1;
+    h.precision = s->precision;
+    h.nx = s->m.nx; h.nz = s->m.nz; h.nst = s->m.nst;
+    h.step = s->step; h.cur = s->cur;
+    h.nsnap = s->snaps ? s->nsnap : 0;
+    h.field_bytes = (int64_t)(sz[0] + sz[1] + sz[2]);
+    h.snap_bytes = (int64_t)(h.nsnap * s->snap_size * sizeof(float));
+    for (int k = 0; k < SKS_NSNAP; k++) h.snap_taken[k] = s->snap_taken[k] ? 1 : 0;
+    char* o = (char*)host;
+    memcpy(o, &h, sizeof h);
+    o += sizeof h;
+    CK(cudaStreamSynchronize(s->stream));
+    for (int i = 0; i < 3; i++) {
+        if (!sz[i]) continue;
+        CK(cudaMemcpy(o, *p[i], sz[i], cudaMemcpyDeviceToHost));
+        o += sz[i];
+    }
+    if (h.snap_bytes) CK(cudaMemcpy(o, s->snaps, (size_t)h.snap_bytes, cudaMemcpyDeviceToHost));
+    return SKS_OK;
+}
+
+extern "C" int sks_state_load(sks_solver* s, const void* host, int64_t bytes)
+{
+    if (!s || !host) return set_err(SKS_ERR_ARG, "NULL argument");
+    if (bytes < (int64_t)sizeof(StateHeader)) return set_err(SKS_ERR_ARG, "state buffer too short");
+    StateHeader h;
+    memcpy(&h, host, sizeof h);
+    if (memcmp(h.magic, "SKSSTATE", 8) || h.version != 1) return set_err(SKS_ERR_ARG, "not a saved solver state");
+    if (h.precision != s->precision || h.nx != s->m.nx || h.nz != s->m.nz || h.nst != s->m.nst)
+        return set_err(SKS_ERR_ARG, "the state belongs to another solve (form %d, %d x %d points, %d steps)",
+                       h.precision, h.nx, h.nz, h.nst);
+    if (h.nsnap != (s->snaps ? s->nsnap : 0)) return set_err(SKS_ERR_ARG, "the state's snapshot set differs");
+    if (bytes < sks_state_bytes(s)) return set_err(SKS_ERR_ARG, "state buffer too short");
+    if (s->batch && batch_running(s->batch)) return set_err(SKS_ERR_STATE, "the solver's batch is running");
+    cudaSetDevice(s->device);
+    void* const* p[3];
+    size_t sz[3];
+    state_arrays(s, p, sz);
+    const char* in = (const char*)host + sizeof h;
+    CK(cudaStreamSynchronize(s->stream));
+    for (int i = 0; i < 3; i++) {
+        if (!sz[i]) continue;
+        CK(cudaMemcpy(*p[i], in, sz[i], cudaMemcpyHostToDevice));
+        in += sz[i];
+    }
+    if (h.snap_bytes) CK(cudaMemcpy(s->snaps, in, (size_t)h.snap_bytes, cudaMemcpyHostToDevice));
+    s->step = h.step;
+    s->cur = h.cur;
+    s->g_last = 0;
+    for (int k = 0; k < SKS_NSNAP; k++) s->snap_taken[k] = h.snap_taken[k] != 0;
+    return SKS_OK;
+}
+
 extern "C" int sks_snapshot(const sks_solver* s, int32_t k, float* out, int32_t* dims)
 {
     if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");

@@ -32,6 +32,7 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_kernel_launches", "sks_last_run_ms", "sks_enable_kernel_timing", "sks_kernel_timing",
            "sks_set_tuning", "sks_get_tuning", "sks_autotune", "sks_line_increments",
            "sks_line_increments_noalloc", "sks_set_boundary_plane_wave", "sks_snapshot",
+           "sks_state_bytes", "sks_state_save", "sks_state_load",
            "sks_batch_create", "sks_batch_add", "sks_batch_remove", "sks_batch_size", "sks_batch_run",
            "sks_batch_set_tuning", "sks_batch_get_tuning", "sks_batch_autotune", "sks_batch_last_run_ms",
            "sks_batch_kernel_launches", "sks_batch_destroy",
@@ -126,6 +127,10 @@ def lib() -> C.CDLL:
                                                   C.c_int32, vp, vp]
         L.sks_set_boundary_plane_wave.argtypes = [vp, C.POINTER(PlaneWave)]
         L.sks_snapshot.argtypes = [vp, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_int32)]
+        L.sks_state_bytes.argtypes = [vp]
+        L.sks_state_bytes.restype = C.c_int64
+        L.sks_state_save.argtypes = [vp, vp, C.c_int64]
+        L.sks_state_load.argtypes = [vp, vp, C.c_int64]
         L.sks_destroy.argtypes = [vp]
         L.sks_destroy.restype = None
         fpp = C.POINTER(C.POINTER(C.c_float))
@@ -284,6 +289,16 @@ class Solver:
 
     def reset(self):
         _check(lib().sks_reset(self.h))
+
+    def save_state(self) -> np.ndarray:
+        n = _check(lib().sks_state_bytes(self.h))
+        buf = np.zeros(n, np.uint8)
+        _check(lib().sks_state_save(self.h, buf.ctypes.data_as(C.c_void_p), n))
+        return buf
+
+    def load_state(self, buf: np.ndarray):
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        _check(lib().sks_state_load(self.h, buf.ctypes.data_as(C.c_void_p), buf.size))
 
     def snapshot(self, k: int):
         """(step, [nx/2][nz/2][2] float32 of (u_x, u_y)) of snapshot k, or None when not taken."""
