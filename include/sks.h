@@ -117,6 +117,32 @@ int sks_run(sks_solver *s, int32_t nsteps, float *seis_u, float *seis_v, float *
  * plot_snap=0).  sks_run takes snapshots; batch members cannot have them. */
 int sks_snapshot(const sks_solver *s, int32_t k, float *out, int32_t *dims);
 
+/* ---- model builder -----------------------------------------------------
+ * Elastic tensors for SEM models in FP64 (the reference's float tools:
+ * semsyn/model/src/elastic_rotate.c, elastic_dip.c, cjcbi0.c).  Matrices are
+ * 6x6 Voigt, row-major, index order 11 22 33 23 13 12. */
+/* new x1 at angle_deg from old x1, counter-clockwise about x3; out may be c */
+int sks_elastic_rotate(const double c[36], double angle_deg, double out[36]);
+/* new x1 at angle_deg from old x1 toward old x3, about x2; out may be c */
+int sks_elastic_dip(const double c[36], double angle_deg, double out[36]);
+/* phase velocities along dir (any length): the square roots of the
+ * eigenvalues of the Christoffel matrix c_ijkl n_j n_l / rho, descending
+ * (qP, then the two quasi-shear waves) */
+int sks_christoffel(const double c[36], double rho, const double dir[3], double v[3]);
+/* one layer of a SEM model: its stiffness and density, and the control
+ * points (x, height above the box bottom, km) of its top interface */
+typedef struct {
+    double c[36];
+    double rho;
+    int32_t npts;
+    const double *x;
+    const double *z;
+} sks_layer_t;
+/* writes the SEM model file (sem2d_psvsh.c:663-713), bottom layer first:
+ * 13 constants per layer as the reference keeps them, or (full != 0) all 21
+ * for semmodel_full=1 */
+int sks_semmodel_write(const char *path, int32_t nlayers, const sks_layer_t *layers, int32_t full);
+
 /* Restart: a solve's state (both displacement buffers, the FP32C increment
  * and compensation, the step, taken snapshots) copied to host memory and
  * back, for checkpoints and for preempting a served solve.  A saved state

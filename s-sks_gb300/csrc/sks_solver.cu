@@ -28,6 +28,12 @@ int sks_err(int code, const char* fmt, ...)
 
 extern "C" const char* sks_last_error(void) { return g_err; }
 
+// error reporting for the library's C translation units
+extern "C" __attribute__((visibility("hidden"))) int sks_internal_error_c(int code, const char* msg)
+{
+    return set_err(code, "%s", msg);
+}
+
 // error reporting for the library's other translation units
 extern "C" __attribute__((visibility("hidden"))) int sks_internal_set_error(int code, const char* msg, cudaError_t e)
 {

@@ -33,6 +33,7 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_set_tuning", "sks_get_tuning", "sks_autotune", "sks_line_increments",
            "sks_line_increments_noalloc", "sks_set_boundary_plane_wave", "sks_snapshot",
            "sks_state_bytes", "sks_state_save", "sks_state_load",
+           "sks_elastic_rotate", "sks_elastic_dip", "sks_christoffel", "sks_semmodel_write",
            "sks_batch_create", "sks_batch_add", "sks_batch_remove", "sks_batch_size", "sks_batch_run",
            "sks_batch_set_tuning", "sks_batch_get_tuning", "sks_batch_autotune", "sks_batch_last_run_ms",
            "sks_batch_kernel_launches", "sks_batch_destroy",
@@ -71,6 +72,11 @@ class RequestInfo(C.Structure):
 
     def asdict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Layer(C.Structure):
+    _fields_ = [("c", C.c_double * 36), ("rho", C.c_double), ("npts", C.c_int32),
+                ("x", C.POINTER(C.c_double)), ("z", C.POINTER(C.c_double))]
 
 
 class PlaneWave(C.Structure):
@@ -127,6 +133,10 @@ def lib() -> C.CDLL:
                                                   C.c_int32, vp, vp]
         L.sks_set_boundary_plane_wave.argtypes = [vp, C.POINTER(PlaneWave)]
         L.sks_snapshot.argtypes = [vp, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_int32)]
+        L.sks_elastic_rotate.argtypes = [dp, C.c_double, dp]
+        L.sks_elastic_dip.argtypes = [dp, C.c_double, dp]
+        L.sks_christoffel.argtypes = [dp, C.c_double, dp, dp]
+        L.sks_semmodel_write.argtypes = [C.c_char_p, C.c_int32, C.POINTER(Layer), C.c_int32]
         L.sks_state_bytes.argtypes = [vp]
         L.sks_state_bytes.restype = C.c_int64
         L.sks_state_save.argtypes = [vp, vp, C.c_int64]
@@ -504,3 +514,49 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# ---- model builder --------------------------------------------------------
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def elastic_rotate(c, angle_deg: float) -> np.ndarray:
+    """6x6 Voigt matrix in axes turned by angle_deg about x3 (new x1 from old x1, counter-clockwise)."""
+    c = np.ascontiguousarray(c, dtype=np.float64).reshape(6, 6)
+    out = np.zeros((6, 6))
+    _check(lib().sks_elastic_rotate(_d(c), angle_deg, _d(out)))
+    return out
+
+
+def elastic_dip(c, angle_deg: float) -> np.ndarray:
+    """6x6 Voigt matrix in axes turned by angle_deg about x2 (new x1 from old x1 toward old x3)."""
+    c = np.ascontiguousarray(c, dtype=np.float64).reshape(6, 6)
+    out = np.zeros((6, 6))
+    _check(lib().sks_elastic_dip(_d(c), angle_deg, _d(out)))
+    return out
+
+
+def christoffel(c, rho: float, direction) -> np.ndarray:
+    """Phase velocities (descending) along direction."""
+    c = np.ascontiguousarray(c, dtype=np.float64).reshape(6, 6)
+    n = np.ascontiguousarray(direction, dtype=np.float64)
+    v = np.zeros(3)
+    _check(lib().sks_christoffel(_d(c), rho, _d(n), _d(v)))
+    return v
+
+
+def semmodel_write(path: str, layers, full: bool = True):
+    """layers: (c 6x6, rho, x control points, z heights) bottom to top."""
+    keep = []
+    arr = (Layer * len(layers))()
+    for i, (c, rho, x, z) in enumerate(layers):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        keep += [x, z]
+        arr[i].c[:] = list(np.asarray(c, dtype=np.float64).reshape(36))
+        arr[i].rho = rho
+        arr[i].npts = len(x)
+        arr[i].x = _d(x)
+        arr[i].z = _d(z)
+    _check(lib().sks_semmodel_write(path.encode(), len(layers), arr, 1 if full else 0))

@@ -46,8 +46,8 @@ def build(verbose: bool = False) -> str:
         "sks_model.h", "sks_internal.h", "sks_kernels.cuh", "sks_aux_kernels.cuh", "sks_variants.cuh",
         "sks_step_inst.cuh", "sks_batch_inst.cuh")]
     units = [
-        (os.path.join(CSRC, "sks_model.c"), os.path.join(OUT, "sks_model.o"),
-         ["gcc", "-O2", "-std=gnu11", "-fPIC", "-Wall", "-I" + INC, "-c"]),
+        (os.path.join(CSRC, c + ".c"), os.path.join(OUT, c + ".o"),
+         ["gcc", "-O2", "-std=gnu11", "-fPIC", "-Wall", "-I" + INC, "-c"]) for c in ("sks_model", "sks_elastic")
     ]
     for cu in ("sks_solver", "sks_batch", "sks_server", "sks_step_f32", "sks_step_f64", "sks_batch_f32", "sks_batch_f64",
                "sks_noalloc"):
