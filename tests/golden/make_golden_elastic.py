@@ -49,5 +49,5 @@ if __name__ == "__main__":
     mats, angles = inputs()
     rot = np.array([reference_rotate("libela_rotate.so", m, a) for m, a in zip(mats, angles)])
     dip = np.array([reference_rotate("libela_dip.so", m, a) for m, a in zip(mats, angles)])
-    np.savez_compressed(os.path.join(HERE, "elastic_tools.npz"), mats=mats, angles=angles, rotate=rot, dip=dip)
+    np.savez_compressed(os.path.join(HERE, "model", "elastic_tools.npz"), mats=mats, angles=angles, rotate=rot, dip=dip)
     print("elastic_tools", mats.shape, rot.shape, dip.shape)

@@ -11,7 +11,7 @@ from golden import make_golden_elastic as mge
 from util import chdir
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-GOLD = np.load(os.path.join(ROOT, "tests", "golden", "elastic_tools.npz"))
+GOLD = np.load(os.path.join(ROOT, "tests", "golden", "model", "elastic_tools.npz"))
 HAVE_REF = os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libela_rotate.so"))
 
 
