@@ -143,6 +143,34 @@ typedef struct {
  * for semmodel_full=1 */
 int sks_semmodel_write(const char *path, int32_t nlayers, const sks_layer_t *layers, int32_t full);
 
+/* ---- post-processing ---------------------------------------------------
+ * The band-pass and shear-wave splitting the reference's scripts run with SAC
+ * and an external Silver-Chan program (applications/test/prem_epi83.pl:96-99,
+ * cal_split.pl:7-56), on the device for every receiver of a solve. */
+typedef struct {
+    double f_lo, f_hi;      /* Butterworth band-pass corners (Hz); f_lo <= 0: no filter */
+    int32_t poles;          /* low-pass prototype poles (SAC "n"), 1..8 */
+    int32_t passes;         /* 1: forward; 2: forward then backward, zero phase (SAC "p") */
+    double before, after;   /* analysis window: s before / after the largest radial amplitude */
+    double max_delay;       /* s, delays 0..max_delay in steps of dt */
+    double dphi;            /* deg, fast axes -90 + k*dphi */
+} sks_split_opts_t;
+/* second-order sections of the band-pass for sample interval dt:
+ * sos[6k..6k+5] = b0 b1 b2 1 a1 a2; returns the number of sections (= poles) */
+int sks_bandpass_design(double f_lo, double f_hi, int32_t poles, double dt, double *sos);
+/* device scratch sks_split_traces needs */
+int sks_split_scratch(int32_t ntrace, int32_t nt, double dt, const sks_split_opts_t *o, int64_t *work_floats,
+                      int64_t *sum_doubles);
+/* Band-pass and Silver-Chan (1991, eigenvalue method) splitting of ntrace
+ * receivers; every pointer is DEVICE memory: sample t of trace r of the radial
+ * (u_x) and transverse (u_y) components at [t*ld + r] (a whole-run
+ * seismogram buffer [nst][3][ntrace] is radial = base, transverse = base +
+ * ntrace, ld = 3*ntrace); work and sums from sks_split_scratch; out[4r..4r+3]
+ * = fast axis (deg from x toward y), delay (samples), lambda2/lambda1, window
+ * start (sample).  Queued on stream (0: the default stream). */
+int sks_split_traces(const float *radial, const float *transverse, int32_t ntrace, int32_t nt, int64_t ld,
+                     double dt, const sks_split_opts_t *o, float *work, double *sums, float *out, void *stream);
+
 /* Restart: a solve's state (both displacement buffers, the FP32C increment
  * and compensation, the step, taken snapshots) copied to host memory and
  * back, for checkpoints and for preempting a served solve.  A saved state

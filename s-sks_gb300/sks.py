@@ -34,6 +34,7 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_line_increments_noalloc", "sks_set_boundary_plane_wave", "sks_snapshot",
            "sks_state_bytes", "sks_state_save", "sks_state_load",
            "sks_elastic_rotate", "sks_elastic_dip", "sks_christoffel", "sks_semmodel_write",
+           "sks_bandpass_design", "sks_split_scratch", "sks_split_traces",
            "sks_batch_create", "sks_batch_add", "sks_batch_remove", "sks_batch_size", "sks_batch_run",
            "sks_batch_set_tuning", "sks_batch_get_tuning", "sks_batch_autotune", "sks_batch_last_run_ms",
            "sks_batch_kernel_launches", "sks_batch_destroy",
@@ -77,6 +78,11 @@ class RequestInfo(C.Structure):
 class Layer(C.Structure):
     _fields_ = [("c", C.c_double * 36), ("rho", C.c_double), ("npts", C.c_int32),
                 ("x", C.POINTER(C.c_double)), ("z", C.POINTER(C.c_double))]
+
+
+class SplitOpts(C.Structure):
+    _fields_ = [("f_lo", C.c_double), ("f_hi", C.c_double), ("poles", C.c_int32), ("passes", C.c_int32),
+                ("before", C.c_double), ("after", C.c_double), ("max_delay", C.c_double), ("dphi", C.c_double)]
 
 
 class PlaneWave(C.Structure):
@@ -137,6 +143,11 @@ def lib() -> C.CDLL:
         L.sks_elastic_dip.argtypes = [dp, C.c_double, dp]
         L.sks_christoffel.argtypes = [dp, C.c_double, dp, dp]
         L.sks_semmodel_write.argtypes = [C.c_char_p, C.c_int32, C.POINTER(Layer), C.c_int32]
+        L.sks_bandpass_design.argtypes = [C.c_double, C.c_double, C.c_int32, C.c_double, dp]
+        L.sks_split_scratch.argtypes = [C.c_int32, C.c_int32, C.c_double, C.POINTER(SplitOpts),
+                                        C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.sks_split_traces.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int64, C.c_double, C.POINTER(SplitOpts),
+                                       vp, vp, vp, vp]
         L.sks_state_bytes.argtypes = [vp]
         L.sks_state_bytes.restype = C.c_int64
         L.sks_state_save.argtypes = [vp, vp, C.c_int64]
@@ -560,3 +571,25 @@ def semmodel_write(path: str, layers, full: bool = True):
         arr[i].x = _d(x)
         arr[i].z = _d(z)
     _check(lib().sks_semmodel_write(path.encode(), len(layers), arr, 1 if full else 0))
+
+
+# ---- post-processing ------------------------------------------------------
+def bandpass_design(f_lo: float, f_hi: float, poles: int, dt: float) -> np.ndarray:
+    """Second-order sections [poles][6] (b0 b1 b2 1 a1 a2) of the Butterworth band-pass."""
+    sos = np.zeros((max(1, poles), 6))
+    n = _check(lib().sks_bandpass_design(f_lo, f_hi, poles, dt, _d(sos)))
+    return sos[:n]
+
+
+def split_traces_device(radial_ptr: int, transverse_ptr: int, ntrace: int, nt: int, ld: int, dt: float,
+                        opts: SplitOpts, work_ptr: int, sums_ptr: int, out_ptr: int, stream: int = 0):
+    """sks_split_traces on device pointers (integers, e.g. torch data_ptr())."""
+    _check(lib().sks_split_traces(C.c_void_p(radial_ptr), C.c_void_p(transverse_ptr), ntrace, nt, ld, dt,
+                                  C.byref(opts), C.c_void_p(work_ptr), C.c_void_p(sums_ptr), C.c_void_p(out_ptr),
+                                  C.c_void_p(stream)))
+
+
+def split_scratch(ntrace: int, nt: int, dt: float, opts: SplitOpts):
+    w, s = C.c_int64(), C.c_int64()
+    _check(lib().sks_split_scratch(ntrace, nt, dt, C.byref(opts), C.byref(w), C.byref(s)))
+    return w.value, s.value

@@ -39,12 +39,9 @@ def _lagged_sums(x: np.ndarray, y: np.ndarray, i0: int, i1: int, kmax: int) -> d
     return out
 
 
-def splitting(x: np.ndarray, y: np.ndarray, dt: float, window: tuple[int, int], max_delay: float = 3.0,
-              dphi: float = 0.25) -> dict:
-    """Silver-Chan estimate from the radial (x) and transverse (y) components.
-
-    window: sample range [i0, i1) holding the SKS phase.  Returns phi (deg, in
-    [-90, 90)), delay (s), the minimum lambda2 / lambda1 and the grids' steps."""
+def eigen_grid(x: np.ndarray, y: np.ndarray, dt: float, window: tuple[int, int], max_delay: float = 3.0,
+               dphi: float = 0.25):
+    """The trial grid: fast axes (rad, [nphi]) and lambda2, lambda1 ([nphi][ndelay])."""
     x = np.asarray(x, dtype=np.float64)
     y = np.asarray(y, dtype=np.float64)
     i0, i1 = int(window[0]), int(window[1])
@@ -61,8 +58,17 @@ def splitting(x: np.ndarray, y: np.ndarray, dt: float, window: tuple[int, int], 
     c11 = np.broadcast_to(c11, c22.shape)
     half = 0.5 * (c11 + c22)
     rad = np.sqrt(np.maximum(0.25 * (c11 - c22) ** 2 + c12 ** 2, 0.0))
-    lam2 = half - rad
-    lam1 = half + rad
+    return phi[:, 0], half - rad, half + rad
+
+
+def splitting(x: np.ndarray, y: np.ndarray, dt: float, window: tuple[int, int], max_delay: float = 3.0,
+              dphi: float = 0.25) -> dict:
+    """Silver-Chan estimate from the radial (x) and transverse (y) components.
+
+    window: sample range [i0, i1) holding the SKS phase.  Returns phi (deg, in
+    [-90, 90)), delay (s), the minimum lambda2 / lambda1 and the grids' steps."""
+    phi, lam2, lam1 = eigen_grid(x, y, dt, window, max_delay, dphi)
+    phi = phi[:, None]
     j = np.unravel_index(int(np.argmin(lam2)), lam2.shape)
     return {"phi_deg": float(np.rad2deg(phi[j[0], 0])), "delay_s": float(j[1] * dt),
             "lambda_ratio": float(lam2[j] / lam1[j]) if lam1[j] > 0 else float("nan"),
