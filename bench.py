@@ -258,14 +258,15 @@ def _open_instances(inst, precision: int, gpu: int, base: str) -> list:
     return sol
 
 
-def run_batch(gpu: int, steps: int, warmup: int, fp64_steps: int = 8) -> dict:
+def run_batch(gpu: int, steps: int, warmup: int, fp64_steps: int = 8, instances: int = 64,
+              full: bool = True, tuning=None) -> dict:
     """The batched workload (64 seeded uneven instances, FP32C): autotuned
     batch, a timed window with every member active, then all 64 full solves
     from step 0 to the end with the seismograms read back, wall-clock timed.
     An FP64 batch of the same instances is timed over a short window."""
     import sks
     import synth
-    inst = synth.config_batch()
+    inst = synth.config_batch(n=instances)
     base = tempfile.mkdtemp(prefix="sks_batch_")
     out = {}
     try:
@@ -279,7 +280,11 @@ def run_batch(gpu: int, steps: int, warmup: int, fp64_steps: int = 8) -> dict:
         for s in sol:
             b.add(s)
         b.run(warmup, want=False)
-        tun = b.autotune(4)
+        if tuning:
+            b.set_tuning(*tuning)
+            tun = b.tuning()
+        else:
+            tun = b.autotune(4)
         k = max(1, min(steps, min(i["nst"] for i in infos) - warmup - 8))
         l0 = b.launches()
         b.run(k, want=False)
@@ -287,14 +292,17 @@ def run_batch(gpu: int, steps: int, warmup: int, fp64_steps: int = 8) -> dict:
         launches = b.launches() - l0
         rate = sum(pts) * k / (ms / 1e3)
         # the full solves, from step 0, seismograms into host arrays
-        for s in sol:
-            s.reset()
-        t0 = time.perf_counter()
-        res = b.run(10 ** 7, want=True)
-        wall = time.perf_counter() - t0
-        full_dev_ms = b.last_run_ms()
-        assert all(r[0].shape[0] == i["nst"] for r, i in zip(res, infos))
-        finite = all(np.isfinite(r[c]).all() for r in res for c in range(3))
+        wall = full_dev_ms = float("nan")
+        finite = None
+        if full:
+            for s in sol:
+                s.reset()
+            t0 = time.perf_counter()
+            res = b.run(10 ** 7, want=True)
+            wall = time.perf_counter() - t0
+            full_dev_ms = b.last_run_ms()
+            assert all(r[0].shape[0] == i["nst"] for r, i in zip(res, infos))
+            finite = all(np.isfinite(r[c]).all() for r in res for c in range(3))
         b.close()
         for s in sol:
             s.close()
@@ -598,6 +606,10 @@ def main() -> None:
                     "waves, pipelined chunks")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-instance workload")
     ap.add_argument("--batch-only", action="store_true", help="only the batched workload (one JSON object)")
+    ap.add_argument("--batch-instances", type=int, default=64,
+                    help="with --batch-only: the first N instances of the seeded batch (profiling a smaller batch)")
+    ap.add_argument("--batch-no-full", action="store_true", help="with --batch-only: skip the full solves")
+    ap.add_argument("--batch-tuning", default="", help="with --batch-only: W,B,Z,C instead of autotuning")
     ap.add_argument("--no-serve", action="store_true", help="skip the served workload")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the whole-solve FP32C-vs-FP64 accuracy run")
     ap.add_argument("--accuracy-only", action="store_true")
@@ -606,6 +618,7 @@ def main() -> None:
     ap.add_argument("--serve-rates", default="", help="only the served workload at these arrival rates (req/s), "
                     "one JSON object per rate, e.g. 2,5,10,20")
     ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-fp64-fraction", type=float, default=0.1)
     a = ap.parse_args()
     a.warmup = max(3, a.warmup)
     dist, rank, world, local = _dist()
@@ -651,7 +664,9 @@ def main() -> None:
         print(json.dumps({"kernel_only": a.form, **r}))
         return
     if a.batch_only:
-        print(json.dumps({"batch": run_batch(gpu, min(a.steps, 200), a.warmup)}))
+        bt = tuple(int(x) for x in a.batch_tuning.split(",")) if a.batch_tuning else None
+        print(json.dumps({"batch": run_batch(gpu, min(a.steps, 200), a.warmup, instances=a.batch_instances,
+                                             full=not a.batch_no_full, tuning=bt)}))
         return
     if a.accuracy_only:
         print(json.dumps({"accuracy": run_accuracy(gpu)}))
@@ -661,7 +676,8 @@ def main() -> None:
         return
     if a.serve_rates:
         for r in a.serve_rates.split(","):
-            print(json.dumps({"serve": run_serve(gpu, float(r), a.serve_requests)}), flush=True)
+            print(json.dumps({"serve": run_serve(gpu, float(r), a.serve_requests,
+                                                 fp64_frac=a.serve_fp64_fraction)}), flush=True)
         return
     d = tempfile.mkdtemp(prefix="sks_bench_")
     try:
