@@ -288,8 +288,8 @@ typedef struct {
                                      persistent CTAs that take (step, tile)
                                      pairs in order, a tile starting once its
                                      neighbours finished the previous step
-                                     (needs zseam = 0, waves = 0); 0: one
-                                     launch per step                        */
+                                     (needs waves = 0); 0: one launch per
+                                     step                                   */
 } sks_tuning_t;
 
 int sks_set_tuning(sks_solver *s, const sks_tuning_t *t);

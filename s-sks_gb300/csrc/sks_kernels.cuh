@@ -684,6 +684,11 @@ k_step_batch(const BatchMember<T>* __restrict__ mem, const BatchState* __restric
 // end; each wait is still bounded, and a wait that runs out sets the error
 // flag, which stops every CTA.  One launch replaces a chunk of step launches:
 // the per-launch ramp and tail of a small mesh are paid once per chunk.
+// With band seams (ZS) the boundary row between bands cz and cz+1 of step s
+// is finished by the later of the two; neither waits, and both have finished
+// step s -- read the partial forces, bumped the arrival counter -- before
+// either neighbour starts step s+1 (the 3 x 3 wait), so the seam buffers and
+// the counter's parity carry over from step to step.
 struct PipeCtl {
     int* claim;            // next (step, tile) index
     int* done;             // per tile: steps of the chunk it has finished
@@ -735,7 +740,7 @@ __device__ __forceinline__ void st_release(int* p, int v)
 
 constexpr int PIPE_SPIN_LIMIT = 1 << 22;   // polls of one wait (with 128 ns sleeps: about a second)
 
-template <typename T, bool ANISO, bool LF, int NW, int CAP>
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP>
 __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
 k_step_pipe(Field<T> F, Geo<T> G, Coef<T> k, PipeChunk C, PipeCtl ctl)
 {
@@ -787,7 +792,7 @@ k_step_pipe(Field<T> F, Geo<T> G, Coef<T> k, PipeChunk C, PipeCtl ctl)
         }
         __syncthreads();
         if (s_fail) break;
-        step_tile<T, ANISO, LF, NW, false, true>(sF, G, k, cx, cz, cz * G.HZ, min(cz * G.HZ + G.HZ, G.nez), sh);
+        step_tile<T, ANISO, LF, NW, ZS, true>(sF, G, k, cx, cz, cz * G.HZ, min(cz * G.HZ + G.HZ, G.nez), sh);
         __threadfence();
         __syncthreads();
         if (threadIdx.x == 0) {

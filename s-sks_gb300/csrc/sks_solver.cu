@@ -265,7 +265,7 @@ int upload_tables(sks_solver* s)
 // buffers grow to fit and their counters restart at 0.
 int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES, int PIPE)
 {
-    if (PIPE && (ZS || WAVES)) return set_err(SKS_ERR_ARG, "pipeline=1 needs zseam=0 and waves=0");
+    if (PIPE && WAVES) return set_err(SKS_ERR_ARG, "pipeline=1 needs waves=0");
     s->NW = NW;
     s->ZS = ZS;
     s->CAP = CAP;
@@ -310,7 +310,7 @@ int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES, int PIPE
         s->nblocks = (int)it.size();
     }
     if (PIPE) {
-        const StepVariant pv{NW, 0, CAP};
+        const StepVariant pv{NW, ZS, CAP};
         const int occ = s->precision == SKS_FP64 ? pipe_occupancy_f64(pv, s->m.anisotropic != 0)
                                                  : pipe_occupancy_f32(pv, s->m.anisotropic != 0);
         s->pipe_blocks = std::max(1, std::min(s->sms * occ, s->ncx * s->ncz));
@@ -450,7 +450,7 @@ int pipe_impl(sks_solver* s, int it1, int cnt, int i0)
     CK(cudaMemsetAsync(ctl.done, 0, sizeof(int) * (size_t)ntiles, s->stream));
     {
         KTimer t(s, SKS_KC_ELEMENT);
-        const StepVariant v{s->NW, 0, s->CAP};
+        const StepVariant v{s->NW, s->ZS, s->CAP};
         cudaError_t e;
         if (sizeof(T) == 4)
             e = launch_pipe_f32(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<float>*)&F,
@@ -1121,7 +1121,7 @@ extern "C" int sks_autotune(sks_solver* s, int32_t steps, sks_tuning_t* best)
             for (int cand = 0; cand < nhz + 3; cand++) {
                 const int hz = cand < nhz ? hzs[cand] : 0, wv = cand < nhz ? 0 : cand - nhz + 1;
                 if (wv == 0 && hz > m.nez && hz != hzs[0]) continue;
-                if (pipe && (zs || wv)) continue;
+                if (pipe && wv) continue;
                 if ((rc = snap_restore(s, snap))) break;
                 if ((rc = set_grid(s, nw, hz, zs, cap, wv, pipe))) break;
                 // one untimed step, then the timed ones

@@ -19,7 +19,7 @@ cudaError_t launch_step_f32(const StepVariant& v, bool aniso, int blocks, cudaSt
 
 int pipe_occupancy_f32(const StepVariant& v, bool aniso)
 {
-    const StepVariant p{v.nw, 0, v.cap};
+    const StepVariant p{v.nw, v.zseam, v.cap};
     PipeOcc<float, true> o;
     return visit_variant(p, aniso, o);
 }
@@ -27,7 +27,7 @@ int pipe_occupancy_f32(const StepVariant& v, bool aniso)
 cudaError_t launch_pipe_f32(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<float>& F,
                             const Geo<float>& G, const Coef<float>& k, const PipeChunk& C, const PipeCtl& ctl)
 {
-    const StepVariant p{v.nw, 0, v.cap};
+    const StepVariant p{v.nw, v.zseam, v.cap};
     PipeLaunch<float, true> l{blocks, st, F, G, k, C, ctl};
     visit_variant(p, aniso, l);
     return cudaGetLastError();

@@ -19,7 +19,7 @@ cudaError_t launch_step_f64(const StepVariant& v, bool aniso, int blocks, cudaSt
 
 int pipe_occupancy_f64(const StepVariant& v, bool aniso)
 {
-    const StepVariant p{v.nw, 0, v.cap};
+    const StepVariant p{v.nw, v.zseam, v.cap};
     PipeOcc<double, false> o;
     return visit_variant(p, aniso, o);
 }
@@ -27,7 +27,7 @@ int pipe_occupancy_f64(const StepVariant& v, bool aniso)
 cudaError_t launch_pipe_f64(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<double>& F,
                             const Geo<double>& G, const Coef<double>& k, const PipeChunk& C, const PipeCtl& ctl)
 {
-    const StepVariant p{v.nw, 0, v.cap};
+    const StepVariant p{v.nw, v.zseam, v.cap};
     PipeLaunch<double, false> l{blocks, st, F, G, k, C, ctl};
     visit_variant(p, aniso, l);
     return cudaGetLastError();

@@ -33,7 +33,7 @@ struct PipeLaunch {
     template <bool A, int NW, bool ZS, int CAP>
     int run()
     {
-        k_step_pipe<T, A, LF, NW, CAP><<<blocks, NW * 32, 0, st>>>(F, G, k, C, ctl);
+        k_step_pipe<T, A, LF, NW, ZS, CAP><<<blocks, NW * 32, 0, st>>>(F, G, k, C, ctl);
         return 0;
     }
 };
@@ -41,7 +41,7 @@ struct PipeLaunch {
 template <typename T, bool LF>
 struct PipeOcc {
     template <bool A, int NW, bool ZS, int CAP>
-    int run() { return occupancy_of(k_step_pipe<T, A, LF, NW, CAP>, NW * 32); }
+    int run() { return occupancy_of(k_step_pipe<T, A, LF, NW, ZS, CAP>, NW * 32); }
 };
 
 template <typename T, bool LF>

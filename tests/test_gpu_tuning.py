@@ -51,7 +51,7 @@ def _run(d, prec, nst, tuning=None, autotune=False):
 
 TUNINGS = ([(nw, hz, zs, cap, wv, 0) for nw in (2, 4) for hz in (1, 3, 23) for zs in (0, 1) for cap in (0, 1, 2)
             for wv in (0,)] + [(nw, 4, zs, 1, wv, 0) for nw in (2, 4) for zs in (0, 1) for wv in (1, 2, 5)]
-           + [(nw, hz, 0, cap, 0, 1) for nw in (2, 4) for hz in (1, 3, 23) for cap in (0, 1, 2)])
+           + [(nw, hz, zs, cap, 0, 1) for nw in (2, 4) for hz in (1, 3, 23) for zs in (0, 1) for cap in (0, 1, 2)])
 
 
 @pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])
