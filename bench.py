@@ -337,7 +337,7 @@ def run_batch(gpu: int, steps: int, warmup: int, fp64_steps: int = 8, instances:
 
 
 def run_serve(gpu: int, rate: float, nreq: int = 24, seed: int = 7, fp64_frac: float = 0.1,
-              prep_threads: int = 8, quantum: int = 64) -> dict:
+              prep_threads: int = 8, quantum: int = 64, tuning32=(4, 12, 0, 1, 1)) -> dict:
     """The served workload: seeded Poisson arrivals of `nreq` SKS solve
     requests at `rate` per second (mesh sizes lognormal, median 400 x 200
     elements, clipped to 100 x 50 .. 2000 x 600, element 1-2 km; physics as in
@@ -361,7 +361,7 @@ def run_serve(gpu: int, rate: float, nreq: int = 24, seed: int = 7, fp64_frac: f
         specs.append((inst, form))
     base = tempfile.mkdtemp(prefix="sks_serve_")
     srv = sks.Server(gpu, 0, quantum)
-    srv.set_tuning(sks.FP32C, 4, 6, 0, 1)
+    srv.set_tuning(sks.FP32C, *tuning32)
     srv.set_tuning(sks.FP64, 4, 8, 1, 0)
     lock = threading.Lock()
     ids, errors = {}, []
@@ -430,7 +430,8 @@ def run_serve(gpu: int, rate: float, nreq: int = 24, seed: int = 7, fp64_frac: f
             "span_s": span, "solves_per_hour": len(ok) * 3600.0 / span if span else None,
             "updates_per_s": sum(work[k] for k in ok) / span if span else None,
             "all_finite": all(v["finite"] for v in ok.values()),
-            "arrival_window_s": float(arrivals[-1]), "quantum_steps": quantum}
+            "arrival_window_s": float(arrivals[-1]), "quantum_steps": quantum,
+            "tuning_fp32c": dict(zip(("warps_per_block", "band_rows", "zseam", "register_cap", "pipeline"), tuning32))}
 
 
 def run_accuracy(gpu: int, nst: int = FULL_STEPS) -> dict:
@@ -619,6 +620,8 @@ def main() -> None:
                     "one JSON object per rate, e.g. 2,5,10,20")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-fp64-fraction", type=float, default=0.1)
+    ap.add_argument("--serve-tuning", default="4,12,0,1,1",
+                    help="with --serve-rates: W,B,Z,C,P of the FP32C batch (P: pipelined chunks)")
     a = ap.parse_args()
     a.warmup = max(3, a.warmup)
     dist, rank, world, local = _dist()
@@ -676,8 +679,9 @@ def main() -> None:
         return
     if a.serve_rates:
         for r in a.serve_rates.split(","):
-            print(json.dumps({"serve": run_serve(gpu, float(r), a.serve_requests,
-                                                 fp64_frac=a.serve_fp64_fraction)}), flush=True)
+            t32 = tuple(int(x) for x in a.serve_tuning.split(","))
+            print(json.dumps({"serve": run_serve(gpu, float(r), a.serve_requests, fp64_frac=a.serve_fp64_fraction,
+                                                 tuning32=t32)}), flush=True)
         return
     d = tempfile.mkdtemp(prefix="sks_bench_")
     try:

@@ -329,8 +329,10 @@ void sks_destroy(sks_solver *s);
  * applications/test/prem_epi83.pl:81-82); a batch replaces a set of such
  * processes.  Members are ordinary solvers of one form and device, each with
  * its own mesh, materials, time step, boundary records and step count.  One
- * step of every member is one launch of a persistent kernel; a chunk of 64
- * steps (boundary interpolation, increments, 64 step launches) is one launch
+ * step of every member is one launch of a persistent kernel (or, with
+ * pipeline = 1, the chunk's steps of every member are one launch whose
+ * tiles start as their neighbours finish the previous step); a chunk of 64
+ * steps (boundary interpolation, increments, the step launches) is one launch
  * of a CUDA graph that the batch captures once and reuses.  A member runs
  * with the batch's tuning, and its seismograms are bit-identical to the same
  * solver run alone with that tuning.  Members keep their wavefields on the
@@ -353,7 +355,7 @@ int sks_batch_size(const sks_batch *b);
 int sks_batch_run(sks_batch *b, int32_t nsteps, float *const *su, float *const *sv, float *const *sw);
 
 /* Tuning shared by the members (waves must be 0: the batch's persistent grid
- * balances the tiles).  sks_batch_autotune times every candidate on the
+ * balances the tiles; pipeline 0 or 1).  sks_batch_autotune times every candidate on the
  * members' next `steps` steps and restores their state afterwards. */
 int sks_batch_set_tuning(sks_batch *b, const sks_tuning_t *t);
 int sks_batch_get_tuning(const sks_batch *b, sks_tuning_t *t);

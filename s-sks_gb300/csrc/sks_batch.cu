@@ -30,6 +30,7 @@ struct sks_batch {
     std::vector<sks_solver*> mem;
     cudaStream_t stream = nullptr;
     int NW = 4, HZ = 6, ZS = 0, CAP = 1;  // tuning shared by the members
+    int PIPE = 0;                         // 1: a chunk is one pipelined launch (k_step_batch_pipe)
     int chunk = 64;
     bool aniso = false;                   // the step variant: any member anisotropic
     int grid = 0;                         // persistent CTAs of a step launch
@@ -39,6 +40,7 @@ struct sks_batch {
     BatchState* dstate = nullptr;
     BatchHeader* dhdr = nullptr;
     int4* ditems = nullptr;
+    int* dpipe = nullptr;                 // pipelined chunks: [claim, error, done[items_cap]]
     int cap = 0;
     size_t items_cap = 0;
     int nitems = 0;
@@ -65,11 +67,12 @@ int nline_of(const sks_solver* s) { return (s->m.nx - s->nbl) + (s->m.nz - s->nb
 
 void free_tables(sks_batch* b)
 {
-    void* ps[] = {b->dmem, b->daux, b->dstate, b->dhdr, b->ditems};
+    void* ps[] = {b->dmem, b->daux, b->dstate, b->dhdr, b->ditems, b->dpipe};
     for (void* p : ps)
         if (p) cudaFree(p);
     if (b->hstate) cudaFreeHost(b->hstate);
     b->dmem = nullptr; b->daux = nullptr; b->dstate = nullptr; b->dhdr = nullptr; b->ditems = nullptr;
+    b->dpipe = nullptr;
     b->hstate = nullptr;
     b->cap = 0;
     b->items_cap = 0;
@@ -148,6 +151,7 @@ int build_tables(sks_batch* b)
         sks_solver* s = b->mem[i];
         aniso = aniso || member_aniso(s);
         md.push_back(member_desc<T>(s));
+        md.back().item0 = (int)items.size();
         ad.push_back(aux_desc(s));
         if (s->ncx >= (1 << 16) || s->ncz >= (1 << 15))
             return set_err(SKS_ERR_UNSUPPORTED, "member %d: %d x %d tiles exceed the batch's tile index", i, s->ncx, s->ncz);
@@ -182,14 +186,17 @@ int build_tables(sks_batch* b)
     if (items.size() > b->items_cap) {
         const size_t ic = std::max(items.size(), 2 * b->items_cap);
         if (b->ditems) cudaFree(b->ditems);
+        if (b->dpipe) cudaFree(b->dpipe);
         b->ditems = nullptr;
+        b->dpipe = nullptr;
         b->items_cap = 0;
         CK(cudaMalloc((void**)&b->ditems, sizeof(int4) * ic));
+        CK(cudaMalloc((void**)&b->dpipe, sizeof(int) * (2 + ic)));
         b->items_cap = ic;
         b->graph_dirty = true;
     }
     b->device_bytes = (int64_t)(sizeof(BatchMember<T>) + sizeof(BatchAux) + sizeof(BatchState)) * b->cap +
-                      (int64_t)sizeof(int4) * (int64_t)b->items_cap + (int64_t)sizeof(BatchHeader);
+                      (int64_t)(sizeof(int4) + sizeof(int)) * (int64_t)b->items_cap + 8 + (int64_t)sizeof(BatchHeader);
     if (n) {
         CK(cudaMemcpyAsync(b->dmem, md.data(), sizeof(BatchMember<T>) * n, cudaMemcpyHostToDevice, b->stream));
         CK(cudaMemcpyAsync(b->daux, ad.data(), sizeof(BatchAux) * n, cudaMemcpyHostToDevice, b->stream));
@@ -217,11 +224,30 @@ cudaError_t launch_steps(sks_batch* b, int j)
                             b->dhdr, j, *(const Coef<double>*)&k);
 }
 
+// a pipelined chunk of nsteps steps: the counters back to zero, then one launch
+template <typename T>
+cudaError_t launch_pipe_chunk(sks_batch* b, int nsteps)
+{
+    const StepVariant v{b->NW, b->ZS, b->CAP};
+    static thread_local Coef<T> k;
+    k = make_coef<T>(b->mem[0]->m);
+    cudaError_t e = cudaMemsetAsync(b->dpipe, 0, sizeof(int) * (2 + b->items_cap), b->stream);
+    if (e != cudaSuccess) return e;
+    const BatchPipeCtl ctl{b->dpipe, b->dpipe + 1, b->dpipe + 2};
+    if (sizeof(T) == 4)
+        return launch_batch_pipe_f32(v, b->aniso, b->grid, b->stream, (const BatchMember<float>*)b->dmem, b->dstate,
+                                     b->ditems, b->dhdr, nsteps, ctl, *(const Coef<float>*)&k);
+    return launch_batch_pipe_f64(v, b->aniso, b->grid, b->stream, (const BatchMember<double>*)b->dmem, b->dstate,
+                                 b->ditems, b->dhdr, nsteps, ctl, *(const Coef<double>*)&k);
+}
+
 // persistent grid: every SM full of resident CTAs of the step variant
 void set_persistent_grid(sks_batch* b)
 {
     const StepVariant v{b->NW, b->ZS, b->CAP};
-    const int occ = b->precision == SKS_FP64 ? batch_occupancy_f64(v, b->aniso) : batch_occupancy_f32(v, b->aniso);
+    int occ;
+    if (b->PIPE) occ = b->precision == SKS_FP64 ? batch_pipe_occupancy_f64(v, b->aniso) : batch_pipe_occupancy_f32(v, b->aniso);
+    else occ = b->precision == SKS_FP64 ? batch_occupancy_f64(v, b->aniso) : batch_occupancy_f32(v, b->aniso);
     b->grid = b->sms * occ;
 }
 
@@ -235,7 +261,10 @@ int capture_graph(sks_batch* b)
     k_interp_batch<<<dim3(b->chunk + 1, b->cap), 256, 0, st>>>(b->daux, b->dstate, b->dhdr);
     k_line_delta_batch<T><<<dim3(32, b->cap), 256, 0, st>>>(b->daux, b->dstate, b->dhdr);
     cudaError_t e = cudaSuccess;
-    for (int j = 0; j < b->chunk && e == cudaSuccess; j++) e = launch_steps<T>(b, j);
+    if (b->PIPE)
+        e = launch_pipe_chunk<T>(b, b->chunk);
+    else
+        for (int j = 0; j < b->chunk && e == cudaSuccess; j++) e = launch_steps<T>(b, j);
     k_batch_advance<<<1, 256, 0, st>>>(b->dstate, b->dhdr);
     cudaGraph_t g = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(st, &g);
@@ -247,7 +276,7 @@ int capture_graph(sks_batch* b)
     }
     b->graph = g;
     CK(cudaGraphInstantiate(&b->exec, g, 0));
-    b->graph_kernels = b->chunk + 3;
+    b->graph_kernels = (b->PIPE ? 1 : b->chunk) + 3;
     b->graph_dirty = false;
     return SKS_OK;
 }
@@ -440,6 +469,8 @@ int batch_finish(sks_batch* b)
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
     b->last_ms = ms;
+    int err = 0;
+    if (b->PIPE) CK(cudaMemcpy(&err, b->dpipe + 1, sizeof(int), cudaMemcpyDeviceToHost));
     int adv = 0;
     for (size_t i = 0; i < b->mem.size() && i < b->target.size(); i++) {
         sks_solver* s = b->mem[i];
@@ -450,6 +481,7 @@ int batch_finish(sks_batch* b)
         }
         adv = std::max(adv, b->target[i] - b->start[i]);
     }
+    if (err) return set_err(SKS_ERR_CUDA, "pipelined batch chunk: a wait for neighbouring tiles ran out");
     return adv;
 }
 
@@ -492,7 +524,7 @@ extern "C" int sks_batch_set_tuning(sks_batch* b, const sks_tuning_t* t)
     if (t->register_cap < 0 || t->register_cap > 2) return set_err(SKS_ERR_ARG, "register_cap=%d: 0, 1 or 2", t->register_cap);
     if (t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
     if (t->waves != 0) return set_err(SKS_ERR_ARG, "a batch uses plain bands (waves=0)");
-    if (t->pipeline != 0) return set_err(SKS_ERR_ARG, "a batch is launched per step (pipeline=0)");
+    if (t->pipeline != 0 && t->pipeline != 1) return set_err(SKS_ERR_ARG, "pipeline=%d: 0 or 1", t->pipeline);
     if (b->running) return set_err(SKS_ERR_STATE, "the batch is running");
     cudaSetDevice(b->device);
     cudaStreamSynchronize(b->stream);
@@ -500,10 +532,12 @@ extern "C" int sks_batch_set_tuning(sks_batch* b, const sks_tuning_t* t)
     b->HZ = t->band_rows;
     b->ZS = t->zseam ? 1 : 0;
     b->CAP = t->register_cap;
+    b->PIPE = t->pipeline;
     for (sks_solver* s : b->mem) {
         int rc = apply_tuning(b, s);
         if (rc) return rc;
     }
+    set_persistent_grid(b);
     b->tables_dirty = true;
     b->graph_dirty = true;
     return SKS_OK;
@@ -519,7 +553,7 @@ extern "C" int sks_batch_get_tuning(const sks_batch* b, sks_tuning_t* t)
     t->waves = 0;
     t->blocks = b->grid;
     t->ms_per_step = 0.f;
-    t->pipeline = 0;
+    t->pipeline = b->PIPE;
     return SKS_OK;
 }
 
@@ -546,15 +580,16 @@ extern "C" int sks_batch_autotune(sks_batch* b, int32_t steps, sks_tuning_t* bes
     for (int i = 0; i < n && !rc; i++) rc = cudaStreamSynchronize(b->mem[i]->stream) == cudaSuccess ? SKS_OK : SKS_ERR_CUDA;
     for (int i = 0; i < n && !rc; i++)
         if (b->mem[i]->step == 0) rc = first_step(b->mem[i]);
-    const sks_tuning_t old = {b->NW, b->HZ, b->ZS, b->CAP, 0, b->grid, 0.f};
+    const sks_tuning_t old = {b->NW, b->HZ, b->ZS, b->CAP, 0, b->grid, 0.f, b->PIPE};
     sks_tuning_t bt = old;
     bt.ms_per_step = 1e30f;
     const int hzs[] = {3, 4, 6, 8, 12};
+    for (int pipe = 0; pipe < 2 && !rc; pipe++)
     for (int nw = 2; nw <= 4 && !rc; nw += 2)
         for (int zs = 0; zs < 2 && !rc; zs++)
             for (int cap = 0; cap < 3 && !rc; cap++)
                 for (int hz : hzs) {
-                    sks_tuning_t t = {nw, hz, zs, cap, 0, 0, 0.f};
+                    sks_tuning_t t = {nw, hz, zs, cap, 0, 0, 0.f, pipe};
                     if ((rc = sks_batch_set_tuning(b, &t))) break;
                     rc = b->precision == SKS_FP64 ? build_tables<double>(b) : build_tables<float>(b);
                     if (rc) break;
@@ -573,17 +608,26 @@ extern "C" int sks_batch_autotune(sks_batch* b, int32_t steps, sks_tuning_t* bes
                     cudaError_t e = cudaSuccess;
                     for (int pass = 0; pass < 2 && e == cudaSuccess; pass++) {
                         if (pass) cudaEventRecord(b->ev[0], b->stream);
-                        for (int j = 0; j < steps && e == cudaSuccess; j++)
-                            e = b->precision == SKS_FP64 ? launch_steps<double>(b, j) : launch_steps<float>(b, j);
+                        if (pipe)
+                            e = b->precision == SKS_FP64 ? launch_pipe_chunk<double>(b, steps)
+                                                         : launch_pipe_chunk<float>(b, steps);
+                        else
+                            for (int j = 0; j < steps && e == cudaSuccess; j++)
+                                e = b->precision == SKS_FP64 ? launch_steps<double>(b, j) : launch_steps<float>(b, j);
                     }
                     cudaEventRecord(b->ev[1], b->stream);
                     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
                     if (e != cudaSuccess) { rc = set_err(SKS_ERR_CUDA, "batch autotune: %s", cudaGetErrorString(e)); break; }
+                    if (pipe) {
+                        int err = 0;
+                        CK(cudaMemcpy(&err, b->dpipe + 1, sizeof(int), cudaMemcpyDeviceToHost));
+                        if (err) { rc = set_err(SKS_ERR_CUDA, "batch autotune: a pipelined wait ran out"); break; }
+                    }
                     float ms = 0.f;
                     cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]);
-                    b->launches += 2 + 2 * steps;
+                    b->launches += 2 + 2 * (pipe ? 1 : steps);
                     ms /= (float)steps;
-                    if (ms < bt.ms_per_step) bt = {nw, hz, zs, cap, 0, b->grid, ms};
+                    if (ms < bt.ms_per_step) bt = {nw, hz, zs, cap, 0, b->grid, ms, pipe};
                 }
     for (int i = 0; i < n; i++) {
         const int r2 = snap_restore(b->mem[i], snaps[i]);

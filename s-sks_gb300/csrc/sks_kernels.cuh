@@ -612,6 +612,7 @@ struct BatchMember {
     float* seis;           // whole-run seismograms, [nst][3][ntrace]
     int nt_sem;            // steps that inject
     int nline;
+    int item0;             // the member's first tile in the batch's tile table
 };
 
 // per member: step at the chunk's start, steps in this chunk, step to stop at
@@ -803,6 +804,103 @@ k_step_pipe(Field<T> F, Geo<T> G, Coef<T> k, PipeChunk C, PipeCtl ctl)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined batch chunk: the steps of a chunk of every member of a batch in
+// one launch.  Persistent CTAs claim (step j, tile i) pairs in step-major
+// order over the batch's tile table (members one after another, each
+// member's tiles row by row); tile i of step j starts once the 3 x 3
+// neighbourhood of its member's own tiles has finished step j-1, exactly as
+// in the single-mesh pipelined chunk, and a member whose chunk has fewer
+// steps has no tile at step j.  The steps' own fields (displacement buffers,
+// injection row, seismogram row) follow from the member's step as in
+// k_step_batch.  One launch replaces the chunk's per-step launches and their
+// partly idle tails.
+struct BatchPipeCtl {
+    int* claim;            // next (step, tile) index
+    int* error;            // set when a wait ran out
+    int* done;             // per tile: steps of the chunk it has finished
+};
+
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP>
+__global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
+k_step_batch_pipe(const BatchMember<T>* __restrict__ mem, const BatchState* __restrict__ state,
+                  const int4* __restrict__ items, const BatchHeader* __restrict__ hdr, int nsteps, BatchPipeCtl ctl,
+                  Coef<T> k)
+{
+    __shared__ TileShared<T, NW> sh;
+    __shared__ __align__(16) Field<T> sF;
+    __shared__ __align__(16) Geo<T> sG;
+    __shared__ int s_claim, s_next, s_fail, s_go, s_m, s_j;
+    const int nitems = hdr->nitems;
+    const int total = nsteps * nitems;
+    if (threadIdx.x == 0) { s_m = -1; s_j = -1; s_claim = atomicAdd(ctl.claim, 1); }
+    __syncthreads();
+    for (;;) {
+        const int c = s_claim;
+        if (c >= total) break;
+        const int j = c / nitems, i = c - j * nitems;
+        const int4 it = items[i];
+        const int m = it.x, cx = it.y & 0xffff, cz = it.y >> 16;
+        const BatchMember<T>* M = mem + m;
+        if (m != s_m) {
+            // descriptor of a new member
+            constexpr int FW = (int)(sizeof(Field<T>) / 4), GW = (int)(sizeof(Geo<T>) / 4);
+            for (int q = threadIdx.x; q < FW + GW; q += blockDim.x) {
+                if (q < FW) reinterpret_cast<int*>(&sF)[q] = __ldg(reinterpret_cast<const int*>(&M->F) + q);
+                else reinterpret_cast<int*>(&sG)[q - FW] = __ldg(reinterpret_cast<const int*>(&M->G) + q - FW);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) { s_m = m; s_j = -1; }
+            __syncthreads();
+        }
+        if (threadIdx.x < 32) {
+            // lanes 0..8 wait, each for one tile of the member's 3 x 3
+            // neighbourhood to finish step j-1; lane 0 claims the next pair
+            const BatchState st = state[m];
+            const int step = st.it0 + j;
+            const bool go = j < st.n && step >= 1;
+            int next = 0;
+            if (threadIdx.x == 0) { next = atomicAdd(ctl.claim, 1); s_fail = 0; }
+            int fail = 0;
+            if (go && j > 0 && threadIdx.x < 9) {
+                const int z = cz + (int)threadIdx.x / 3 - 1, x = cx + (int)threadIdx.x % 3 - 1;
+                if (z >= 0 && z < sG.ncz && x >= 0 && x < sG.ncx) {
+                    const int* f = ctl.done + M->item0 + z * sG.ncx + x;
+                    int spins = 0;
+                    while (ld_acquire(f) < j) {
+                        if (++spins > PIPE_SPIN_LIMIT || ld_acquire(ctl.error)) { fail = 1; break; }
+                        __nanosleep(128);
+                    }
+                }
+            }
+            fail = __any_sync(0xffffffffu, fail);
+            if (threadIdx.x == 0) {
+                s_next = next;
+                s_go = go;
+                if (fail) { atomicExch(ctl.error, 1); s_fail = 1; }
+                else if (go && j != s_j) {
+                    sF.uc = M->U[(step - 1) & 1];
+                    sF.un = M->U[step & 1];
+                    sF.dline = M->dl + (size_t)j * M->nline * 3;
+                    sF.inject_next = step + 1 < M->nt_sem ? 1 : 0;
+                    sF.seis_row = M->seis + (size_t)step * 3 * sF.ntrace;
+                    s_j = j;
+                }
+            }
+        }
+        __syncthreads();
+        if (s_fail) break;
+        if (s_go) step_tile<T, ANISO, LF, NW, ZS, true>(sF, sG, k, cx, cz, it.z, it.w, sh);
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (s_go) st_release(ctl.done + i, j + 1);
+            s_claim = ld_acquire(ctl.error) ? total : s_next;
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace sks
 
 namespace sks {
@@ -818,6 +916,14 @@ cudaError_t launch_batch_f64(const StepVariant& v, bool aniso, int blocks, cudaS
                              const BatchState* state, const int4* items, const BatchHeader* hdr, int j,
                              const Coef<double>& k);
 int batch_occupancy_f32(const StepVariant& v, bool aniso);
+cudaError_t launch_batch_pipe_f32(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                                  const BatchMember<float>* mem, const BatchState* state, const int4* items,
+                                  const BatchHeader* hdr, int nsteps, const BatchPipeCtl& ctl, const Coef<float>& k);
+cudaError_t launch_batch_pipe_f64(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                                  const BatchMember<double>* mem, const BatchState* state, const int4* items,
+                                  const BatchHeader* hdr, int nsteps, const BatchPipeCtl& ctl, const Coef<double>& k);
+int batch_pipe_occupancy_f32(const StepVariant& v, bool aniso);
+int batch_pipe_occupancy_f64(const StepVariant& v, bool aniso);
 cudaError_t launch_pipe_f32(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<float>& F,
                             const Geo<float>& G, const Coef<float>& k, const PipeChunk& C, const PipeCtl& ctl);
 cudaError_t launch_pipe_f64(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<double>& F,

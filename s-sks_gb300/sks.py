@@ -427,8 +427,9 @@ class Batch:
         _check(lib().sks_batch_get_tuning(self.h, C.byref(t)))
         return t.asdict()
 
-    def set_tuning(self, warps_per_block: int, band_rows: int, zseam: int = 0, register_cap: int = 1):
-        t = Tuning(warps_per_block, band_rows, zseam, register_cap, 0, 0, 0.0)
+    def set_tuning(self, warps_per_block: int, band_rows: int, zseam: int = 0, register_cap: int = 1,
+                   pipeline: int = 0):
+        t = Tuning(warps_per_block, band_rows, zseam, register_cap, 0, 0, 0.0, pipeline)
         _check(lib().sks_batch_set_tuning(self.h, C.byref(t)))
 
     def autotune(self, steps: int = 4) -> dict:
@@ -469,8 +470,9 @@ class Server:
         _check(lib().sks_server_create(device, budget, quantum, C.byref(self.h)))
         self.outputs: dict[int, tuple] = {}
 
-    def set_tuning(self, precision: int, warps_per_block: int, band_rows: int, zseam: int, register_cap: int):
-        t = Tuning(warps_per_block, band_rows, zseam, register_cap, 0, 0, 0.0)
+    def set_tuning(self, precision: int, warps_per_block: int, band_rows: int, zseam: int, register_cap: int,
+                   pipeline: int = 0):
+        t = Tuning(warps_per_block, band_rows, zseam, register_cap, 0, 0, 0.0, pipeline)
         _check(lib().sks_server_set_tuning(self.h, precision, C.byref(t)))
 
     def set_active_points(self, precision: int, max_points: int):

@@ -68,8 +68,12 @@ def _cat(parts):
     return tuple(np.concatenate([p[c] for p in parts]) for c in range(3))
 
 
-@pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])
-def test_batch_matches_members_alone(cases, prec):
+@pytest.mark.parametrize("prec,tuning", [(sks.FP64, TUNING + (0,)), (sks.FP32C, TUNING + (0,)),
+                                         (sks.FP64, (4, 3, 1, 0, 1)), (sks.FP32C, (4, 3, 0, 1, 1)),
+                                         (sks.FP32C, (2, 5, 1, 0, 1))])
+def test_batch_matches_members_alone(cases, prec, tuning):
+    """Per-step launches and pipelined chunks (tuning[4] = 1), with halo rows
+    and with band seams."""
     nst = [k["nst"] for k in CASES]
     ref = [_alone(d, prec, n) for d, n in zip(cases, nst)]
     assert all(max(np.abs(x).max() for x in r) > 0.05 for r in ref)
@@ -77,7 +81,8 @@ def test_batch_matches_members_alone(cases, prec):
         sol = [_open(d, prec) for d in cases]
         for s in sol:
             b.add(s)
-        b.set_tuning(*TUNING)
+        b.set_tuning(*tuning)
+        assert b.tuning()["pipeline"] == tuning[4]
         parts = [[] for _ in sol]
         for n in (1, 63, 200, 1000):            # split calls; members finish at different calls
             outs = b.run(n)
@@ -95,11 +100,12 @@ def test_batch_matches_members_alone(cases, prec):
             s.close()
 
 
-def test_batch_members_join_and_leave_between_calls(cases):
+@pytest.mark.parametrize("pipeline", [0, 1])
+def test_batch_members_join_and_leave_between_calls(cases, pipeline):
     prec = sks.FP32C
     ref = [_alone(d, prec, k["nst"]) for d, k in zip(cases, CASES)]
     with sks.Batch(prec) as b:
-        b.set_tuning(*TUNING)
+        b.set_tuning(*TUNING, pipeline)
         a = _open(cases[0], prec)
         c = _open(cases[2], prec)
         b.add(a)
