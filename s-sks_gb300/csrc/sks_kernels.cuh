@@ -373,9 +373,19 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
     pfl.on_col = ix == G.nbl;
     pfl.row_ok = ix >= G.nbl;
 
+    // x contractions: the lane's own column term first, then the element's
+    // other 4 columns in rotation (al+1, al+2, ... mod 5) by shuffle
+    int src[N];
     T Dx[NP], DWc[NP];
+    Dx[0] = k.D[al * NP + al];
+    DWc[0] = k.DWs[al * NP + al];
 #pragma unroll
-    for (int t = 0; t < NP; t++) { Dx[t] = k.D[al * NP + t]; DWc[t] = k.DWs[t * NP + al]; }
+    for (int r = 1; r < NP; r++) {
+        const int t = al + r < NP ? al + r : al + r - NP;
+        src[r - 1] = base + t;
+        Dx[r] = k.D[al * NP + t];
+        DWc[r] = k.DWs[t * NP + al];
+    }
     const T wal = k.w[al];
     // lumped-mass weight of this lane's column: inside an element, on an
     // element edge shared by two elements, or on the box's left/right edge
@@ -428,9 +438,9 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
             T dx[3], dz[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                T s = 0;
+                T s = u[bb][c] * Dx[0];
 #pragma unroll
-                for (int t = 0; t < NP; t++) s = fma(__shfl_sync(FULL, u[bb][c], base + t), Dx[t], s);
+                for (int r = 1; r < NP; r++) s = fma(__shfl_sync(FULL, u[bb][c], src[r - 1]), Dx[r], s);
                 dx[c] = s;
                 T z = 0;
 #pragma unroll
@@ -449,9 +459,9 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
             if (!halo || bb == N) {
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    T s = 0;
+                    T s = sg[c] * DWc[0];
 #pragma unroll
-                    for (int a = 0; a < NP; a++) s = fma(__shfl_sync(FULL, sg[c], base + a), DWc[a], s);
+                    for (int r = 1; r < NP; r++) s = fma(__shfl_sync(FULL, sg[c], src[r - 1]), DWc[r], s);
                     kk[bb][c] = fma(s, k.w[bb], kk[bb][c]);
                 }
             }
