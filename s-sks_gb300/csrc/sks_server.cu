@@ -36,11 +36,14 @@ struct Request {
     bool has_pw = false;
     sks_plane_wave_t pw{};
     float* out[3] = {nullptr, nullptr, nullptr};
+    // the serving thread owns the solver; what other threads read (state,
+    // status, step, bytes, times) is written under the server's mutex
     sks_solver* s = nullptr;           // while running
     int64_t est_bytes = 0, bytes = 0;
     double t_submit = -1, t_admit = -1, t_done = -1;
     int state = SKS_REQ_QUEUED;
     int status = SKS_OK;
+    int step = 0;                      // steps done, as of the last finished quantum
     int nst = 0, ntrace = 0;
     int64_t points = 0;                // grid points of the mesh
 };
@@ -96,7 +99,8 @@ struct sks_server {
     int64_t max_points[2] = {(int64_t)8 << 20, (int64_t)24 << 20};
     int64_t active_points[2] = {0, 0};
     sks_batch* batch[2] = {nullptr, nullptr};      // by precision
-    std::mutex mu;                                 // guards queue, reqs, next_id
+    std::mutex mu;                                 // guards queue, reqs, next_id, in_use and the
+                                                   // request fields other threads read
     std::deque<Request*> queue;
     std::unordered_map<int64_t, Request*> reqs;
     std::vector<Request*> active[2];
@@ -106,6 +110,33 @@ struct sks_server {
 };
 
 namespace {
+
+// A running request leaves: its solver leaves the batch and is destroyed,
+// its memory and grid points are returned, and its end state is published.
+void finish_request(sks_server* v, Request* r, int rc)
+{
+    sks_solver* s = r->s;
+    {
+        std::lock_guard<std::mutex> lk(v->mu);
+        r->s = nullptr;
+    }
+    sks_batch_remove(v->batch[r->precision], s);
+    sks_destroy(s);
+    v->active_points[r->precision] -= r->points;
+    std::lock_guard<std::mutex> lk(v->mu);
+    v->in_use -= r->bytes;
+    r->t_done = v->now();
+    r->state = rc ? SKS_REQ_FAILED : SKS_REQ_DONE;
+    r->status = rc;
+    if (!rc) r->step = r->nst;
+}
+
+// every running request of form f failed with status rc (its quantum did)
+void fail_form(sks_server* v, int f, int rc)
+{
+    for (Request* r : v->active[f]) finish_request(v, r, rc);
+    v->active[f].clear();
+}
 
 // A finished request: its seismograms to the caller, its device memory freed.
 void retire(sks_server* v, Request* r)
@@ -123,15 +154,7 @@ void retire(sks_server* v, Request* r)
         if (!rc && cudaStreamSynchronize(s->stream) != cudaSuccess)
             rc = set_err(SKS_ERR_CUDA, "copy of the seismograms of request %lld", (long long)r->id);
     }
-    sks_batch_remove(v->batch[r->precision], s);
-    sks_destroy(s);
-    r->s = nullptr;
-    v->in_use -= r->bytes;
-    v->active_points[r->precision] -= r->points;
-    r->t_done = v->now();
-    std::lock_guard<std::mutex> lk(v->mu);
-    r->state = rc ? SKS_REQ_FAILED : SKS_REQ_DONE;
-    r->status = rc;
+    finish_request(v, r, rc);
 }
 
 // open the request's solver and make it a member of its form's batch
@@ -151,13 +174,14 @@ int admit_one(sks_server* v, Request* r)
         r->t_done = v->now();
         return rc;
     }
+    v->active_points[r->precision] += r->points;
+    v->active[r->precision].push_back(r);
+    std::lock_guard<std::mutex> lk(v->mu);
     r->s = s;
     r->bytes = s->device_bytes;
     v->in_use += r->bytes;
-    v->active_points[r->precision] += r->points;
     r->t_admit = v->now();
-    v->active[r->precision].push_back(r);
-    std::lock_guard<std::mutex> lk(v->mu);
+    r->step = s->step;
     r->state = SKS_REQ_RUNNING;
     return SKS_OK;
 }
@@ -296,13 +320,21 @@ extern "C" int sks_server_step(sks_server* v)
     if (!v) return set_err(SKS_ERR_ARG, "server is NULL");
     cudaSetDevice(v->device);
     bool progressed = false;
-    // finished quanta: move steps on, retire the requests that reached their end
+    // finished quanta: move steps on, retire the requests that reached their
+    // end; a quantum that failed fails its form's running requests
     for (int f = 0; f < 2; f++) {
         sks_batch* b = v->batch[f];
         if (!batch_running(b) || !batch_done(b)) continue;
         const int rc = batch_finish(b);
-        if (rc < 0) return rc;
         progressed = true;
+        if (rc < 0) {
+            fail_form(v, f, rc);
+            continue;
+        }
+        {
+            std::lock_guard<std::mutex> lk(v->mu);
+            for (Request* r : v->active[f]) r->step = r->s->step;
+        }
         std::vector<Request*> keep;
         for (Request* r : v->active[f]) {
             if (r->s->step >= r->s->m.nst) retire(v, r);
@@ -316,7 +348,11 @@ extern "C" int sks_server_step(sks_server* v)
     for (int f = 0; f < 2; f++) {
         if (!idle[f] || v->active[f].empty()) continue;
         const int rc = batch_launch(v->batch[f], v->quantum, nullptr, nullptr, nullptr);
-        if (rc < 0) return rc;
+        if (rc < 0) {
+            if (batch_running(v->batch[f])) batch_finish(v->batch[f]);
+            fail_form(v, f, rc);
+            continue;
+        }
         progressed = true;
     }
     if (!progressed && (batch_running(v->batch[0]) || batch_running(v->batch[1])))
@@ -335,7 +371,7 @@ extern "C" int sks_server_request_info(sks_server* v, int64_t id, sks_request_in
     info->state = r->state;
     info->status = r->status;
     info->precision = r->precision;
-    info->step = r->s ? r->s->step : (r->state == SKS_REQ_DONE ? r->nst : 0);
+    info->step = r->step;
     info->nst = r->nst;
     info->ntrace = r->ntrace;
     info->submit_s = r->t_submit;
@@ -360,7 +396,12 @@ extern "C" int sks_server_release(sks_server* v, int64_t id)
 
 extern "C" double sks_server_clock(const sks_server* v) { return v ? v->now() : -1.0; }
 
-extern "C" int64_t sks_server_device_bytes(const sks_server* v) { return v ? v->in_use : -1; }
+extern "C" int64_t sks_server_device_bytes(const sks_server* v)
+{
+    if (!v) return -1;
+    std::lock_guard<std::mutex> lk(const_cast<sks_server*>(v)->mu);
+    return v->in_use;
+}
 
 extern "C" void sks_server_destroy(sks_server* v)
 {
