@@ -48,6 +48,14 @@ FULL_STEPS = 24000
 # material is a 2-byte index into a table and the inverse mass is rebuilt from
 # GLL weights): 74 B per point in both forms (LAYOUT_BYTES_PER_POINT).
 BYTES_PER_POINT = {"fp32c": 124, "fp64": 200}
+# algorithmic flops per grid-point update of the anisotropic step (an FMA is 2
+# flops, an n-term dot product 2n-1): per element row a GLL column does, for
+# each of its 5 rows, the x and z derivatives of 3 components (54), one strain
+# sum (1), the 5x5 stress (45), the x-divergence with its weight (33), the
+# z-flux scaling (3) and the z-divergence into 5 rows (30): 166 x 5 = 830, an
+# element's 5 columns 4150, over its 16 unique points 259.4; plus assembly
+# (1.5) and the 3-level update (15)
+FLOPS_PER_POINT_ANISO = 276
 LAYOUT_BYTES_PER_POINT = {"fp32c": 74, "fp64": 74}
 WORKLOAD = ("anisotropic 3-component SKS solve: 800x300 elements of 1 km, GLL degree 4, "
             "3,844,401 points, 100 km hexagonal layer (4 %, azimuth 45, tilt 20), dt 5 ms, 201 receivers")
@@ -722,6 +730,8 @@ def main() -> None:
     value = world * npts * r32["steps"] / (ms32 / 1e3)      # ms32: max over ranks (replica_rate)
     v64 = world * npts * r64["steps"] / (ms64 / 1e3)
     peak, peak_kind = _peaks()
+    import sks
+    fma_peaks = {"fp64": sks.probe_fma_peak(sks.FP64, gpu), "fp32": sks.probe_fma_peak(sks.FP32C, gpu)}
     # roofline of the dominant kernel (the fused step kernel): algorithmic
     # bytes per launch = points it updates x 124 B over its mean event-timed
     # duration; the same with the 74 B the layout actually moves beside it
@@ -755,9 +765,15 @@ def main() -> None:
         "clocks": r32.get("clocks"),
         "fp64": {"value": v64, "unit": "GLL-pt updates/s", "ms_per_step": ms64 / r64["steps"],
                  "steps": r64["steps"],
-                 "roofline": {"bound": "fp64 pipe", "kernel_ms_per_step": t64 * 1e3,
+                 "roofline": {"bound": "fp64 pipe", "achieved": npts * FLOPS_PER_POINT_ANISO / t64 / 1e12,
+                              "peak": fma_peaks["fp64"], "unit": "TFLOP/s",
+                              "frac": (npts * FLOPS_PER_POINT_ANISO / t64 / 1e12) / fma_peaks["fp64"]
+                              if fma_peaks["fp64"] else None,
+                              "peak_kind": "measured: FMA-chain probe of the FP64 pipe (sks_probe_fma_peak)",
+                              "flops_per_point": FLOPS_PER_POINT_ANISO, "kernel_ms_per_step": t64 * 1e3,
                               "achieved_gbs": npts * BYTES_PER_POINT["fp64"] / t64 / 1e9,
-                              "bytes_per_point": BYTES_PER_POINT["fp64"], "peak_gbs": peak}},
+                              "bytes_per_point": BYTES_PER_POINT["fp64"], "peak_gbs": peak,
+                              "fp32_fma_peak_tflops": fma_peaks["fp32"]}},
         "solves_per_hour": {"fp32c": 3600.0 / (FULL_STEPS * ms32 / r32["steps"] / 1e3) * world,
                             "fp64": 3600.0 / (FULL_STEPS * ms64 / r64["steps"] / 1e3) * world,
                             "solve_steps": FULL_STEPS},

@@ -320,6 +320,12 @@ double sks_last_run_ms(const sks_solver *s);
 int sks_enable_kernel_timing(sks_solver *s, int on);   /* also clears the sums */
 int sks_kernel_timing(const sks_solver *s, double *ms, int64_t *count);  /* arrays of SKS_KERNEL_CLASSES */
 
+/* Measured peak FMA throughput of the device's CUDA cores in TFLOP/s (an FMA
+ * counts 2 flops), for precision SKS_FP64 (the FP64 pipe the FP64 form is
+ * bound by) or SKS_FP32C (FP32): independent FMA chains on every SM, the best
+ * of three event-timed launches after one untimed. */
+int sks_probe_fma_peak(int device, int precision, double *tflops);
+
 /* Destroys the solver; a batch member leaves its batch first. */
 void sks_destroy(sks_solver *s);
 

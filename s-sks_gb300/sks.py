@@ -30,6 +30,7 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_get_info", "sks_setup_open", "sks_setup_info", "sks_setup_material", "sks_setup_mass",
            "sks_setup_receivers", "sks_setup_schedule", "sks_setup_close", "sks_open_setup",
            "sks_kernel_launches", "sks_last_run_ms", "sks_enable_kernel_timing", "sks_kernel_timing",
+           "sks_probe_fma_peak",
            "sks_set_tuning", "sks_get_tuning", "sks_autotune", "sks_line_increments",
            "sks_line_increments_noalloc", "sks_set_boundary_plane_wave", "sks_snapshot",
            "sks_state_bytes", "sks_state_save", "sks_state_load",
@@ -131,6 +132,7 @@ def lib() -> C.CDLL:
         L.sks_last_run_ms.restype = C.c_double
         L.sks_enable_kernel_timing.argtypes = [vp, C.c_int]
         L.sks_kernel_timing.argtypes = [vp, dp, C.POINTER(C.c_int64)]
+        L.sks_probe_fma_peak.argtypes = [C.c_int, C.c_int, dp]
         L.sks_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
         L.sks_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
         L.sks_autotune.argtypes = [vp, C.c_int32, C.POINTER(Tuning)]
@@ -530,6 +532,13 @@ class Server:
 
 
 # ---- model builder --------------------------------------------------------
+def probe_fma_peak(precision: int, device: int = 0) -> float:
+    """Measured peak FMA throughput of the device's CUDA cores (TFLOP/s) for the FP64 or FP32 pipe."""
+    t = C.c_double(0.0)
+    _check(lib().sks_probe_fma_peak(device, precision, C.byref(t)))
+    return t.value
+
+
 def _d(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 

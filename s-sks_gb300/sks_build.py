@@ -50,7 +50,7 @@ def build(verbose: bool = False) -> str:
          ["gcc", "-O2", "-std=gnu11", "-fPIC", "-Wall", "-I" + INC, "-c"]) for c in ("sks_model", "sks_elastic")
     ]
     for cu in ("sks_solver", "sks_batch", "sks_server", "sks_step_f32", "sks_step_f64", "sks_batch_f32", "sks_batch_f64",
-               "sks_noalloc", "sks_post"):
+               "sks_noalloc", "sks_post", "sks_probe"):
         units.append((os.path.join(CSRC, cu + ".cu"), os.path.join(OUT, cu + ".o"),
                       [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC,
                        "-c"]))
