@@ -804,9 +804,11 @@ k_step_pipe(Field<T> F, Geo<T> G, Coef<T> k, PipeChunk C, PipeCtl ctl)
         __syncthreads();
         if (s_fail) break;
         step_tile<T, ANISO, LF, NW, ZS, true>(sF, G, k, cx, cz, cz * G.HZ, min(cz * G.HZ + G.HZ, G.nez), sh);
-        __threadfence();
+        // the CTA's stores are ordered before thread 0's fence by the barrier
+        // (fences are cumulative), so one fence publishes the whole tile
         __syncthreads();
         if (threadIdx.x == 0) {
+            __threadfence();
             st_release(ctl.done + t, st + 1);
             s_claim = ld_acquire(ctl.error) ? total : s_next;
         }
@@ -901,9 +903,9 @@ k_step_batch_pipe(const BatchMember<T>* __restrict__ mem, const BatchState* __re
         __syncthreads();
         if (s_fail) break;
         if (s_go) step_tile<T, ANISO, LF, NW, ZS, true>(sF, sG, k, cx, cz, it.z, it.w, sh);
-        __threadfence();
         __syncthreads();
         if (threadIdx.x == 0) {
+            __threadfence();                // publishes the whole tile (see k_step_pipe)
             if (s_go) st_release(ctl.done + i, j + 1);
             s_claim = ld_acquire(ctl.error) ? total : s_next;
         }
