@@ -171,6 +171,32 @@ int sks_split_scratch(int32_t ntrace, int32_t nt, double dt, const sks_split_opt
 int sks_split_traces(const float *radial, const float *transverse, int32_t ntrace, int32_t nt, int64_t ld,
                      double dt, const sks_split_opts_t *o, float *work, double *sums, float *out, void *stream);
 
+/* SAC files of a solve's seismograms, as the reference's uvw2sac writes them
+ * (semsyn/plot/uvw2sac.c).  sks_sac_write writes one SAC version 6 binary file
+ * (host byte order): the fields below, iftype = time series, leven = 1,
+ * nvhdr = 6, npts; every other header word unset (-12345).
+ * sks_sac_fields_init sets every field unset. */
+typedef struct {
+    float delta, b, e, o;          /* sample interval, begin, end, origin (s)   */
+    float evla, evlo, evdp;        /* event latitude, longitude, depth          */
+    float stla, stlo, stel;        /* station latitude, longitude, elevation    */
+    float gcarc, cmpaz, cmpinc;    /* distance (deg), component azimuth, incidence */
+    int32_t nzyear, nzjday, nzhour, nzmin, nzsec, nzmsec;   /* reference time  */
+    char kstnm[9];                 /* station name (8 characters)               */
+} sks_sac_fields_t;
+
+void sks_sac_fields_init(sks_sac_fields_t *f);
+int sks_sac_write(const char *path, int32_t npts, const float *data, const sks_sac_fields_t *f);
+
+/* The uvw2sac program: par words as the reference reads them (raymodel, nex,
+ * nst, hpn, eh, dp, sdt, kdt, xmin, tstart, xtrace, ztrace, zbeg, idzplot, xbeg,
+ * idxplot, zs, get_rec/rec_file, enlarge, fix_rec/pos_file/baz, Conv_Source);
+ * reads seis.u/v/w from dir (NULL: the working directory) and writes there, per
+ * receiver n, n.ce / n.cn / n.cz (every second record, times enlarge), log.txt
+ * and pm.xy.  Conv_Source=1 (a source time function convolved by Fortran
+ * routines outside the reference tree) returns SKS_ERR_UNSUPPORTED. */
+int sks_uvw2sac(int argc, const char *const *argv, const char *dir);
+
 /* Restart: a solve's state (both displacement buffers, the FP32C increment
  * and compensation, the step, taken snapshots) copied to host memory and
  * back, for checkpoints and for preempting a served solve.  A saved state

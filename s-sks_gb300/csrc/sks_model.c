@@ -697,6 +697,63 @@ done:
     return rc;
 }
 
+/* the element size and GLL spacing as the reference computes them in float,
+ * and the element rows, from the ray model's box height (sem2d_psvsh.c:592-606;
+ * semsyn/plot/uvw2sac.c:137-155 repeats the computation) */
+int sks_mesh_spacing(const char *raymodel, int flat, int nfil, float eh_par, int hpn, int *nez, float *eh_f, float *h_f,
+                     char *err, size_t errlen)
+{
+    Ray r;
+    int i, rc;
+    float thick_f = 0.f;
+    memset(&r, 0, sizeof r);
+    rc = ray_read(&r, raymodel, flat, err, errlen);
+    if (rc) { ray_free(&r); return rc; }
+    if (nfil > r.nrec) {
+        for (i = r.nrec; i < nfil && i < r.jo; i++) thick_f += r.thk_f[i];
+    } else {
+        for (i = nfil - 1; i < r.nrec - 1; i++) thick_f += r.thk_f[i];
+    }
+    ray_free(&r);
+    if (!(eh_par > 0.f) || hpn < 1) ERR(SKS_ERR_ARG, "eh=%g hpn=%d", eh_par, hpn);
+    *nez = (int)((thick_f - 1.e-3) / eh_par);
+    if (*nez < 1) ERR(SKS_ERR_MODEL, "ray model gives a box of %.6g km: no element rows of %g km", thick_f, eh_par);
+    *eh_f = (float)((thick_f - 1.e-3) / *nez);
+    *h_f = *eh_f / hpn;
+    return SKS_OK;
+}
+
+/* the values of the named par words (NULL when absent; the last occurrence
+ * wins, par=FILE splices files as above); the caller frees them */
+int sks_par_lookup(int argc, const char *const *argv, int n, const char *const *names, char **values, char *err,
+                   size_t errlen)
+{
+    Words ws = {0, 0, 0};
+    int rc = SKS_OK, i;
+    for (i = 0; i < n; i++) values[i] = NULL;
+    for (i = 1; i < argc; i++) {
+        const char *a = argv[i], *eq;
+        while (*a == ' ' || *a == '\t') a++;
+        eq = strchr(a, '=');
+        if (!eq) { words_add(&ws, a, strlen(a), "", 0); continue; }
+        words_add(&ws, a, (size_t)(eq - a), eq + 1, strlen(eq + 1));
+        if (eq - a == 3 && !strncmp(a, "par", 3)) {
+            rc = words_file(&ws, eq + 1, 1, err, errlen);
+            if (rc) break;
+        }
+    }
+    if (!rc)
+        for (i = 0; i < n; i++) {
+            const char *v = words_get(&ws, names[i]);
+            if (v) {
+                values[i] = (char *)malloc(strlen(v) + 1);
+                strcpy(values[i], v);
+            }
+        }
+    words_free(&ws);
+    return rc;
+}
+
 void sks_model_free(sks_model *m)
 {
     free(m->mat); free(m->mat_id); free(m->mass); free(m->ab); free(m->rec_off);

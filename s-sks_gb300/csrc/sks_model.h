@@ -72,6 +72,12 @@ __attribute__((visibility("hidden")))
 int  sks_model_from_par(sks_model *m, int argc, const char *const *argv, char *err, size_t errlen);
 __attribute__((visibility("hidden")))
 void sks_model_free(sks_model *m);
+__attribute__((visibility("hidden")))
+int  sks_mesh_spacing(const char *raymodel, int flat, int nfil, float eh_par, int hpn, int *nez, float *eh_f,
+                      float *h_f, char *err, size_t errlen);
+__attribute__((visibility("hidden")))
+int  sks_par_lookup(int argc, const char *const *argv, int n, const char *const *names, char **values, char *err,
+                    size_t errlen);
 
 /* Stacey boundary-point index (-1 off the absorbing edges): left column,
  * bottom row, right column, then top-row points 1..3N (sem2d_psvsh.c:1834-1892) */

@@ -36,6 +36,7 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_state_bytes", "sks_state_save", "sks_state_load",
            "sks_elastic_rotate", "sks_elastic_dip", "sks_christoffel", "sks_semmodel_write",
            "sks_bandpass_design", "sks_split_scratch", "sks_split_traces",
+           "sks_sac_fields_init", "sks_sac_write", "sks_uvw2sac",
            "sks_batch_create", "sks_batch_add", "sks_batch_remove", "sks_batch_size", "sks_batch_run",
            "sks_batch_set_tuning", "sks_batch_get_tuning", "sks_batch_autotune", "sks_batch_last_run_ms",
            "sks_batch_kernel_launches", "sks_batch_destroy",
@@ -91,6 +92,13 @@ class PlaneWave(C.Structure):
                 ("sh_amp", C.c_double)]
 
 
+class SacFields(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("delta", "b", "e", "o", "evla", "evlo", "evdp", "stla", "stlo", "stel",
+                                          "gcarc", "cmpaz", "cmpinc")] + \
+               [(n, C.c_int32) for n in ("nzyear", "nzjday", "nzhour", "nzmin", "nzsec", "nzmsec")] + \
+               [("kstnm", C.c_char * 9)]
+
+
 class Tuning(C.Structure):
     _fields_ = [("warps_per_block", C.c_int32), ("band_rows", C.c_int32), ("zseam", C.c_int32),
                 ("register_cap", C.c_int32), ("waves", C.c_int32), ("blocks", C.c_int32),
@@ -133,6 +141,10 @@ def lib() -> C.CDLL:
         L.sks_enable_kernel_timing.argtypes = [vp, C.c_int]
         L.sks_kernel_timing.argtypes = [vp, dp, C.POINTER(C.c_int64)]
         L.sks_probe_fma_peak.argtypes = [C.c_int, C.c_int, dp]
+        L.sks_sac_fields_init.argtypes = [C.POINTER(SacFields)]
+        L.sks_sac_fields_init.restype = None
+        L.sks_sac_write.argtypes = [C.c_char_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(SacFields)]
+        L.sks_uvw2sac.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_char_p]
         L.sks_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
         L.sks_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
         L.sks_autotune.argtypes = [vp, C.c_int32, C.POINTER(Tuning)]
@@ -532,6 +544,22 @@ class Server:
 
 
 # ---- model builder --------------------------------------------------------
+def sac_write(path: str, data, **fields):
+    """One SAC file (sks_sac_write): header fields by name (SacFields), the rest unset."""
+    f = SacFields()
+    lib().sks_sac_fields_init(C.byref(f))
+    for k, v in fields.items():
+        setattr(f, k, v.encode() if k == "kstnm" else v)
+    a = np.ascontiguousarray(data, dtype=np.float32)
+    _check(lib().sks_sac_write(path.encode(), a.size, a.ctypes.data_as(C.POINTER(C.c_float)), C.byref(f)))
+
+
+def uvw2sac(words, directory: str | None = None):
+    """The uvw2sac program (sks_uvw2sac) on par words, reading seis.u/v/w in `directory`."""
+    n, arr = _argv(words)
+    _check(lib().sks_uvw2sac(n, arr, directory.encode() if directory else None))
+
+
 def probe_fma_peak(precision: int, device: int = 0) -> float:
     """Measured peak FMA throughput of the device's CUDA cores (TFLOP/s) for the FP64 or FP32 pipe."""
     t = C.c_double(0.0)

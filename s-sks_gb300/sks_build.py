@@ -47,7 +47,8 @@ def build(verbose: bool = False) -> str:
         "sks_step_inst.cuh", "sks_batch_inst.cuh")]
     units = [
         (os.path.join(CSRC, c + ".c"), os.path.join(OUT, c + ".o"),
-         ["gcc", "-O2", "-std=gnu11", "-fPIC", "-Wall", "-I" + INC, "-c"]) for c in ("sks_model", "sks_elastic")
+         ["gcc", "-O2", "-std=gnu11", "-fPIC", "-Wall", "-I" + INC, "-c"]) for c in ("sks_model", "sks_elastic",
+                                                                                    "sks_sac")
     ]
     for cu in ("sks_solver", "sks_batch", "sks_server", "sks_step_f32", "sks_step_f64", "sks_batch_f32", "sks_batch_f64",
                "sks_noalloc", "sks_post", "sks_probe"):
@@ -73,6 +74,11 @@ def build(verbose: bool = False) -> str:
         if os.path.lexists(link):
             os.remove(link)
         os.symlink("sem2d_psvsh_gb300", link)
+    conv = os.path.join(OUT, "uvw2sac_gb300")
+    conv_c = os.path.join(CSRC, "uvw2sac_main.c")
+    if _stale(conv, [conv_c, LIB]):
+        _run(["gcc", "-O2", "-std=gnu11", "-I" + INC, "-o", conv, conv_c, "-L" + OUT, "-lsks_gb300",
+              "-Wl,-rpath,$ORIGIN"])
     if verbose:
         print("built", LIB)
     return LIB

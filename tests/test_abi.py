@@ -43,6 +43,7 @@ def test_cli_is_built():
     cli = os.path.join(os.path.dirname(sks.LIB_PATH), "sem2d_psvsh_gb300")
     assert os.access(cli, os.X_OK)
     assert os.path.islink(os.path.join(os.path.dirname(sks.LIB_PATH), "sem2d_gb300"))
+    assert os.access(os.path.join(os.path.dirname(sks.LIB_PATH), "uvw2sac_gb300"), os.X_OK)
 
 
 def test_error_string_after_failure():
