@@ -767,6 +767,7 @@ extern "C" int sks_run(sks_solver* s, int32_t nsteps, float* su, float* sv, floa
 {
     if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
     if (nsteps < 0) return set_err(SKS_ERR_ARG, "nsteps=%d", nsteps);
+    if (s->batch && batch_running(s->batch)) return set_err(SKS_ERR_STATE, "the solver's batch is running");
     const sks_model& m = s->m;
     if (s->step < m.nt_sem && !s->boundary_ready)
         return set_err(SKS_ERR_STATE, "boundary records not set: call sks_load_boundary_files or sks_set_boundary");
@@ -845,6 +846,7 @@ extern "C" int sks_run(sks_solver* s, int32_t nsteps, float* su, float* sv, floa
 extern "C" int sks_reset(sks_solver* s)
 {
     if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    if (s->batch && batch_running(s->batch)) return set_err(SKS_ERR_STATE, "the solver's batch is running");
     s->step = 0;
     s->cur = 0;
     s->g_last = 0;
@@ -892,6 +894,7 @@ extern "C" int sks_state_save(sks_solver* s, void* host, int64_t bytes)
 {
     if (!s || !host) return set_err(SKS_ERR_ARG, "NULL argument");
     if (bytes < sks_state_bytes(s)) return set_err(SKS_ERR_ARG, "state buffer of %lld bytes, %lld needed", (long long)bytes, (long long)sks_state_bytes(s));
+    if (s->batch && batch_running(s->batch)) return set_err(SKS_ERR_STATE, "the solver's batch is running");
     cudaSetDevice(s->device);
     void* const* p[3];
     size_t sz[3];
