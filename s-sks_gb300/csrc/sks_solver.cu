@@ -553,12 +553,29 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         return set_err(SKS_ERR_UNSUPPORTED, "mesh of %d x %d points: 3*nx*nz must stay below 2^31", m.nx, m.nz);
     }
     {
-        // defaults from sweeps on the 3.8 M-point anisotropic mesh: FP32 runs
-        // best with many short bands and registers capped for 16 warps/SM,
-        // FP64 (bound by the FP64 pipe) with fewer, taller bands
+        // defaults from sweeps on a GB300 (what sks_autotune would pick, without
+        // its cost).  Up to 2 M points: one balanced wave of CTAs (the 0.32 M-
+        // point mesh: 0.018 ms per FP32C step against 0.024 for the next best).
+        // Above: pipelined chunks -- FP32C with halo rows in bands of 8
+        // (3.8 M points: 0.091 ms against 0.102 per-step), FP64 with band
+        // seams in bands of 6 (1.28 ms against 1.43) -- except FP32C above
+        // 16 M points, where per-step launches of 12-row bands win (64 M
+        // points: 1.26 ms against 1.43 pipelined).  One wave of tall bands is
+        // not used on large meshes: with fewer CTA slots than twice the
+        // element columns its bands differ in height by up to 2x (FP64, 64 M
+        // points: 30.5 ms against 21.1).
         const int ncx4 = (m.nex + (TEX * 4 - 1) - 1) / (TEX * 4 - 1);
-        const int rcg = precision == SKS_FP32C ? set_grid(s, 4, pick_band(m, ncx4, sms, 10), 0, 1, 1)
-                                               : set_grid(s, 4, pick_band(m, ncx4, sms, 5), 1, 0, 1);
+        const int64_t pts = (int64_t)m.nx * m.nz;
+        int rcg;
+        if (pts <= ((int64_t)2 << 20))
+            rcg = precision == SKS_FP32C ? set_grid(s, 4, pick_band(m, ncx4, sms, 10), 0, 1, 1)
+                                         : set_grid(s, 4, pick_band(m, ncx4, sms, 5), 1, 0, 1);
+        else if (precision == SKS_FP64)
+            rcg = set_grid(s, 4, 6, 1, 1, 0, 1);
+        else if (pts <= ((int64_t)16 << 20))
+            rcg = set_grid(s, 4, 8, 0, 1, 0, 1);
+        else
+            rcg = set_grid(s, 4, 12, 0, 1, 0, 0);
         if (rcg) { free_device(s); cudaStreamDestroy(s->stream); sks_model_free(&s->m); delete s; return rcg; }
     }
     s->chunk = 64;
