@@ -244,6 +244,15 @@ extern "C" int sks_server_create(int device, int64_t budget, int32_t quantum, sk
     // FP32C quanta are short and many; FP64 quanta long: FP32C first
     if (!rc) rc = batch_set_priority(v->batch[SKS_FP32C], true);
     if (!rc) rc = batch_set_priority(v->batch[SKS_FP64], false);
+    // tunings measured on the served workload (FP32C requests at saturation:
+    // pipelined chunks of 12-row bands, 14,437 solves/h against 14,044 with
+    // per-step launches of 6-row bands); sks_server_set_tuning overrides them
+    if (!rc) {
+        sks_tuning_t t32 = {4, 12, 0, 1, 0, 0, 0.f, 1};
+        sks_tuning_t t64 = {4, 8, 1, 0, 0, 0, 0.f, 0};
+        rc = sks_batch_set_tuning(v->batch[SKS_FP32C], &t32);
+        if (!rc) rc = sks_batch_set_tuning(v->batch[SKS_FP64], &t64);
+    }
     if (rc) {
         sks_batch_destroy(v->batch[0]);
         sks_batch_destroy(v->batch[1]);
