@@ -44,3 +44,71 @@ def test_vertical_sks_splits_by_the_layer(case, prec):
         assert abs(res["phi_deg"] - AZ) <= 2.0, (r, res)
         assert abs(res["delay_s"] - want) <= 0.03, (r, res, want)
         assert res["lambda_ratio"] < 0.01
+
+
+def _state_fields(st, nx, nz, prec):
+    """views into a saved state: U0, U1 as [3][np] arrays in the buffer's
+    layout ((u_x, u_z) pairs, then u_y) and, for FP32C, the (d, c) pairs"""
+    np_ = nx * nz
+    dt = np.float64 if prec == sks.FP64 else np.float32
+    el = np.dtype(dt).itemsize
+    o = 88
+    u0 = np.frombuffer(st, dtype=dt, count=3 * np_, offset=o)
+    u1 = np.frombuffer(st, dtype=dt, count=3 * np_, offset=o + 3 * np_ * el)
+    dv = np.frombuffer(st, dtype=np.float32, count=6 * np_, offset=o + 6 * np_ * el) if prec == sks.FP32C else None
+    return u0, u1, dv
+
+
+def _layout(ux, uy, uz):
+    return np.concatenate([np.stack([ux, uz], axis=1).ravel(), uy])
+
+
+@pytest.mark.parametrize("prec,tol", [(sks.FP64, 1e-12), (sks.FP32C, 2e-5)])
+@pytest.mark.parametrize("motion", ["translation", "rotation"])
+def test_rigid_motions_stay_at_rest(tmp_path, prec, tol, motion):
+    """K annihilates rigid motions: a uniform displacement, or a small rigid
+    rotation of the x-z plane (zero strain; exact through the degree-4 GLL
+    derivatives), loaded as the state of a solve with no incident wave, stays
+    where it is -- inside, on the free surface and on the absorbing edges."""
+    d = str(tmp_path)
+    layers = [synth.SemLayer(10.0, synth.iso_cij(8.1, 4.5, 3.4), 3.4),
+              synth.SemLayer(20.5, synth.hexagonal_cij(7.0, 4.0, 3.0, 0.05, 35.0, 20.0), 3.0)]
+    c = synth.Case(nex=24, nez=10, eh=2.0, sdt=0.01, nst=260, layers=layers, p=0.04, f0=1.0, ntrace=5, rec_dx=4.0,
+                   semmodel_full=True, write_records=False)
+    summ = synth.write_case(c, d)
+    with chdir(d):
+        s = sks.Solver(["par=run.par"], precision=prec)
+    s.set_boundary_plane_wave(summ["vs"], c.p, c.f0, 0.0, 0.0)      # no incident wave
+    s.run(10)
+    info = s.info()
+    nx, nz = info["nx"], info["nz"]
+    st = s.save_state().copy()
+    u0, u1, dv = _state_fields(st, nx, nz, prec)
+    # node coordinates: GLL points of degree 4 inside each element (not evenly spaced)
+    eh = info["eh"]
+    xi = np.array([-1.0, -np.sqrt(3.0 / 7.0), 0.0, np.sqrt(3.0 / 7.0), 1.0])
+
+    def coord(i):
+        e, a = np.divmod(i, 4)
+        return e * eh + (xi[a] + 1.0) * eh / 2.0
+
+    z, x = np.meshgrid(coord(np.arange(nz)), coord(np.arange(nx)), indexing="ij")
+    if motion == "translation":
+        ux, uy, uz = np.full(nx * nz, 0.7), np.full(nx * nz, -0.4), np.full(nx * nz, 0.25)
+    else:
+        a = 1e-3                                                   # radians
+        ux, uy, uz = (a * (z - 10.0)).ravel(), np.zeros(nx * nz), (-a * (x - 24.0)).ravel()
+    field = _layout(ux, uy, uz)
+    np.copyto(u0, field.astype(u0.dtype))
+    np.copyto(u1, field.astype(u1.dtype))
+    if dv is not None:
+        np.copyto(dv, 0.0)
+    s.load_state(st)
+    s.run(200)
+    after = s.save_state()
+    a0, a1, _ = _state_fields(after, nx, nz, prec)
+    scale = np.abs(field).max()
+    for arr in (a0, a1):
+        err = np.abs(arr.astype(np.float64) - field).max() / scale
+        assert err <= tol, (motion, err)
+    s.close()
