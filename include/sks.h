@@ -89,7 +89,9 @@ int sks_set_boundary(sks_solver *s, const float *psv, int32_t nrec_psv,
  * P-SV (SV polarisation) and SH wave in the bottom layer, velocity vs (km/s),
  * ray parameter p (s/km), Ricker pulse of dominant frequency f0 (Hz) centred
  * at 1.5/f0 s, sampled every dp (the par file's) on the interface row and
- * column, in the layout of greenfile/shgreenfile.  Stands in for the
+ * column at their GLL node positions (as the reference's generator places
+ * them, semsyn/src/aserpsv_sem.c:887-920), in the layout of
+ * greenfile/shgreenfile.  Stands in for the
  * reference's boundary-trace producers (semsyn/src/aserpsv_sem.c:319-488 and
  * the record splitting of demult.c:63-78) for plane-wave runs, with no file
  * round trip; the records equal the host generator's (s-sks_gb300/synth.py)

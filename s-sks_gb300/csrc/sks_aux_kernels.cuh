@@ -289,16 +289,27 @@ __device__ __forceinline__ double ricker_at(double t, double pf)
     return __dmul_rn(__dsub_rn(1.0, __dmul_rn(2.0, a)), exp(-a));
 }
 
+// coordinate of grid point j along a row or column of degree-4 elements of
+// size eh: element j/4, GLL node j%4 at e*eh + (xi + 1)*eh/2 -- the node
+// positions of the reference's boundary-trace generator
+// (semsyn/src/aserpsv_sem.c:887-920), in the host generator's operation order
+__device__ __forceinline__ double gll_pos(int j, double eh)
+{
+    const double xi[4] = {-1.0, -0.6546536707079771, 0.0, 0.6546536707079771};
+    return __dadd_rn(__dmul_rn((double)(j >> 2), eh), __ddiv_rn(__dmul_rn(__dadd_rn(xi[j & 3], 1.0), eh), 2.0));
+}
+
 static __global__ void __launch_bounds__(256) k_plane_wave(float* __restrict__ psv, float* __restrict__ sh, int nrec_psv,
-                                                    int nrec_sh, int nx, int nz, double h, int nbl, double vs,
+                                                    int nrec_sh, int nx, int nz, double eh, int nbl, double vs,
                                                     double p, double f0, double dp, double sv_amp, double sh_amp)
 {
     const int mtotal = 2 * (nx + nz), shtotal = nx + nz;
     const double eta = sqrt(fmax(__dsub_rn(__ddiv_rn(1.0, __dmul_rn(vs, vs)), __dmul_rn(p, p)), 0.0));
     const double delay = __ddiv_rn(1.5, f0);
     const double pf = __dmul_rn(3.141592653589793, f0);
-    const double zb = __dmul_rn(eta, __dmul_rn((double)nbl, h));   // eta * (nbl h)
-    const double xl = __dmul_rn(p, __dmul_rn((double)nbl, h));     // p * (nbl h)
+    const double line = gll_pos(nbl, eh);                          // height of row nbl = x of column nbl
+    const double zb = __dmul_rn(eta, line);
+    const double xl = __dmul_rn(p, line);
     const double ux = __dmul_rn(__dmul_rn(sv_amp, eta), vs), uz = __dmul_rn(__dmul_rn(-sv_amp, p), vs);
     const int64_t n1 = (int64_t)nrec_psv * mtotal, n2 = (int64_t)nrec_sh * shtotal;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n1 + n2; i += (int64_t)gridDim.x * blockDim.x) {
@@ -317,8 +328,8 @@ static __global__ void __launch_bounds__(256) k_plane_wave(float* __restrict__ p
             part = c >= nx ? 1 : 0;
             j = part ? c - nx : c;
         }
-        if (!part) tau = __dadd_rn(__dmul_rn(p, __dmul_rn((double)j, h)), zb);
-        else tau = __dadd_rn(xl, __dmul_rn(eta, __dmul_rn((double)j, h)));
+        if (!part) tau = __dadd_rn(__dmul_rn(p, gll_pos(j, eh)), zb);
+        else tau = __dadd_rn(xl, __dmul_rn(eta, gll_pos(j, eh)));
         const double rk = ricker_at(__dsub_rn(__dsub_rn(t, delay), tau), pf);
         if (fam_sh) {
             sh[k] = (float)__dmul_rn(sh_amp, rk);

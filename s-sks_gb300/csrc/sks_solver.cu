@@ -722,7 +722,7 @@ extern "C" int sks_set_boundary_plane_wave(sks_solver* s, const sks_plane_wave_t
     const int64_t tot = (int64_t)m.nrec_psv * m.mtotal + (int64_t)m.nrec_sh * m.shtotal;
     if (tot > 0) {
         const int blocks = (int)std::min<int64_t>((tot + 255) / 256, (int64_t)s->sms * 16);
-        k_plane_wave<<<blocks, 256, 0, s->stream>>>(s->rec_psv, s->rec_sh, m.nrec_psv, m.nrec_sh, m.nx, m.nz, m.h, s->nbl,
+        k_plane_wave<<<blocks, 256, 0, s->stream>>>(s->rec_psv, s->rec_sh, m.nrec_psv, m.nrec_sh, m.nx, m.nz, m.eh, s->nbl,
                                                     pw->vs, pw->p, pw->f0, m.dp, pw->sv_amp, sh_amp);
         CK(cudaGetLastError());
     }

@@ -190,7 +190,7 @@ def write_case(case: Case, d: str, absolute: bool = False) -> dict:
     if case.write_records:
         write_plane_wave(os.path.join(d, "greenfile"), os.path.join(d, "shgreenfile"),
                          nx=nx, nz=nz, h=h, nbl=nbl, vs=vs_b, p=case.p, f0=case.f0,
-                         dp=dp, nt=nt, sv_amp=case.sv_amp, sh_amp=case.sh_amp)
+                         dp=dp, nt=nt, sv_amp=case.sv_amp, sh_amp=case.sh_amp, eh=float(eh_eff))
     name = (lambda f: os.path.join(os.path.abspath(d), f)) if absolute else (lambda f: f)
     par = {
         "greenfile": name("greenfile"), "shgreenfile": name("shgreenfile"), "raymodel": name("raymodel"),
@@ -216,14 +216,30 @@ def ricker(t: np.ndarray, f0: float) -> np.ndarray:
     return (1.0 - 2.0 * a) * np.exp(-a)
 
 
-def plane_wave_records(nx, nz, h, nbl, vs, p, f0, dp, r0, r1, sv_amp=1.0, sh_amp=0.0):
-    """Records r0..r1-1 of the boundary traces (float32, time-major)."""
+GLL4 = (-1.0, -0.6546536707079771, 0.0, 0.6546536707079771, 1.0)    # GLL points of degree 4
+
+
+def gll_positions(n: int, eh: float) -> np.ndarray:
+    """Coordinates of grid points 0..n-1 along a row or column of degree-4
+    elements of size eh: point 4e+m at e*eh + (xi_m + 1)*eh/2, the node
+    positions the reference's boundary-trace generator uses
+    (semsyn/src/aserpsv_sem.c:887-920, Grid_Point)."""
+    e, m = np.divmod(np.arange(n), 4)
+    return e * eh + (np.array(GLL4)[m] + 1.0) * eh / 2.0
+
+
+def plane_wave_records(nx, nz, h, nbl, vs, p, f0, dp, r0, r1, sv_amp=1.0, sh_amp=0.0, eh=None):
+    """Records r0..r1-1 of the boundary traces (float32, time-major), the
+    plane wave timed at the GLL node positions of the line (eh: the element
+    size, 4h when not given)."""
+    eh = 4.0 * h if eh is None else eh
     eta = math.sqrt(max(1.0 / vs ** 2 - p ** 2, 0.0))
     delay = 1.5 / f0
-    xb = np.arange(nx) * h                     # bottom line, height nbl*h
-    zl = np.arange(nz) * h                     # left column, x = nbl*h
-    tau_b = p * xb + eta * (nbl * h)
-    tau_l = p * (nbl * h) + eta * zl
+    xb = gll_positions(nx, eh)                 # bottom line, at the height of row nbl
+    zl = gll_positions(nz, eh)                 # left column, at the position of column nbl
+    line = gll_positions(nbl + 1, eh)[nbl]
+    tau_b = p * xb + eta * line
+    tau_l = p * line + eta * zl
     t = (np.arange(r0, r1) * dp)[:, None]
     rb = ricker(t - delay - tau_b[None, :], f0)
     rl = ricker(t - delay - tau_l[None, :], f0)
@@ -234,11 +250,11 @@ def plane_wave_records(nx, nz, h, nbl, vs, p, f0, dp, r0, r1, sv_amp=1.0, sh_amp
 
 
 def write_plane_wave(psv_path, sh_path, *, nx, nz, h, nbl, vs, p, f0, dp, nt,
-                     sv_amp=1.0, sh_amp=0.0, chunk=1024):
+                     sv_amp=1.0, sh_amp=0.0, chunk=1024, eh=None):
     with open(psv_path, "wb") as fp, open(sh_path, "wb") as fs:
         for r0 in range(0, nt, chunk):
             psv, sh = plane_wave_records(nx, nz, h, nbl, vs, p, f0, dp, r0, min(nt, r0 + chunk),
-                                         sv_amp, sh_amp)
+                                         sv_amp, sh_amp, eh)
             fp.write(psv.tobytes())
             fs.write(sh.tobytes())
 

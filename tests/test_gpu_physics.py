@@ -179,3 +179,50 @@ def test_energy_is_conserved_without_absorbing_edges(tmp_path):
     assert e0 > 0
     assert abs(e1 - e0) <= 1e-10 * e0, (e0, e1)
     s.close()
+
+
+@pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])
+def test_plane_sh_wave_in_a_homogeneous_box(tmp_path, prec):
+    """A plane SH wave (p = 0.04 s/km, 0.3 Hz Ricker) in a homogeneous box
+    against the analytic solution.  Inside the box, before the free-surface
+    reflection comes back down, the snapshots follow R(t - t0 - p x - eta z)
+    with eta = sqrt(1/vs^2 - p^2): same shape and timing, amplitude constant in
+    time (the injection of the line's record increments scales the incident
+    wave by a constant, 2.24 here, the same in the reference's scheme).  At the
+    free surface the seismogram is the incident wave doubled."""
+    import math
+    d = str(tmp_path)
+    vs, p, f0, dt = 4.5, 0.04, 0.3, 0.005
+    layers = [synth.SemLayer(41.002, synth.iso_cij(8.1, vs, 3.4), 3.4)]
+    c = synth.Case(nex=80, nez=40, eh=1.0, sdt=dt, nst=3300, layers=layers, p=p, f0=f0, sv_amp=0.0, sh_amp=1.0,
+                   ntrace=3, rec_x0=30.0, rec_dx=10.0, write_records=False,
+                   extra={"plot_snap": 1, "startsnap": 1900, "incresnap": 100})
+    summ = synth.write_case(c, d)
+    with chdir(d):
+        s = sks.Solver(["par=run.par"], precision=prec)
+    s.set_boundary_plane_wave(summ["vs"], p, f0, 0.0, 1.0)
+    _, v, _ = s.run(c.nst)
+    info = s.info()
+    nx, nz, eh = info["nx"], info["nz"], info["eh"]
+    xs, zs = synth.gll_positions(nx, eh), synth.gll_positions(nz, eh)
+    eta = math.sqrt(1.0 / vs ** 2 - p ** 2)
+    amps = []
+    for k in range(7):                                   # steps 1900 .. 2500: the pulse between 13 and 27 km
+        step, snap = s.snapshot(k)
+        col = snap[80, :, 1].astype(np.float64)          # u_y on the column x = 40 km (every second point)
+        want = synth.ricker(step * dt - 1.5 / f0 - (p * xs[160] + eta * zs[0::2][:col.size]), f0)
+        assert np.dot(col, want) / np.linalg.norm(col) / np.linalg.norm(want) >= 0.999, step
+        assert abs(np.argmax(np.abs(col)) - np.argmax(np.abs(want))) <= 1, step
+        amps.append(np.dot(col, want) / np.dot(want, want))
+    A = float(np.mean(amps))
+    assert max(abs(a - A) for a in amps) <= 0.01 * A
+    # the receiver at x = 50 km on the free surface: twice the incident wave
+    ix = int(round(50.0 / info["h"]))
+    t = np.arange(c.nst) * dt
+    want = synth.ricker(t - 1.5 / f0 - (p * xs[ix] + eta * zs[-1]), f0)
+    got = v[:, 2].astype(np.float64)
+    lag = max(range(-4, 5), key=lambda L: np.dot(np.roll(want, L), got))
+    w = np.roll(want, lag)
+    assert np.dot(w, got) / np.linalg.norm(w) / np.linalg.norm(got) >= 0.999
+    assert abs(np.dot(w, got) / np.dot(w, w) / A - 2.0) <= 0.02
+    s.close()

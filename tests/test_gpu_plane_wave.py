@@ -41,7 +41,7 @@ def test_device_records_match_host_generator(tmp_path, psv_only):
     nbl = i["neh"] * i["hpn"]
     nrec = max(i["nrec_psv"], i["nrec_sh"])
     psv, sh = synth.plane_wave_records(i["nx"], i["nz"], i["h"], nbl, vs, c.p, c.f0, c.sdt, 0, nrec,
-                                       c.sv_amp, sh_amp)
+                                       c.sv_amp, sh_amp, eh=i["eh"])
     host.set_boundary(psv[:i["nrec_psv"]], None if psv_only else sh[:i["nrec_sh"]])
     dev.set_boundary_plane_wave(vs, c.p, c.f0, c.sv_amp, sh_amp)
     # interpolated FP64 increments of the interface line: one float32 ulp of a record at most
