@@ -101,6 +101,58 @@ typedef struct {
 } sks_plane_wave_t;
 int sks_set_boundary_plane_wave(sks_solver *s, const sks_plane_wave_t *pw);
 
+/* ---- plane waves through a layered stack --------------------------------
+ * Boundary records of a plane P, SV or SH wave that comes up through a 1-D
+ * stack of isotropic layers below the box: the upgoing P, SV and SH waves it
+ * leaves in the box's bottom medium, with every conversion and reverberation
+ * inside the stack (Thomson-Haskell propagators in FP64, frequency domain).
+ * Stands in for the reference's ray-sum generator
+ * (semsyn/src/aserpsv_sem.c:319-488, asersh_sem.c, aser.rout_noplot.f) for
+ * plane-wave runs; a stack of identical media gives sks_set_boundary_plane_wave's
+ * records.  Stack order: layers[0] the box's bottom medium (unbounded
+ * upward), layers[1..n-2] going down with their thickness (km), layers[n-1]
+ * the half-space the wave comes from.  Every medium needs vp > vs > 0,
+ * rho > 0 and p < 1/vp (all modes propagate).  The incident wave is
+ * referenced to the base of layers[0] as if the half-space reached it. */
+typedef struct {
+    double vp, vs, rho;         /* km/s, km/s, g/cm^3                      */
+    double thickness;           /* km; ignored for the first and last entries */
+} sks_stack_layer_t;
+
+typedef struct {
+    double p, f0;               /* ray parameter (s/km), Ricker frequency (Hz) */
+    double p_amp, sv_amp, sh_amp; /* incident amplitudes in the half-space  */
+} sks_layered_wave_t;
+
+/* plane-wave coefficients at angular frequency omega (rad/s) for a unit
+ * incident wave: t_* the upgoing amplitudes in layers[0] at its base, r_*
+ * the downgoing amplitudes in the half-space at its top; [out][in] with 0 =
+ * P, 1 = SV; [re, im].  Polarisations: P along its propagation; SV upgoing
+ * (eta_s vs, -p vs), downgoing (eta_s vs, p vs) in (x, z up); SH u_y. */
+typedef struct {
+    double t_psv[2][2][2], r_psv[2][2][2];
+    double t_sh[2], r_sh[2];
+} sks_layered_coef_t;
+int sks_layered_coefficients(const sks_stack_layer_t *layers, int32_t n, double p, double omega,
+                             sks_layered_coef_t *out);
+
+/* The upgoing P, SV and SH displacement series in layers[0] at its base and
+ * x = 0, for the Ricker pulse centred at 1.5/f0: out[m*nt + i] at time i*dt
+ * (m = 0 P, 1 SV, 2 SH), periodic in nt*dt (negative times at the end).
+ * sks_layered_series_length gives a power-of-2 nt whose period holds span
+ * seconds of record plus the stack's reverberations. */
+int64_t sks_layered_series_length(const sks_stack_layer_t *layers, int32_t n, double p, double f0, double dt,
+                                  double span);
+int sks_layered_series(const sks_stack_layer_t *layers, int32_t n, const sks_layered_wave_t *wave, double dt,
+                       int64_t nt, double *out);
+
+/* Boundary records from the layered stack, on the device, in the layout
+ * and at the node positions of sks_set_boundary_plane_wave.  Each value is
+ * a series above evaluated at t - p x - eta z (cubic Lagrange between
+ * samples dp/4 apart). */
+int sks_set_boundary_layered_wave(sks_solver *s, const sks_stack_layer_t *layers, int32_t n,
+                                  const sks_layered_wave_t *wave);
+
 /* Replaces the time loop (sem2d_psvsh.c:418-513) for steps
  * [step, step+nsteps): each step writes ntrace floats to each of seis_u
  * (u_x), seis_w (-u_z) and seis_v (u_y), time-major, like kirrecord_zhl

@@ -340,5 +340,64 @@ static __global__ void __launch_bounds__(256) k_plane_wave(float* __restrict__ p
     }
 }
 
+// a series sampled every dt, periodic in nt samples, at time t: cubic
+// Lagrange through the four samples around t
+__device__ __forceinline__ double series_at(const double* __restrict__ f, int64_t nt, double t_over_dt)
+{
+    const double fl = floor(t_over_dt);
+    const double d = t_over_dt - fl;
+    int64_t i0 = (int64_t)fl % nt;
+    if (i0 < 0) i0 += nt;
+    const int64_t im = i0 == 0 ? nt - 1 : i0 - 1, i1 = i0 + 1 < nt ? i0 + 1 : i0 + 1 - nt,
+                  i2 = i0 + 2 < nt ? i0 + 2 : i0 + 2 - nt;
+    const double wm = -d * (d - 1.0) * (d - 2.0) / 6.0;
+    const double w0 = (d + 1.0) * (d - 1.0) * (d - 2.0) / 2.0;
+    const double w1 = -(d + 1.0) * d * (d - 2.0) / 2.0;
+    const double w2 = (d + 1.0) * d * (d - 1.0) / 6.0;
+    return wm * f[im] + w0 * f[i0] + w1 * f[i1] + w2 * f[i2];
+}
+
+// Boundary records of the upgoing P, SV and SH waves a layered stack leaves
+// in the bottom medium (vp0, vs0): the mode series ser[m*nt + i] (m = P, SV,
+// SH; sample i at i*dts) evaluated at t - p x - eta_m z on the interface row
+// and column (the node positions and record layout of k_plane_wave).
+// Displacement: P (p vp0, eta_p vp0), SV (eta_s vs0, -p vs0), SH u_y; the
+// records hold u_x and -u_z (P-SV), u_y (SH).
+static __global__ void __launch_bounds__(256) k_layered_wave(float* __restrict__ psv, float* __restrict__ sh,
+                                                      int nrec_psv, int nrec_sh, int nx, int nz, double eh, int nbl,
+                                                      const double* __restrict__ ser, int64_t nt, double dts,
+                                                      double vp0, double vs0, double p, double dp)
+{
+    const int mtotal = 2 * (nx + nz), shtotal = nx + nz;
+    const double ep = sqrt(fmax(1.0 / (vp0 * vp0) - p * p, 0.0));
+    const double es = sqrt(fmax(1.0 / (vs0 * vs0) - p * p, 0.0));
+    const double line = gll_pos(nbl, eh);
+    const int64_t n1 = (int64_t)nrec_psv * mtotal, n2 = (int64_t)nrec_sh * shtotal;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n1 + n2; i += (int64_t)gridDim.x * blockDim.x) {
+        const bool fam_sh = i >= n1;
+        const int64_t k = fam_sh ? i - n1 : i;
+        const int L = fam_sh ? shtotal : mtotal;
+        const int r = (int)(k / L), c = (int)(k - (int64_t)r * L);
+        const double t = (double)r * dp;
+        int part, j;
+        if (!fam_sh) {
+            part = (c >= 2 * nx) ? 1 : 0;
+            j = part ? (c - 2 * nx) % nz : c % nx;
+        } else {
+            part = c >= nx ? 1 : 0;
+            j = part ? c - nx : c;
+        }
+        const double x = part ? line : gll_pos(j, eh), z = part ? gll_pos(j, eh) : line;
+        if (fam_sh) {
+            sh[k] = (float)series_at(ser + 2 * nt, nt, (t - p * x - es * z) / dts);
+        } else {
+            const double fp = series_at(ser, nt, (t - p * x - ep * z) / dts);
+            const double fs = series_at(ser + nt, nt, (t - p * x - es * z) / dts);
+            const bool vert = part ? (c - 2 * nx) >= nz : c >= nx;
+            psv[k] = (float)(vert ? -(fp * ep * vp0 - fs * p * vs0) : fp * p * vp0 + fs * es * vs0);
+        }
+    }
+}
+
 }  // namespace sks
 

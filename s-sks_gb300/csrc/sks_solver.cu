@@ -731,6 +731,50 @@ extern "C" int sks_set_boundary_plane_wave(sks_solver* s, const sks_plane_wave_t
     return SKS_OK;
 }
 
+extern "C" int sks_set_boundary_layered_wave(sks_solver* s, const sks_stack_layer_t* layers, int32_t n,
+                                             const sks_layered_wave_t* w)
+{
+    if (!s || !layers || !w) return set_err(SKS_ERR_ARG, "NULL argument");
+    if (n < 2) return set_err(SKS_ERR_ARG, "layered wave: at least 2 media (top, half-space)");
+    const sks_model& m = s->m;
+    // the series: samples dp/4 apart over the records' span plus the largest
+    // delay along the line (p x + eta z at the far corner, slowest mode)
+    const double dts = m.dp / 4.0;
+    const double xmax = (double)(m.nx - 1) * m.h + m.eh, zmax = (double)(m.nz - 1) * m.h + m.eh;
+    const double smax = 1.0 / layers[0].vs;
+    const double span = (double)std::max(m.nrec_psv, m.nrec_sh) * m.dp + w->p * xmax + smax * zmax;
+    const int64_t nt = sks_layered_series_length(layers, n, w->p, w->f0, dts, span);
+    if (nt < 0) return (int)nt;
+    std::vector<double> ser;
+    try {
+        ser.resize((size_t)nt * 3);
+    } catch (...) {
+        return set_err(SKS_ERR_NOMEM, "layered wave: out of host memory");
+    }
+    sks_layered_wave_t ww = *w;
+    if (m.psv_only) ww.sh_amp = 0.0;
+    int rc = sks_layered_series(layers, n, &ww, dts, nt, ser.data());
+    if (rc) return rc;
+    cudaSetDevice(s->device);
+    rc = alloc_records(s);
+    if (rc) return rc;
+    double* dser = nullptr;
+    CK(cudaMalloc(&dser, sizeof(double) * (size_t)nt * 3));
+    cudaError_t e = cudaMemcpyAsync(dser, ser.data(), sizeof(double) * (size_t)nt * 3, cudaMemcpyHostToDevice, s->stream);
+    const int64_t tot = (int64_t)m.nrec_psv * m.mtotal + (int64_t)m.nrec_sh * m.shtotal;
+    if (e == cudaSuccess && tot > 0) {
+        const int blocks = (int)std::min<int64_t>((tot + 255) / 256, (int64_t)s->sms * 16);
+        k_layered_wave<<<blocks, 256, 0, s->stream>>>(s->rec_psv, s->rec_sh, m.nrec_psv, m.nrec_sh, m.nx, m.nz, m.eh,
+                                                      s->nbl, dser, nt, dts, layers[0].vp, layers[0].vs, w->p, m.dp);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(dser);
+    if (e != cudaSuccess) return set_err(SKS_ERR_CUDA, "layered wave: %s", cudaGetErrorString(e));
+    s->boundary_ready = true;
+    return SKS_OK;
+}
+
 extern "C" int sks_set_boundary(sks_solver* s, const float* psv, int32_t nrec_psv, const float* sh, int32_t nrec_sh)
 {
     if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");

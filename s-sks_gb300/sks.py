@@ -33,6 +33,8 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_probe_fma_peak",
            "sks_set_tuning", "sks_get_tuning", "sks_autotune", "sks_line_increments",
            "sks_line_increments_noalloc", "sks_set_boundary_plane_wave", "sks_snapshot",
+           "sks_layered_coefficients", "sks_layered_series_length", "sks_layered_series",
+           "sks_set_boundary_layered_wave",
            "sks_state_bytes", "sks_state_save", "sks_state_load",
            "sks_elastic_rotate", "sks_elastic_dip", "sks_christoffel", "sks_semmodel_write",
            "sks_bandpass_design", "sks_split_scratch", "sks_split_traces",
@@ -90,6 +92,20 @@ class SplitOpts(C.Structure):
 class PlaneWave(C.Structure):
     _fields_ = [("vs", C.c_double), ("p", C.c_double), ("f0", C.c_double), ("sv_amp", C.c_double),
                 ("sh_amp", C.c_double)]
+
+
+class StackLayer(C.Structure):
+    _fields_ = [("vp", C.c_double), ("vs", C.c_double), ("rho", C.c_double), ("thickness", C.c_double)]
+
+
+class LayeredWave(C.Structure):
+    _fields_ = [("p", C.c_double), ("f0", C.c_double), ("p_amp", C.c_double), ("sv_amp", C.c_double),
+                ("sh_amp", C.c_double)]
+
+
+class LayeredCoef(C.Structure):
+    _fields_ = [("t_psv", C.c_double * 8), ("r_psv", C.c_double * 8), ("t_sh", C.c_double * 2),
+                ("r_sh", C.c_double * 2)]
 
 
 class SacFields(C.Structure):
@@ -152,6 +168,14 @@ def lib() -> C.CDLL:
         L.sks_line_increments_noalloc.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp,
                                                   C.c_int32, vp, vp]
         L.sks_set_boundary_plane_wave.argtypes = [vp, C.POINTER(PlaneWave)]
+        L.sks_layered_coefficients.argtypes = [C.POINTER(StackLayer), C.c_int32, C.c_double, C.c_double,
+                                               C.POINTER(LayeredCoef)]
+        L.sks_layered_series_length.argtypes = [C.POINTER(StackLayer), C.c_int32, C.c_double, C.c_double,
+                                                C.c_double, C.c_double]
+        L.sks_layered_series_length.restype = C.c_int64
+        L.sks_layered_series.argtypes = [C.POINTER(StackLayer), C.c_int32, C.POINTER(LayeredWave), C.c_double,
+                                         C.c_int64, dp]
+        L.sks_set_boundary_layered_wave.argtypes = [vp, C.POINTER(StackLayer), C.c_int32, C.POINTER(LayeredWave)]
         L.sks_snapshot.argtypes = [vp, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_int32)]
         L.sks_elastic_rotate.argtypes = [dp, C.c_double, dp]
         L.sks_elastic_dip.argtypes = [dp, C.c_double, dp]
@@ -313,6 +337,13 @@ class Solver:
     def set_boundary_plane_wave(self, vs: float, p: float, f0: float, sv_amp: float = 1.0, sh_amp: float = 0.0):
         pw = PlaneWave(vs, p, f0, sv_amp, sh_amp)
         _check(lib().sks_set_boundary_plane_wave(self.h, C.byref(pw)))
+
+    def set_boundary_layered_wave(self, layers, p: float, f0: float, p_amp: float = 0.0, sv_amp: float = 1.0,
+                                  sh_amp: float = 0.0):
+        """layers: (vp, vs, rho, thickness) from the box's bottom medium down to the half-space."""
+        st = _stack(layers)
+        w = LayeredWave(p, f0, p_amp, sv_amp, sh_amp)
+        _check(lib().sks_set_boundary_layered_wave(self.h, st, len(layers), C.byref(w)))
 
     def run(self, nsteps: int, out=None):
         nt = self.info()["ntrace"]
@@ -569,6 +600,37 @@ def probe_fma_peak(precision: int, device: int = 0) -> float:
 
 def _d(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _stack(layers):
+    st = (StackLayer * len(layers))()
+    for i, l in enumerate(layers):
+        vp, vs, rho = l[0], l[1], l[2]
+        st[i] = StackLayer(vp, vs, rho, l[3] if len(l) > 3 else 0.0)
+    return st
+
+
+def layered_coefficients(layers, p: float, omega: float) -> dict:
+    """Plane-wave coefficients of a layered stack at angular frequency omega:
+    t_psv/r_psv [out][in] (0 = P, 1 = SV) complex 2x2, t_sh, r_sh complex."""
+    c = LayeredCoef()
+    _check(lib().sks_layered_coefficients(_stack(layers), len(layers), p, omega, C.byref(c)))
+    t = np.array(c.t_psv[:]).reshape(2, 2, 2)
+    r = np.array(c.r_psv[:]).reshape(2, 2, 2)
+    return {"t_psv": t[..., 0] + 1j * t[..., 1], "r_psv": r[..., 0] + 1j * r[..., 1],
+            "t_sh": c.t_sh[0] + 1j * c.t_sh[1], "r_sh": c.r_sh[0] + 1j * c.r_sh[1]}
+
+
+def layered_series(layers, p: float, f0: float, dt: float, span: float, p_amp: float = 0.0, sv_amp: float = 1.0,
+                   sh_amp: float = 0.0) -> np.ndarray:
+    """Upgoing P, SV, SH series (3, nt) at the base of the top medium, sample i at i*dt (periodic)."""
+    st = _stack(layers)
+    nt = lib().sks_layered_series_length(st, len(layers), p, f0, dt, span)
+    _check(int(nt) if nt < 0 else 0)
+    out = np.zeros(3 * nt)
+    w = LayeredWave(p, f0, p_amp, sv_amp, sh_amp)
+    _check(lib().sks_layered_series(st, len(layers), C.byref(w), dt, nt, _d(out)))
+    return out.reshape(3, nt)
 
 
 def elastic_rotate(c, angle_deg: float) -> np.ndarray:

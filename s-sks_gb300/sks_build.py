@@ -48,7 +48,7 @@ def build(verbose: bool = False) -> str:
     units = [
         (os.path.join(CSRC, c + ".c"), os.path.join(OUT, c + ".o"),
          ["gcc", "-O2", "-std=gnu11", "-fPIC", "-Wall", "-I" + INC, "-c"]) for c in ("sks_model", "sks_elastic",
-                                                                                    "sks_sac")
+                                                                                    "sks_sac", "sks_layered")
     ]
     for cu in ("sks_solver", "sks_batch", "sks_server", "sks_step_f32", "sks_step_f64", "sks_batch_f32", "sks_batch_f64",
                "sks_noalloc", "sks_post", "sks_probe"):
