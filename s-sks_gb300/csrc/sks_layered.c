@@ -155,7 +155,7 @@ static int coefs_at(const sks_stack_layer_t *L, int n, const medium_t *md, doubl
 {
     cplx M[4][4], H[2][2];
     int i, j, k, l;
-    double D_p = 0.0, D_s = 0.0;
+    double D = 0.0;
     for (i = 0; i < 4; i++)
         for (j = 0; j < 4; j++) M[i][j] = i == j;
     H[0][0] = 1; H[0][1] = 0; H[1][0] = 0; H[1][1] = 1;
@@ -192,13 +192,11 @@ static int coefs_at(const sks_stack_layer_t *L, int n, const medium_t *md, doubl
                 for (j = 0; j < 2; j++) S[i][j] = H[i][0] * Q[0][j] + H[i][1] * Q[1][j];
             memcpy(H, S, sizeof H);
         }
-        D_p += h;
-        D_s += h;
+        D += h;
     }
     {
         /* E_0 [tP, tS, 0, 0] - G[:,2] rP - G[:,3] rS = G[:,0] aP' + G[:,1] aS', G = M E_hs */
         const medium_t *hs = md + n - 1, *top = md;
-        const double D = D_p;
         cplx G[4][4], A[4][4], B[4][2];
         const cplx advp = cexp(I * w * hs->ep * D), advs = cexp(I * w * hs->es * D);
         for (i = 0; i < 4; i++)
@@ -242,7 +240,6 @@ static int coefs_at(const sks_stack_layer_t *L, int n, const medium_t *md, doubl
             c->r_sh[1] = cimag(Bs[1][0]);
         }
     }
-    (void)D_s;
     return SKS_OK;
 }
 

@@ -64,3 +64,22 @@ def test_no_device_is_an_error_not_a_crash(tmp_path):
         with pytest.raises(sks.SksError) as e:
             sks.Solver(["par=run.par"])
     assert e.value.code == -5
+
+
+@pytest.mark.parametrize("words,msg", [
+    (["sks_plane_wave=4.5,0.04"], "sks_plane_wave=vs,p,f0"),
+    (["sks_plane_wave=4.5,x,1"], "sks_plane_wave=vs,p,f0"),
+    (["sks_plane_wave=4.5,0.04,1", "sks_wave=0.04,1"], "exclude each other"),
+    (["sks_wave=0.04,1"], "go together"),
+    (["sks_stack=stack.txt", "sks_wave=0.04"], "sks_wave=p,f0"),
+    (["sks_stack=missing.txt", "sks_wave=0.04,1"], "cannot read the stack file"),
+    (["sks_stack=short.txt", "sks_wave=0.04,1"], "2 media at least"),
+])
+def test_program_refuses_malformed_generator_words(tmp_path, words, msg):
+    """The device-generator words of the drop-in program are checked before
+    any device work, so their refusals need no GPU."""
+    (tmp_path / "stack.txt").write_text("# vp vs rho thickness\n7.6 4.3 3.3 0\n8.1 4.5 3.4 0\n")
+    (tmp_path / "short.txt").write_text("7.6 4.3 3.3 0\n")
+    cli = os.path.join(os.path.dirname(sks.LIB_PATH), "sem2d_psvsh_gb300")
+    r = subprocess.run([cli, "par=run.par"] + words, cwd=str(tmp_path), capture_output=True, text=True)
+    assert r.returncode == 1 and msg in r.stderr, r.stderr

@@ -197,3 +197,37 @@ def test_sem_through_a_layer_matches_the_layered_generator(tmp_path):
     print(f"layered box: misfit {e_layered:.4f} to the layered generator, {e_naive:.4f} to the unlayered wave")
     assert e_layered < 0.015, (e_layered, e_naive)
     assert e_naive > 30 * e_layered, (e_layered, e_naive)
+
+
+@pytest.mark.parametrize("form", ["plane", "stack"])
+def test_program_generator_words(tmp_path, form):
+    """The drop-in program with sks_plane_wave= or sks_stack= / sks_wave=
+    writes the seismograms the library gives with the same generator."""
+    import os
+    import subprocess
+    d = str(tmp_path)
+    p, f0 = 0.04, 1.2
+    top = (7.9, 4.4, 3.35)
+    c = _case(d, [_iso(*top, 13.0)], 29, 12, 500, p, f0, 6, 2.0, 4.0, 1.0, 0.5)
+    stack = [top, (6.6, 3.8, 2.9, 6.0), (VP, VS, RHO)]
+    with open(os.path.join(d, "stack.txt"), "w") as f:
+        f.write("# box bottom medium, layer, half-space\n")
+        for m in stack:
+            f.write(" ".join(repr(float(v)) for v in (tuple(m) + (0.0,))[:4]) + "\n")
+    words = (["sks_plane_wave=4.4,0.04,1.2,1.0,0.5"] if form == "plane"
+             else ["sks_stack=stack.txt", "sks_wave=0.04,1.2,0.0,1.0,0.5"])
+    cli = os.path.join(os.path.dirname(sks.LIB_PATH), "sem2d_psvsh_gb300")
+    r = subprocess.run([cli, "par=run.par"] + words, cwd=d, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    with chdir(d):
+        s = sks.Solver(["par=run.par"], precision=sks.FP64)
+    if form == "plane":
+        s.set_boundary_plane_wave(4.4, p, f0, 1.0, 0.5)
+    else:
+        s.set_boundary_layered_wave(stack, p, f0, 0.0, 1.0, 0.5)
+    u, v, w = s.run(c.nst)
+    s.close()
+    for name, want in (("seis.u", u), ("seis.v", v), ("seis.w", w)):
+        got = np.fromfile(os.path.join(d, name), np.float32).reshape(c.nst, -1)
+        assert np.abs(want).max() > 0
+        assert np.array_equal(got, want), name
