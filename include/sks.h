@@ -500,6 +500,11 @@ int sks_server_set_active_points(sks_server *srv, int precision, int64_t max_poi
  * may be NULL); they must stay valid until then. */
 int sks_server_submit(sks_server *srv, sks_setup *su, int precision, const sks_plane_wave_t *pw,
                       float *seis_u, float *seis_v, float *seis_w, int64_t *id);
+/* Same with boundary records from a plane wave through a layered stack
+ * (sks_set_boundary_layered_wave at admission; the stack is copied). */
+int sks_server_submit_layered(sks_server *srv, sks_setup *su, int precision, const sks_stack_layer_t *layers,
+                              int32_t n, const sks_layered_wave_t *wave, float *seis_u, float *seis_v,
+                              float *seis_w, int64_t *id);
 /* One scheduling round: retire requests whose batch quantum finished,
  * admit, launch the idle forms' next quantum.  Returns the requests queued or
  * running (0 when all are done), or a negative status. */

@@ -23,6 +23,7 @@
 #include <mutex>
 #include <thread>
 #include <unordered_map>
+#include <vector>
 
 using namespace sks;
 using namespace sksi;
@@ -35,6 +36,8 @@ struct Request {
     int precision = SKS_FP32C;
     bool has_pw = false;
     sks_plane_wave_t pw{};
+    std::vector<sks_stack_layer_t> stack;  // non-empty: records from the layered stack
+    sks_layered_wave_t lw{};
     float* out[3] = {nullptr, nullptr, nullptr};
     // the serving thread owns the solver; what other threads read (state,
     // status, step, bytes, times) is written under the server's mutex
@@ -164,7 +167,11 @@ int admit_one(sks_server* v, Request* r)
     sks_setup* su = r->su;
     r->su = nullptr;
     int rc = sks_open_setup(su, r->precision, v->device, &s);   // takes the set-up over
-    if (!rc) rc = r->has_pw ? sks_set_boundary_plane_wave(s, &r->pw) : sks_load_boundary_files(s);
+    if (!rc) {
+        if (!r->stack.empty()) rc = sks_set_boundary_layered_wave(s, r->stack.data(), (int32_t)r->stack.size(), &r->lw);
+        else if (r->has_pw) rc = sks_set_boundary_plane_wave(s, &r->pw);
+        else rc = sks_load_boundary_files(s);
+    }
     if (!rc) rc = sks_batch_add(v->batch[r->precision], s);
     if (rc) {
         if (s) sks_destroy(s);
@@ -281,8 +288,11 @@ extern "C" int sks_server_set_active_points(sks_server* v, int precision, int64_
     return SKS_OK;
 }
 
-extern "C" int sks_server_submit(sks_server* v, sks_setup* su, int precision, const sks_plane_wave_t* pw, float* su_out,
-                                 float* sv_out, float* sw_out, int64_t* id)
+namespace {
+
+// queue a request; pw or (layers, n, lw) name a device generator, neither the files
+int submit(sks_server* v, sks_setup* su, int precision, const sks_plane_wave_t* pw, const sks_stack_layer_t* layers,
+           int32_t n, const sks_layered_wave_t* lw, float* su_out, float* sv_out, float* sw_out, int64_t* id)
 {
     if (!v || !su || !id) {
         if (su) sks_setup_close(su);
@@ -292,7 +302,7 @@ extern "C" int sks_server_submit(sks_server* v, sks_setup* su, int precision, co
         sks_setup_close(su);
         return set_err(SKS_ERR_ARG, "unknown precision %d", precision);
     }
-    if (!pw) {
+    if (!pw && !layers) {
         int rc = absolute_path(su->m.greenfile, sizeof su->m.greenfile);
         if (!rc && !su->m.psv_only) rc = absolute_path(su->m.shgreenfile, sizeof su->m.shgreenfile);
         if (rc) { sks_setup_close(su); return rc; }
@@ -302,6 +312,16 @@ extern "C" int sks_server_submit(sks_server* v, sks_setup* su, int precision, co
     r->su = su;
     r->precision = precision;
     if (pw) { r->has_pw = true; r->pw = *pw; }
+    if (layers) {
+        try {
+            r->stack.assign(layers, layers + n);
+        } catch (...) {
+            delete r;
+            sks_setup_close(su);
+            return set_err(SKS_ERR_NOMEM, "cannot copy the layer stack");
+        }
+        r->lw = *lw;
+    }
     r->out[0] = su_out; r->out[1] = sv_out; r->out[2] = sw_out;
     r->est_bytes = estimate_bytes(su->m, precision);
     r->nst = su->m.nst;
@@ -322,6 +342,25 @@ extern "C" int sks_server_submit(sks_server* v, sks_setup* su, int precision, co
     }
     *id = r->id;
     return SKS_OK;
+}
+
+}  // namespace
+
+extern "C" int sks_server_submit(sks_server* v, sks_setup* su, int precision, const sks_plane_wave_t* pw, float* su_out,
+                                 float* sv_out, float* sw_out, int64_t* id)
+{
+    return submit(v, su, precision, pw, nullptr, 0, nullptr, su_out, sv_out, sw_out, id);
+}
+
+extern "C" int sks_server_submit_layered(sks_server* v, sks_setup* su, int precision, const sks_stack_layer_t* layers,
+                                         int32_t n, const sks_layered_wave_t* wave, float* su_out, float* sv_out,
+                                         float* sw_out, int64_t* id)
+{
+    if (!layers || !wave || n < 2) {
+        if (su) sks_setup_close(su);
+        return set_err(SKS_ERR_ARG, "layered request: a stack of 2 media at least and a wave");
+    }
+    return submit(v, su, precision, nullptr, layers, n, wave, su_out, sv_out, sw_out, id);
 }
 
 extern "C" int sks_server_step(sks_server* v)

@@ -42,7 +42,7 @@ EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_r
            "sks_batch_create", "sks_batch_add", "sks_batch_remove", "sks_batch_size", "sks_batch_run",
            "sks_batch_set_tuning", "sks_batch_get_tuning", "sks_batch_autotune", "sks_batch_last_run_ms",
            "sks_batch_kernel_launches", "sks_batch_destroy",
-           "sks_server_create", "sks_server_set_tuning", "sks_server_set_active_points", "sks_server_submit", "sks_server_step",
+           "sks_server_create", "sks_server_set_tuning", "sks_server_set_active_points", "sks_server_submit", "sks_server_submit_layered", "sks_server_step",
            "sks_server_request_info", "sks_server_release", "sks_server_clock", "sks_server_device_bytes",
            "sks_server_destroy",
            "sks_destroy", "sks_last_error"]
@@ -211,6 +211,8 @@ def lib() -> C.CDLL:
         L.sks_server_set_tuning.argtypes = [vp, C.c_int, C.POINTER(Tuning)]
         L.sks_server_set_active_points.argtypes = [vp, C.c_int, C.c_int64]
         L.sks_server_submit.argtypes = [vp, vp, C.c_int, C.POINTER(PlaneWave), fp, fp, fp, C.POINTER(C.c_int64)]
+        L.sks_server_submit_layered.argtypes = [vp, vp, C.c_int, C.POINTER(StackLayer), C.c_int32,
+                                                C.POINTER(LayeredWave), fp, fp, fp, C.POINTER(C.c_int64)]
         L.sks_server_step.argtypes = [vp]
         L.sks_server_request_info.argtypes = [vp, C.c_int64, C.POINTER(RequestInfo)]
         L.sks_server_release.argtypes = [vp, C.c_int64]
@@ -523,15 +525,22 @@ class Server:
     def set_active_points(self, precision: int, max_points: int):
         _check(lib().sks_server_set_active_points(self.h, precision, max_points))
 
-    def submit(self, setup: "Setup", precision: int, plane_wave: tuple | None = None, want: bool = True) -> int:
-        """plane_wave = (vs, p, f0, sv_amp, sh_amp) or None (the par's boundary files)."""
+    def submit(self, setup: "Setup", precision: int, plane_wave: tuple | None = None, want: bool = True,
+               layered: tuple | None = None) -> int:
+        """plane_wave = (vs, p, f0, sv_amp, sh_amp); layered = (layers, p, f0, p_amp, sv_amp, sh_amp) with
+        layers as for Solver.set_boundary_layered_wave; neither: the par's boundary files."""
         i = setup.info()
         out = tuple(np.zeros((i["nst"], max(i["ntrace"], 0)), np.float32) for _ in range(3)) if want else None
         pw = C.byref(PlaneWave(*plane_wave)) if plane_wave is not None else None
         h, setup.h = setup.h, C.c_void_p()
         rid = C.c_int64()
         ptrs = [_f32(o) for o in out] if out else [None, None, None]
-        _check(lib().sks_server_submit(self.h, h, precision, pw, ptrs[0], ptrs[1], ptrs[2], C.byref(rid)))
+        if layered is not None:
+            layers, wave = layered[0], LayeredWave(*layered[1:])
+            _check(lib().sks_server_submit_layered(self.h, h, precision, _stack(layers), len(layers), C.byref(wave),
+                                                   ptrs[0], ptrs[1], ptrs[2], C.byref(rid)))
+        else:
+            _check(lib().sks_server_submit(self.h, h, precision, pw, ptrs[0], ptrs[1], ptrs[2], C.byref(rid)))
         self.outputs[rid.value] = out
         return rid.value
 

@@ -165,3 +165,42 @@ def test_points_cap_runs_each_form_first_come_first_served(reqs):
         for c in range(3):
             assert np.array_equal(got[c], alone[k][c])
     srv.close()
+
+
+def test_layered_requests_are_the_same_alone_and_served(tmp_path):
+    """Requests whose boundary records come from a plane wave through a
+    layered stack (sks_server_submit_layered) equal the same solve alone."""
+    runs = []
+    for k, form in enumerate((sks.FP32C, sks.FP64)):
+        d = str(tmp_path / f"layered{k}")
+        H = 10 * 1.0 + 0.002
+        layers = _layers(H, True)
+        c = synth.Case(nex=27 + 6 * k, nez=10, eh=1.0, sdt=0.005, nst=640, layers=layers, p=0.042, f0=1.2,
+                       sv_amp=1.0, sh_amp=0.4, ntrace=6, rec_dx=3.0, semmodel_full=True, write_records=False)
+        synth.write_case(c, d)
+        stack = [(8.1, 4.5, 3.4), (6.9, 3.9, 3.0, 7.0 + k), (8.3, 4.6, 3.45)]
+        runs.append((d, form, stack, c.nst))
+    alone = []
+    for d, form, stack, nst in runs:
+        with chdir(d):
+            s = sks.Solver(["par=run.par"], precision=form)
+        s.set_boundary_layered_wave(stack, 0.042, 1.2, 0.0, 1.0, 0.4)
+        s.set_tuning(*(T32 if form == sks.FP32C else T64), 0)
+        alone.append(s.run(nst))
+        s.close()
+    assert all(max(np.abs(x).max() for x in a) > 0.05 for a in alone)
+    srv = sks.Server(0, 0, 64)
+    srv.set_tuning(sks.FP32C, *T32)
+    srv.set_tuning(sks.FP64, *T64)
+    ids = [srv.submit(_setup(d), form, layered=(stack, 0.042, 1.2, 0.0, 1.0, 0.4)) for d, form, stack, _ in runs]
+    rnd = 0
+    while srv.step() > 0:
+        rnd += 1
+        assert rnd < 100000
+    for i, rid in enumerate(ids):
+        assert srv.info(rid)["state"] == sks.REQ_DONE
+        got = srv.result(rid)
+        for c in range(3):
+            assert np.array_equal(got[c], alone[i][c]), f"request {i} component {c}"
+        srv.release(rid)
+    srv.close()
