@@ -182,6 +182,10 @@ typedef struct {
     int plot_snap, ist, incre, nxs, nzs;
     float *snaps;               /* [NSNAP][nxs][nzs][2] */
     int snap_taken[32];
+    /* boundary taper (atten > 0): nh = neh*hpn factors, ass at the edge */
+    int nh_att;
+    float ass_f; real ass;
+    real *taper;
 } Oracle;
 
 #define NSNAP 26
@@ -678,6 +682,42 @@ static void time_update(Oracle *o)
     for (i = 1; i < (size_t)(3 * o->hpn + 1) && i < (size_t)nx; i++) absorb_point(o, (size_t)(nz - 1) * nx + i, dt2);
 }
 
+/* ---------------- boundary taper (sem2d_psvsh.c:1724-1738, 1780-1822) ---- */
+/* atten_taper: taper[n] = exp(alpha n), alpha = log10(ass) / (nh log10(2.73));
+ * the float build rounds each factor to float as the reference stores it */
+static int taper_table(Oracle *o)
+{
+    int n, nh = o->nh_att;
+    o->taper = (real *)malloc(sizeof(real) * (size_t)(nh > 0 ? nh : 1));
+    if (!o->taper) return fail("cannot allocate the taper", NULL);
+    if (IS_FLOAT) {
+        const double alpha = 1.0 / nh * log10((double)o->ass_f) / log10(2.73);
+        for (n = 0; n < nh; n++) o->taper[n] = (real)(float)exp((double)(alpha * n));
+    } else {
+        const double alpha = 1.0 / nh * log10((double)o->ass) / log10(2.73);
+        for (n = 0; n < nh; n++) o->taper[n] = (real)exp(alpha * n);
+    }
+    return ORC_OK;
+}
+
+/* atten_wave2: u^{n+1} scaled in the bottom rows (atten > 0), then the left
+ * (> 1) and right (> 2) columns above them, then the top rows between those
+ * columns (> 3), one multiplication per zone in that order */
+static void taper_wave(Oracle *o)
+{
+    const int nh = o->nh_att, nx = o->nx, nz = o->nz;
+    int ix, iz, k;
+    for (k = 0; k < 3; k++)
+        for (ix = 0; ix < nx; ix++)
+            for (iz = 0; iz < nz; iz++) {
+                real *p = &o->u1[(size_t)iz * nx + ix].u[k];
+                if (o->atten > 0 && iz < nh) *p *= o->taper[nh - iz - 1];
+                if (o->atten > 1 && ix < nh && iz >= nh) *p *= o->taper[nh - ix - 1];
+                if (o->atten > 2 && ix >= nx - nh && iz >= nh) *p *= o->taper[ix - nx + nh];
+                if (o->atten > 3 && iz >= nz - nh && ix < nx - nh && ix >= nh) *p *= o->taper[iz - nz + nh];
+            }
+}
+
 /* ---------------- GRT boundary injection (sem2d_psvsh.c:1953-2111) ------- */
 static void grt_interface_set(Oracle *o)
 {
@@ -835,6 +875,9 @@ static int oracle_setup(Oracle *o, int argc, char **argv)
     GETI("readpars", o->readpars, 0);
     GETI("neh", o->neh, 0);
     GETI("atten", o->atten, 0);
+    o->ass_f = 0.93f;
+    o->ass = IS_FLOAT ? (real)o->ass_f : (real)0.93;
+    GETF("ass", o->ass, o->ass_f, 0);
     GETI("xtrace", o->xtrace, 0);
     GETF("xbeg", o->xbeg, o->xbeg_f, 1);
     GETF("zbeg", o->zbeg, o->zbeg_f, 0);
@@ -845,7 +888,10 @@ static int oracle_setup(Oracle *o, int argc, char **argv)
     GETI("msource", o->msource, 1);
     free(pl.e);
     if (o->msource != 0) return fail("only the GRT boundary source (msource=0) is restated", NULL);
-    if (o->atten != 0) return fail("boundary attenuation (atten>0) is not restated", NULL);
+    if (o->atten > 0) {
+        o->nh_att = o->neh * o->hpn;
+        if (taper_table(o)) return ORC_ERR;
+    }
     if (o->nex < 1) return fail("nex must be positive", NULL);
     N = o->hpn;
     if (gll_points(N, o->gllp)) return ORC_ERR;
@@ -929,6 +975,7 @@ static void oracle_free(Oracle *o)
     free(o->u); free(o->u0); free(o->u1); free(o->K); free(o->rec_off);
     free(o->grtuw); free(o->grtuw0); free(o->grtv); free(o->grtv0); free(o->sy); free(o->sy_sh);
     free(o->snaps);
+    free(o->taper);
     memset(o, 0, sizeof *o);
 }
 
@@ -979,6 +1026,7 @@ static int oracle_steps(Oracle *o, int it_begin, int it_end, float *su, float *s
             if (it < o->nt_sem) grt_interface_add(o);
             stiff_matrix(o);
             time_update(o);
+            if (o->atten > 0) taper_wave(o);
             t = o->u0; o->u0 = o->u; o->u = o->u1; o->u1 = t;
         }
         if (o->plot_trace && su) {

@@ -33,6 +33,7 @@ struct sks_batch {
     int PIPE = 0;                         // 1: a chunk is one pipelined launch (k_step_batch_pipe)
     int chunk = 64;
     bool aniso = false;                   // the step variant: any member anisotropic
+    bool taper = false;                   // ... any member with the boundary taper (atten > 0)
     int grid = 0;                         // persistent CTAs of a step launch
     // device tables (capacity `cap` members, `items_cap` tiles)
     void* dmem = nullptr;                 // BatchMember<T>[cap]
@@ -146,10 +147,11 @@ int build_tables(sks_batch* b)
     std::vector<BatchMember<T>> md;
     std::vector<BatchAux> ad;
     std::vector<int4> items;
-    bool aniso = false;
+    bool aniso = false, taper = false;
     for (int i = 0; i < n; i++) {
         sks_solver* s = b->mem[i];
         aniso = aniso || member_aniso(s);
+        taper = taper || s->m.nh_att > 0;
         md.push_back(member_desc<T>(s));
         md.back().item0 = (int)items.size();
         ad.push_back(aux_desc(s));
@@ -159,8 +161,9 @@ int build_tables(sks_batch* b)
             for (int cx = 0; cx < s->ncx; cx++)
                 items.push_back(make_int4(i, cx | (cz << 16), cz * s->HZ, std::min((cz + 1) * s->HZ, s->m.nez)));
     }
-    if (aniso != b->aniso) {
+    if (aniso != b->aniso || taper != b->taper) {
         b->aniso = aniso;
+        b->taper = taper;
         b->graph_dirty = true;
     }
     if (n > b->cap) {
@@ -214,7 +217,7 @@ int build_tables(sks_batch* b)
 template <typename T>
 cudaError_t launch_steps(sks_batch* b, int j)
 {
-    const StepVariant v{b->NW, b->ZS, b->CAP};
+    const StepVariant v{b->NW, b->ZS, b->CAP, b->taper};
     static thread_local Coef<T> k;
     k = make_coef<T>(b->mem[0]->m);     // GLL tables: the same for every member
     if (sizeof(T) == 4)
@@ -228,7 +231,7 @@ cudaError_t launch_steps(sks_batch* b, int j)
 template <typename T>
 cudaError_t launch_pipe_chunk(sks_batch* b, int nsteps)
 {
-    const StepVariant v{b->NW, b->ZS, b->CAP};
+    const StepVariant v{b->NW, b->ZS, b->CAP, b->taper};
     static thread_local Coef<T> k;
     k = make_coef<T>(b->mem[0]->m);
     cudaError_t e = cudaMemsetAsync(b->dpipe, 0, sizeof(int) * (2 + b->items_cap), b->stream);
@@ -244,7 +247,7 @@ cudaError_t launch_pipe_chunk(sks_batch* b, int nsteps)
 // persistent grid: every SM full of resident CTAs of the step variant
 void set_persistent_grid(sks_batch* b)
 {
-    const StepVariant v{b->NW, b->ZS, b->CAP};
+    const StepVariant v{b->NW, b->ZS, b->CAP, b->taper};
     int occ;
     if (b->PIPE) occ = b->precision == SKS_FP64 ? batch_pipe_occupancy_f64(v, b->aniso) : batch_pipe_occupancy_f32(v, b->aniso);
     else occ = b->precision == SKS_FP64 ? batch_occupancy_f64(v, b->aniso) : batch_occupancy_f32(v, b->aniso);

@@ -1,36 +1,33 @@
-// Batch step kernel variants of the FP32-compensated form.
+// Batch step kernel variants of the FP32-compensated form without the boundary taper;
+// the tapered ones (a member with atten > 0) compile in sks_batch_f32_tp.cu.
 #include "sks_batch_inst.cuh"
 
 namespace sks {
 
 int batch_occupancy_f32(const StepVariant& v, bool aniso)
 {
-    BatchOcc<float, true> o;
-    return visit_variant(v, aniso, o);
+    return v.taper ? batch_occupancy_f32_tp(v, aniso) : batch_occupancy_t<float, true, false>(v, aniso);
 }
 
 cudaError_t launch_batch_f32(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const BatchMember<float>* mem,
                              const BatchState* state, const int4* items, const BatchHeader* hdr, int j,
                              const Coef<float>& k)
 {
-    BatchLaunch<float, true> l{blocks, st, mem, state, items, hdr, j, k};
-    visit_variant(v, aniso, l);
-    return cudaGetLastError();
+    return v.taper ? launch_batch_f32_tp(v, aniso, blocks, st, mem, state, items, hdr, j, k)
+                   : launch_batch_t<float, true, false>(v, aniso, blocks, st, mem, state, items, hdr, j, k);
 }
 
 int batch_pipe_occupancy_f32(const StepVariant& v, bool aniso)
 {
-    BatchPipeOcc<float, true> o;
-    return visit_variant(v, aniso, o);
+    return v.taper ? batch_pipe_occupancy_f32_tp(v, aniso) : batch_pipe_occupancy_t<float, true, false>(v, aniso);
 }
 
 cudaError_t launch_batch_pipe_f32(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
                                   const BatchMember<float>* mem, const BatchState* state, const int4* items,
                                   const BatchHeader* hdr, int nsteps, const BatchPipeCtl& ctl, const Coef<float>& k)
 {
-    BatchPipeLaunch<float, true> l{blocks, st, mem, state, items, hdr, nsteps, ctl, k};
-    visit_variant(v, aniso, l);
-    return cudaGetLastError();
+    return v.taper ? launch_batch_pipe_f32_tp(v, aniso, blocks, st, mem, state, items, hdr, nsteps, ctl, k)
+                   : launch_batch_pipe_t<float, true, false>(v, aniso, blocks, st, mem, state, items, hdr, nsteps, ctl, k);
 }
 
 }  // namespace sks

@@ -1,12 +1,12 @@
-// Launchers of the batch step kernel for one form (T, LF); included by one
-// translation unit per form.
+// Launchers of the batch step kernel for one form (T, LF) and taper flag
+// (TP); included by one translation unit per (form, TP).
 #pragma once
 #include "sks_variants.cuh"
 
 namespace sks {
 namespace {
 
-template <typename T, bool LF>
+template <typename T, bool LF, bool TP>
 struct BatchLaunch {
     int blocks;
     cudaStream_t st;
@@ -19,12 +19,12 @@ struct BatchLaunch {
     template <bool A, int NW, bool ZS, int CAP>
     int run()
     {
-        k_step_batch<T, A, LF, NW, ZS, CAP><<<blocks, NW * 32, 0, st>>>(mem, state, items, hdr, j, k);
+        k_step_batch<T, A, LF, NW, ZS, CAP, TP><<<blocks, NW * 32, 0, st>>>(mem, state, items, hdr, j, k);
         return 0;
     }
 };
 
-template <typename T, bool LF>
+template <typename T, bool LF, bool TP>
 struct BatchPipeLaunch {
     int blocks;
     cudaStream_t st;
@@ -38,22 +38,56 @@ struct BatchPipeLaunch {
     template <bool A, int NW, bool ZS, int CAP>
     int run()
     {
-        k_step_batch_pipe<T, A, LF, NW, ZS, CAP><<<blocks, NW * 32, 0, st>>>(mem, state, items, hdr, nsteps, ctl, k);
+        k_step_batch_pipe<T, A, LF, NW, ZS, CAP, TP><<<blocks, NW * 32, 0, st>>>(mem, state, items, hdr, nsteps, ctl, k);
         return 0;
     }
 };
 
-template <typename T, bool LF>
+template <typename T, bool LF, bool TP>
 struct BatchPipeOcc {
     template <bool A, int NW, bool ZS, int CAP>
-    int run() { return occupancy_of(k_step_batch_pipe<T, A, LF, NW, ZS, CAP>, NW * 32); }
+    int run() { return occupancy_of(k_step_batch_pipe<T, A, LF, NW, ZS, CAP, TP>, NW * 32); }
 };
 
-template <typename T, bool LF>
+template <typename T, bool LF, bool TP>
 struct BatchOcc {
     template <bool A, int NW, bool ZS, int CAP>
-    int run() { return occupancy_of(k_step_batch<T, A, LF, NW, ZS, CAP>, NW * 32); }
+    int run() { return occupancy_of(k_step_batch<T, A, LF, NW, ZS, CAP, TP>, NW * 32); }
 };
+
+// the launchers of one form with (TP) or without the boundary taper
+template <typename T, bool LF, bool TP>
+int batch_occupancy_t(const StepVariant& v, bool aniso)
+{
+    BatchOcc<T, LF, TP> o;
+    return visit_variant(v, aniso, o);
+}
+
+template <typename T, bool LF, bool TP>
+cudaError_t launch_batch_t(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const BatchMember<T>* mem,
+                           const BatchState* state, const int4* items, const BatchHeader* hdr, int j, const Coef<T>& k)
+{
+    BatchLaunch<T, LF, TP> l{blocks, st, mem, state, items, hdr, j, k};
+    visit_variant(v, aniso, l);
+    return cudaGetLastError();
+}
+
+template <typename T, bool LF, bool TP>
+int batch_pipe_occupancy_t(const StepVariant& v, bool aniso)
+{
+    BatchPipeOcc<T, LF, TP> o;
+    return visit_variant(v, aniso, o);
+}
+
+template <typename T, bool LF, bool TP>
+cudaError_t launch_batch_pipe_t(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                                const BatchMember<T>* mem, const BatchState* state, const int4* items,
+                                const BatchHeader* hdr, int nsteps, const BatchPipeCtl& ctl, const Coef<T>& k)
+{
+    BatchPipeLaunch<T, LF, TP> l{blocks, st, mem, state, items, hdr, nsteps, ctl, k};
+    visit_variant(v, aniso, l);
+    return cudaGetLastError();
+}
 
 }  // namespace
 }  // namespace sks

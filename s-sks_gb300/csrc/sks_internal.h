@@ -6,6 +6,7 @@
 #include "sks_kernels.cuh"
 
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -56,6 +57,7 @@ struct sks_solver {
     uint16_t* mid;
     void* mat;                 // [nmat][16] in the form's type
     void* stc;                 // Stacey coefficients
+    void* taper;               // boundary taper factors (atten > 0), nh_att of the form's type
     int64_t* rec_off;          // per trace (step-0 recording)
     uint32_t* recbits;         // receiver bitmap over points
     int64_t* rec_sorted;       // receiver offsets, sorted
@@ -149,10 +151,11 @@ Field<T> make_field(sks_solver* s)
     F.uc = (const T*)s->U[s->cur];
     F.un = (T*)s->U[1 - s->cur];
     F.dv = (T*)s->Dv;
-    F.cc = (T*)s->Cc;
     F.mid = s->mid;
     F.mat = (const T*)s->mat;
     F.stc = (const T*)s->stc;
+    F.taper = (const T*)s->taper;
+    F.taper_zones = s->m.nh_att > 0 ? (std::min(s->m.atten, 4) | (s->m.nh_att << 3)) : 0;
     F.recbits = s->recbits;
     F.rec_off = s->rec_sorted;
     F.rec_idx = s->rec_idx;

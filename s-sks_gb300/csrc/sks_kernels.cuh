@@ -72,7 +72,9 @@ struct Field {
     T* __restrict__ un;           // FP64: u^{n-1} in, u^{n+1} out; FP32: u^{n+1} out
     T* __restrict__ dv;           // FP32 form: per component a float2 (d, c): the increment
                                   // d = u^n - u^{n-1} and the Kahan compensation of u, [3][np]
-    T* __restrict__ cc;           // unused
+    // boundary taper (atten > 0): factors taper[0..nh-1], 1 at the zone's
+    // inner edge; the zones and nh are in taper_zones at the end
+    const T* __restrict__ taper;
     const uint16_t* __restrict__ mid;   // material index per point
     const T* __restrict__ mat;          // [nmat][16]: 15 stiffness entries, 1/rho
     const T* __restrict__ stc;          // Stacey coefficients [nbnd][3][3]: dt^2/(M+A), 2M/(M+A), (M-A)/(M+A)
@@ -99,6 +101,9 @@ struct Field {
     // point, [ix/2][iz/2][2] with snap_nzs = (nz+1)/2 rows of iz per ix
     float* __restrict__ snap;
     int snap_nzs;
+    // the taper's zones in the struct's tail padding: atten (0: none; 1..4:
+    // bottom, + left, + right, + top) in bits 0-2, nh = neh*hpn above them
+    int taper_zones;
 };
 
 // Displacement layout: the P-SV pair (u_x, u_z) of every point as one 2-vector
@@ -235,9 +240,40 @@ struct PointFlags {
     bool row_ok;     // ix >= nbl (the interface row's extent)
 };
 
+// atten_wave2 (sem2d_psvsh.c:1780-1822) at one point: u^{n+1} times the
+// factor of each zone holding the point, in the reference's zone order.  The
+// FP32 form keeps its state consistent with the scaled value: the Kahan term
+// scales with u (the product's rounding error folded in), and the increment d
+// = u^{n+1} - u^n takes the change of u (exact while the factors are at
+// least 1/2, as with the default ass = 0.93).
+template <typename T, bool LF>
+__device__ __forceinline__ void taper_point(const Field<T>& F, const Geo<T>& G, int ix, int iz, T un[3], T dn[3],
+                                            T cn[3])
+{
+    const int atten = F.taper_zones & 7, nh = F.taper_zones >> 3, nx = G.nx, nz = G.nz;
+    auto scale = [&](T f) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            if constexpr (!LF) {
+                un[c] *= f;
+            } else {
+                const T u0 = un[c], u1 = u0 * f;
+                const T e = fma(f, u0, -u1);
+                cn[c] = fma(f, cn[c], -e);
+                dn[c] += u1 - u0;
+                un[c] = u1;
+            }
+        }
+    };
+    if (iz < nh) scale(F.taper[nh - iz - 1]);
+    if (atten > 1 && ix < nh && iz >= nh) scale(F.taper[nh - ix - 1]);
+    if (atten > 2 && ix >= nx - nh && iz >= nh) scale(F.taper[ix - nx + nh]);
+    if (atten > 3 && iz >= nz - nh && ix < nx - nh && ix >= nh) scale(F.taper[iz - nz + nh]);
+}
+
 // update one owned point, sample it if it is a receiver, then add the next
 // step's boundary increment if it lies on the interface line
-template <typename T, bool LF>
+template <typename T, bool LF, bool TP = false>
 __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G, const Coef<T>& k,
                                              int ix, int iz, const T u[3], const T K[3], T rinv,
                                              T wxi, T wzi, const Aux<T, LF>& x, const PointFlags& pf)
@@ -272,6 +308,9 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
             cn[c] = (t - u[c]) - y;
             un[c] = t;
         }
+    }
+    if constexpr (TP) {
+        if (F.taper_zones) taper_point<T, LF>(F, G, ix, iz, un, dn, cn);
     }
     // kirrecord_zhl: the field after the update, before the next injection
     if (iz >= F.rec_iz0 && iz <= F.rec_iz1 && ((__ldg(F.recbits + (g >> 5)) >> (g & 31)) & 1u)) {
@@ -347,7 +386,7 @@ struct TileShared {
 
 // One CTA tile: element column cx (S = 6*NW-1 owned elements), band cz of
 // element rows [ez0, ez1).
-template <typename T, bool ANISO, bool LF, int NW, bool ZS, bool CG = false>
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, bool CG = false, bool TP = false>
 __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, const Coef<T>& k, int cx, int cz,
                                           int ez0, int ez1, TileShared<T, NW>& sh)
 {
@@ -513,7 +552,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
                 }
                 if (own_x) {
                     const T wzi = b > 0 ? k.winv[b] : (ez == 0 ? k.winv[0] : k.winv2);
-                    finish_point<T, LF>(F, G, k, ix, ez * N + b, u[b], kt, rinv[b], wxi, wzi, aux[b], pfl);
+                    finish_point<T, LF, TP>(F, G, k, ix, ez * N + b, u[b], kt, rinv[b], wxi, wzi, aux[b], pfl);
                 }
             }
             if (seam_row0) {
@@ -531,7 +570,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
 #pragma unroll
                         for (int c = 0; c < 3; c++)
                             K[c] = (__ldcg(lo + c) + __ldcg(hi + c)) + (__ldcg(lo + 3 + c) + __ldcg(hi + 3 + c));
-                        finish_point<T, LF>(F, G, k, ix, ez0 * N, u[0], K, rinv[0], wxi, k.winv2, aux[0], pfl);
+                        finish_point<T, LF, TP>(F, G, k, ix, ez0 * N, u[0], K, rinv[0], wxi, k.winv2, aux[0], pfl);
                     }
                 }
             }
@@ -558,7 +597,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
             if (own_x) {
                 Aux<T, LF> x;
                 load_aux<T, LF, CG>(F, G.np, (int64_t)iz * nx + ix, x);
-                finish_point<T, LF>(F, G, k, ix, iz, u[N], kt, rinvN, wxi, k.winv[0], x, pfl);
+                finish_point<T, LF, TP>(F, G, k, ix, iz, u[N], kt, rinvN, wxi, k.winv[0], x, pfl);
             }
         } else {
             if (own_x) {
@@ -580,7 +619,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
                         K[c] = (lft[c] + __ldcg(hi + c)) + (kc[c] + __ldcg(hi + 3 + c));
                     Aux<T, LF> x;
                     load_aux<T, LF, CG>(F, G.np, (int64_t)iz * nx + ix, x);
-                    finish_point<T, LF>(F, G, k, ix, iz, u[N], K, rinvN, wxi, k.winv2, x, pfl);
+                    finish_point<T, LF, TP>(F, G, k, ix, iz, u[N], K, rinvN, wxi, k.winv2, x, pfl);
                 }
             }
         }
@@ -590,7 +629,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
 // The step of one mesh: CTA b takes tile b of the band table, or of the
 // regular ncx x ncz grid.  The arguments are plain by-value kernel
 // parameters: marking them __grid_constant__ measured 4 % slower.
-template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP>
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false>
 __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
 k_step(Field<T> F, Geo<T> G, Coef<T> k)
 {
@@ -603,7 +642,7 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
         cx = blockIdx.x % G.ncx; cz = blockIdx.x / G.ncx;
         ez0 = cz * G.HZ; ez1 = min(ez0 + G.HZ, G.nez);
     }
-    step_tile<T, ANISO, LF, NW, ZS>(F, G, k, cx, cz, ez0, ez1, sh);
+    step_tile<T, ANISO, LF, NW, ZS, false, TP>(F, G, k, cx, cz, ez0, ez1, sh);
 }
 
 // ---------------------------------------------------------------------------
@@ -640,7 +679,7 @@ struct BatchHeader {
 
 // Persistent CTAs stride over the batch's tiles (item = member, cx | cz<<16,
 // ez0, ez1); launch j of a chunk advances each member with j < n by one step.
-template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP>
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false>
 __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
 k_step_batch(const BatchMember<T>* __restrict__ mem, const BatchState* __restrict__ state,
              const int4* __restrict__ items, const BatchHeader* __restrict__ hdr, int j, Coef<T> k)
@@ -679,7 +718,7 @@ k_step_batch(const BatchMember<T>* __restrict__ mem, const BatchState* __restric
             __syncthreads();
         }
         if (s_go)
-            step_tile<T, ANISO, LF, NW, ZS>(sF, sG, k, it.y & 0xffff, it.y >> 16, it.z, it.w, sh);
+            step_tile<T, ANISO, LF, NW, ZS, false, TP>(sF, sG, k, it.y & 0xffff, it.y >> 16, it.z, it.w, sh);
         __syncthreads();
     }
 }
@@ -751,7 +790,7 @@ __device__ __forceinline__ void st_release(int* p, int v)
 
 constexpr int PIPE_SPIN_LIMIT = 1 << 22;   // polls of one wait (with 128 ns sleeps: about a second)
 
-template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP>
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false>
 __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
 k_step_pipe(Field<T> F, Geo<T> G, Coef<T> k, PipeChunk C, PipeCtl ctl)
 {
@@ -803,7 +842,7 @@ k_step_pipe(Field<T> F, Geo<T> G, Coef<T> k, PipeChunk C, PipeCtl ctl)
         }
         __syncthreads();
         if (s_fail) break;
-        step_tile<T, ANISO, LF, NW, ZS, true>(sF, G, k, cx, cz, cz * G.HZ, min(cz * G.HZ + G.HZ, G.nez), sh);
+        step_tile<T, ANISO, LF, NW, ZS, true, TP>(sF, G, k, cx, cz, cz * G.HZ, min(cz * G.HZ + G.HZ, G.nez), sh);
         // the CTA's stores are ordered before thread 0's fence by the barrier
         // (fences are cumulative), so one fence publishes the whole tile
         __syncthreads();
@@ -833,7 +872,7 @@ struct BatchPipeCtl {
     int* done;             // per tile: steps of the chunk it has finished
 };
 
-template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP>
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false>
 __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
 k_step_batch_pipe(const BatchMember<T>* __restrict__ mem, const BatchState* __restrict__ state,
                   const int4* __restrict__ items, const BatchHeader* __restrict__ hdr, int nsteps, BatchPipeCtl ctl,
@@ -902,7 +941,7 @@ k_step_batch_pipe(const BatchMember<T>* __restrict__ mem, const BatchState* __re
         }
         __syncthreads();
         if (s_fail) break;
-        if (s_go) step_tile<T, ANISO, LF, NW, ZS, true>(sF, sG, k, cx, cz, it.z, it.w, sh);
+        if (s_go) step_tile<T, ANISO, LF, NW, ZS, true, TP>(sF, sG, k, cx, cz, it.z, it.w, sh);
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();                // publishes the whole tile (see k_step_pipe)
@@ -916,7 +955,9 @@ k_step_batch_pipe(const BatchMember<T>* __restrict__ mem, const BatchState* __re
 }  // namespace sks
 
 namespace sks {
-struct StepVariant { int nw; int zseam; int cap; };
+// taper: the variant with the boundary taper (atten > 0) compiled in; the
+// others carry no code for it
+struct StepVariant { int nw; int zseam; int cap; int taper = 0; };
 cudaError_t launch_step_f32(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
                             const Field<float>& F, const Geo<float>& G, const Coef<float>& k);
 cudaError_t launch_step_f64(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
@@ -946,4 +987,36 @@ int batch_occupancy_f64(const StepVariant& v, bool aniso);
 // resident CTAs per SM of a variant (cudaOccupancyMaxActiveBlocksPerMultiprocessor)
 int step_occupancy_f32(const StepVariant& v, bool aniso);
 int step_occupancy_f64(const StepVariant& v, bool aniso);
+// the same with the boundary taper compiled in (the entry points above call
+// these for a variant with taper set)
+int step_occupancy_f32_tp(const StepVariant& v, bool aniso);
+cudaError_t launch_step_f32_tp(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                               const Field<float>& F, const Geo<float>& G, const Coef<float>& k);
+int pipe_occupancy_f32_tp(const StepVariant& v, bool aniso);
+cudaError_t launch_pipe_f32_tp(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<float>& F,
+                               const Geo<float>& G, const Coef<float>& k, const PipeChunk& C, const PipeCtl& ctl);
+int batch_occupancy_f32_tp(const StepVariant& v, bool aniso);
+cudaError_t launch_batch_f32_tp(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                                const BatchMember<float>* mem, const BatchState* state, const int4* items,
+                                const BatchHeader* hdr, int j, const Coef<float>& k);
+int batch_pipe_occupancy_f32_tp(const StepVariant& v, bool aniso);
+cudaError_t launch_batch_pipe_f32_tp(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                                     const BatchMember<float>* mem, const BatchState* state, const int4* items,
+                                     const BatchHeader* hdr, int nsteps, const BatchPipeCtl& ctl,
+                                     const Coef<float>& k);
+int step_occupancy_f64_tp(const StepVariant& v, bool aniso);
+cudaError_t launch_step_f64_tp(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                               const Field<double>& F, const Geo<double>& G, const Coef<double>& k);
+int pipe_occupancy_f64_tp(const StepVariant& v, bool aniso);
+cudaError_t launch_pipe_f64_tp(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<double>& F,
+                               const Geo<double>& G, const Coef<double>& k, const PipeChunk& C, const PipeCtl& ctl);
+int batch_occupancy_f64_tp(const StepVariant& v, bool aniso);
+cudaError_t launch_batch_f64_tp(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                                const BatchMember<double>* mem, const BatchState* state, const int4* items,
+                                const BatchHeader* hdr, int j, const Coef<double>& k);
+int batch_pipe_occupancy_f64_tp(const StepVariant& v, bool aniso);
+cudaError_t launch_batch_pipe_f64_tp(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                                     const BatchMember<double>* mem, const BatchState* state, const int4* items,
+                                     const BatchHeader* hdr, int nsteps, const BatchPipeCtl& ctl,
+                                     const Coef<double>& k);
 }  // namespace sks

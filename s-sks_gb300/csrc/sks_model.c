@@ -608,6 +608,33 @@ static int schedule(sks_model *m, char *err, size_t errlen)
     return SKS_OK;
 }
 
+/* ----------------------------------------------------------- taper */
+/* atten_taper (sem2d_psvsh.c:1724-1738): taper[n] = exp(alpha n) for n < nh =
+ * neh*hpn, alpha = log10(ass) / (nh log10(2.73)), so taper[0] = 1 and
+ * taper[nh-1] ~ ass.  The float table is the reference's (float ass, each
+ * factor rounded to float); the FP64 table takes ass as the par word's double. */
+static int taper_tables(sks_model *m, char *err, size_t errlen)
+{
+    int n;
+    const int nh = m->neh * m->hpn;
+    m->nh_att = 0;
+    if (m->atten <= 0) return SKS_OK;
+    if (!(m->ass_f > 0.f)) ERR(SKS_ERR_ARG, "ass=%g: the taper's edge factor must be positive", (double)m->ass_f);
+    m->taper_f = (float *)calloc((size_t)nh, sizeof(float));
+    m->taper_d = (double *)calloc((size_t)nh, sizeof(double));
+    if (!m->taper_f || !m->taper_d) ERR(SKS_ERR_NOMEM, "out of host memory (taper)");
+    {
+        const double alpha_f = 1.0 / nh * log10((double)m->ass_f) / log10(2.73);
+        const double alpha_d = 1.0 / nh * log10(m->ass) / log10(2.73);
+        for (n = 0; n < nh; n++) {
+            m->taper_f[n] = (float)exp((double)(alpha_f * n));
+            m->taper_d[n] = exp(alpha_d * n);
+        }
+    }
+    m->nh_att = nh;
+    return SKS_OK;
+}
+
 /* ------------------------------------------------------------------ main */
 #define PGETI(key, dst, must) do { const char *s_ = words_get(&ws, key); \
     if (s_) (dst) = atoi(s_); else if (must) { rc = SKS_ERR_ARG; snprintf(err, errlen, "par: must specify %s", key); goto done; } } while (0)
@@ -627,6 +654,7 @@ int sks_model_from_par(sks_model *m, int argc, const char *const *argv, char *er
     memset(m, 0, sizeof *m);
     /* defaults as in sem2d_psvsh.c:46-135 */
     m->flat = 1; m->nfil = 1; m->hpn = 5; m->absorb = 1; m->readpars = 1; m->neh = 1;
+    m->ass = 0.93; m->ass_f = 0.93f;
     m->xtrace = 20; m->idxplot = 20;
     m->snap_start = 100; m->snap_incre = 50;
     for (i = 1; i < argc; i++) {
@@ -660,6 +688,7 @@ int sks_model_from_par(sks_model *m, int argc, const char *const *argv, char *er
     PGETI("readpars", m->readpars, 0);
     PGETI("neh", m->neh, 0);
     PGETI("atten", m->atten, 0);
+    PGETF("ass", m->ass, m->ass_f, 0);
     PGETI("xtrace", m->xtrace, 0);
     PGETF("xbeg", m->xbeg, m->xbeg_f, 1);
     PGETF("zbeg", m->zbeg, m->zbeg_f, 0);
@@ -673,7 +702,6 @@ int sks_model_from_par(sks_model *m, int argc, const char *const *argv, char *er
     PGETI("msource", m->msource, 1);
     (void)xmin; (void)xmin_f;
     if (m->msource != 0) { rc = SKS_ERR_UNSUPPORTED; snprintf(err, errlen, "msource=%d: only the GRT boundary source (msource=0) is supported", m->msource); goto done; }
-    if (m->atten != 0) { rc = SKS_ERR_UNSUPPORTED; snprintf(err, errlen, "atten=%d: boundary attenuation is not supported", m->atten); goto done; }
     if (m->nex < 3) { rc = SKS_ERR_ARG; snprintf(err, errlen, "nex=%d: at least 3 elements are needed", m->nex); goto done; }
     if (m->nst < 1) { rc = SKS_ERR_ARG; snprintf(err, errlen, "nst=%d must be positive", m->nst); goto done; }
     if (!(m->sdt > 0) || !(m->dp > 0) || !(m->eh_par > 0)) { rc = SKS_ERR_ARG; snprintf(err, errlen, "sdt, dp and eh must be positive"); goto done; }
@@ -689,6 +717,8 @@ int sks_model_from_par(sks_model *m, int argc, const char *const *argv, char *er
     rc = mass_and_stacey(m, err, errlen);
     if (rc) goto done;
     rc = receivers(m, err, errlen);
+    if (rc) goto done;
+    rc = taper_tables(m, err, errlen);
     if (rc) goto done;
     rc = schedule(m, err, errlen);
 done:
@@ -758,5 +788,6 @@ void sks_model_free(sks_model *m)
 {
     free(m->mat); free(m->mat_id); free(m->mass); free(m->ab); free(m->rec_off);
     free(m->tap_psv); free(m->tap_sh); free(m->w_psv); free(m->w_sh);
+    free(m->taper_f); free(m->taper_d);
     memset(m, 0, sizeof *m);
 }

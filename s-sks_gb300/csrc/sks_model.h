@@ -24,6 +24,14 @@ typedef struct {
     int flat, nt, nex, nst, nfil, hpn, absorb, readpars, neh, atten, xtrace;
     int get_rec, plot_trace, idxplot, msource, semmodel_full, psv_only;
     int plot_snap, snap_start, snap_incre;   /* snapshots (sem2d_psvsh.c:149-150,202-204) */
+    /* boundary taper with atten > 0 (sem2d_psvsh.c:95-98,176-178,236-240):
+     * nh_att = neh*hpn factors exp(alpha n), alpha = log10(ass)/(nh log10(2.73)),
+     * as the reference's floats and in FP64 */
+    double ass;
+    float ass_f;
+    int nh_att;
+    float *taper_f;
+    double *taper_d;
     double dp, eh_par, sdt, xbeg, zbeg;
     float dp_f, eh_par_f, sdt_f, xbeg_f, zbeg_f;
     char greenfile[512], shgreenfile[512], raymodel[512], semmodel[512], rec_file[512];

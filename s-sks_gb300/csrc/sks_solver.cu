@@ -136,13 +136,13 @@ int dmalloc(sks_solver* s, T** p, size_t n)
 
 void free_device(sks_solver* s)
 {
-    void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc,
+    void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc, s->taper,
                   s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seisbuf[0], s->seisbuf[1], s->G, s->Dl, s->rec_psv, s->rec_sh,
                   s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt, s->items, s->seis_full,
                   s->pipe_ctl, s->snaps};
     for (void* p : ps)
         if (p) cudaFree(p);
-    s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = nullptr;
+    s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = s->taper = nullptr;
     s->mid = nullptr; s->rec_off = nullptr; s->recbits = nullptr; s->rec_sorted = nullptr; s->rec_idx = nullptr;
     s->seis = nullptr; s->seisbuf[0] = s->seisbuf[1] = nullptr; s->G = nullptr; s->Dl = nullptr;
     s->rec_psv = s->rec_sh = nullptr; s->tap_psv = s->tap_sh = nullptr; s->w_psv = s->w_sh = nullptr;
@@ -242,6 +242,15 @@ int upload_tables(sks_solver* s)
     s->stc = dstc;
     CK(cudaMemcpy(dmat, mat.data(), mat.size() * sizeof(T), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(dstc, stc.data(), stc.size() * sizeof(T), cudaMemcpyHostToDevice));
+    if (m.nh_att > 0) {
+        // the FP32 form multiplies by the reference's float factors, the FP64 form by FP64 ones
+        std::vector<T> taper((size_t)m.nh_att);
+        for (int n = 0; n < m.nh_att; n++) taper[n] = sizeof(T) == 4 ? (T)m.taper_f[n] : (T)m.taper_d[n];
+        T* dtap;
+        if ((rc = dmalloc(s, &dtap, taper.size()))) return rc;
+        s->taper = dtap;
+        CK(cudaMemcpy(dtap, taper.data(), taper.size() * sizeof(T), cudaMemcpyHostToDevice));
+    }
     // wavefield
     const size_t np = (size_t)m.nx * m.nz;
     T* u0; T* u1;
@@ -278,7 +287,7 @@ int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES, int PIPE
         s->ncz = (nez + s->HZ - 1) / s->HZ;
         s->nblocks = s->ncx * s->ncz;
     } else {
-        const StepVariant v{NW, ZS, CAP};
+        const StepVariant v{NW, ZS, CAP, s->m.nh_att > 0};
         const int occ = s->precision == SKS_FP64 ? step_occupancy_f64(v, s->m.anisotropic != 0)
                                                  : step_occupancy_f32(v, s->m.anisotropic != 0);
         int64_t target = (int64_t)s->sms * occ * WAVES;
@@ -310,7 +319,7 @@ int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES, int PIPE
         s->nblocks = (int)it.size();
     }
     if (PIPE) {
-        const StepVariant pv{NW, ZS, CAP};
+        const StepVariant pv{NW, ZS, CAP, s->m.nh_att > 0};
         const int occ = s->precision == SKS_FP64 ? pipe_occupancy_f64(pv, s->m.anisotropic != 0)
                                                  : pipe_occupancy_f32(pv, s->m.anisotropic != 0);
         s->pipe_blocks = std::max(1, std::min(s->sms * occ, s->ncx * s->ncz));
@@ -369,7 +378,7 @@ int step_impl(sks_solver* s, int it, const T* dline, float* seis_row)
     k = make_coef<T>(m);
     {
         KTimer t(s, SKS_KC_ELEMENT);
-        const StepVariant v{s->NW, s->ZS, s->CAP};
+        const StepVariant v{s->NW, s->ZS, s->CAP, s->m.nh_att > 0};
         if (sizeof(T) == 4)
             launch_step_f32(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<float>*)&F,
                             *(const Geo<float>*)&G, *(const Coef<float>*)&k);
@@ -450,7 +459,7 @@ int pipe_impl(sks_solver* s, int it1, int cnt, int i0)
     CK(cudaMemsetAsync(ctl.done, 0, sizeof(int) * (size_t)ntiles, s->stream));
     {
         KTimer t(s, SKS_KC_ELEMENT);
-        const StepVariant v{s->NW, s->ZS, s->CAP};
+        const StepVariant v{s->NW, s->ZS, s->CAP, s->m.nh_att > 0};
         cudaError_t e;
         if (sizeof(T) == 4)
             e = launch_pipe_f32(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<float>*)&F,

@@ -1,12 +1,13 @@
-// Launchers of the single-mesh step kernel for one form (T, LF); included by
-// one translation unit per form so the variants compile in parallel.
+// Launchers of the single-mesh step kernel for one form (T, LF) and taper
+// flag (TP); included by one translation unit per (form, TP) so the variants
+// compile in parallel.
 #pragma once
 #include "sks_variants.cuh"
 
 namespace sks {
 namespace {
 
-template <typename T, bool LF>
+template <typename T, bool LF, bool TP>
 struct StepLaunch {
     int blocks;
     cudaStream_t st;
@@ -16,12 +17,12 @@ struct StepLaunch {
     template <bool A, int NW, bool ZS, int CAP>
     int run()
     {
-        k_step<T, A, LF, NW, ZS, CAP><<<blocks, NW * 32, 0, st>>>(F, G, k);
+        k_step<T, A, LF, NW, ZS, CAP, TP><<<blocks, NW * 32, 0, st>>>(F, G, k);
         return 0;
     }
 };
 
-template <typename T, bool LF>
+template <typename T, bool LF, bool TP>
 struct PipeLaunch {
     int blocks;
     cudaStream_t st;
@@ -33,22 +34,55 @@ struct PipeLaunch {
     template <bool A, int NW, bool ZS, int CAP>
     int run()
     {
-        k_step_pipe<T, A, LF, NW, ZS, CAP><<<blocks, NW * 32, 0, st>>>(F, G, k, C, ctl);
+        k_step_pipe<T, A, LF, NW, ZS, CAP, TP><<<blocks, NW * 32, 0, st>>>(F, G, k, C, ctl);
         return 0;
     }
 };
 
-template <typename T, bool LF>
+template <typename T, bool LF, bool TP>
 struct PipeOcc {
     template <bool A, int NW, bool ZS, int CAP>
-    int run() { return occupancy_of(k_step_pipe<T, A, LF, NW, ZS, CAP>, NW * 32); }
+    int run() { return occupancy_of(k_step_pipe<T, A, LF, NW, ZS, CAP, TP>, NW * 32); }
 };
 
-template <typename T, bool LF>
+template <typename T, bool LF, bool TP>
 struct StepOcc {
     template <bool A, int NW, bool ZS, int CAP>
-    int run() { return occupancy_of(k_step<T, A, LF, NW, ZS, CAP>, NW * 32); }
+    int run() { return occupancy_of(k_step<T, A, LF, NW, ZS, CAP, TP>, NW * 32); }
 };
+
+// the launchers of one form with (TP) or without the boundary taper
+template <typename T, bool LF, bool TP>
+int step_occupancy_t(const StepVariant& v, bool aniso)
+{
+    StepOcc<T, LF, TP> o;
+    return visit_variant(v, aniso, o);
+}
+
+template <typename T, bool LF, bool TP>
+cudaError_t launch_step_t(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<T>& F,
+                          const Geo<T>& G, const Coef<T>& k)
+{
+    StepLaunch<T, LF, TP> l{blocks, st, F, G, k};
+    visit_variant(v, aniso, l);
+    return cudaGetLastError();
+}
+
+template <typename T, bool LF, bool TP>
+int pipe_occupancy_t(const StepVariant& v, bool aniso)
+{
+    PipeOcc<T, LF, TP> o;
+    return visit_variant(v, aniso, o);
+}
+
+template <typename T, bool LF, bool TP>
+cudaError_t launch_pipe_t(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<T>& F,
+                          const Geo<T>& G, const Coef<T>& k, const PipeChunk& C, const PipeCtl& ctl)
+{
+    PipeLaunch<T, LF, TP> l{blocks, st, F, G, k, C, ctl};
+    visit_variant(v, aniso, l);
+    return cudaGetLastError();
+}
 
 }  // namespace
 }  // namespace sks

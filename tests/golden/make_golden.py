@@ -69,6 +69,10 @@ CASES = {
     "ratio_layers": dict(prog="sem2d_psvsh", semmodel=ratio_semmodel, case=lambda: synth.Case(
         nex=14, nez=8, eh=2.0, sdt=0.01, nst=640, layers=synth.layered_two(16.0, 5.0), p=0.05,
         f0=1.0, sh_amp=0.3, ntrace=8, rec_dx=3.3)),
+    # boundary taper in all four zones (atten=4, ass=0.9), two elements wide (neh=2)
+    "psvsh_atten": dict(prog="sem2d_psvsh", case=lambda: synth.Case(
+        nex=14, nez=9, eh=2.0, sdt=0.01, nst=720, layers=aniso_layers(18.0, 40.0), p=0.05, f0=1.0,
+        sv_amp=3.0, sh_amp=1.5, neh=2, ntrace=7, rec_x0=1.0, rec_dx=4.0, extra={"atten": 4, "ass": "0.9"})),
     # snapshots (plot_snap): the reference's text files out1..outK
     "psvsh_snap": dict(prog="sem2d_psvsh", words=["plot_snap=1", "startsnap=40", "incresnap=60"],
                        case=lambda: synth.Case(

@@ -50,6 +50,14 @@ CASES = {
     "psv_only_no_absorb": lambda: synth.Case(nex=16, nez=10, eh=2.0, sdt=0.01, nst=800, layers=_aniso_layers(20.0),
                                              p=0.05, f0=1.0, ntrace=7, rec_dx=4.0, psv_only=True, absorb=0,
                                              semmodel_full=True),
+    # boundary taper (atten_wave2): bottom, left and right zones two elements wide
+    "atten3_neh2": lambda: synth.Case(nex=20, nez=10, eh=2.0, sdt=0.01, nst=800, layers=_aniso_layers(20.0),
+                                      p=0.05, f0=1.0, sv_amp=2.0, sh_amp=1.0, neh=2, ntrace=9, rec_x0=1.0,
+                                      rec_dx=4.0, semmodel_full=True, extra={"atten": 3, "ass": "0.85"}),
+    # the default taper: the bottom zone only, ass = 0.93
+    "atten1": lambda: synth.Case(nex=18, nez=9, eh=2.0, sdt=0.01, nst=760, layers=_aniso_layers(18.0, tilt=0.0),
+                                 p=0.05, f0=1.0, sv_amp=1.0, sh_amp=0.7, ntrace=9, rec_x0=0.5, rec_dx=3.7,
+                                 extra={"atten": 1}),
     "flat0_raymodel_xbeg": lambda: synth.Case(nex=20, nez=8, eh=2.0, sdt=0.01, nst=700,
                                               layers=synth.layered_two(16.0, 5.0), p=0.04, f0=1.0, flat=0,
                                               readpars=0, get_rec=0, ntrace=6, sh_amp=0.4,
@@ -113,6 +121,33 @@ def test_split_runs_equal_one_run(casedirs, prec):
     split, _ = _gpu_run(d, prec, c.nst, pieces=[1, 63, 64, 5, 70])
     for i in range(3):
         assert np.array_equal(whole[i], split[i])
+
+
+@pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])
+def test_taper_under_every_grid_and_in_a_batch(casedirs, prec):
+    """The boundary taper is applied where the point is updated, so it must
+    not depend on the CTA grid (band seams, pipelined chunks, balanced waves)
+    nor on running as a batch member."""
+    d, c, _ = casedirs["atten3_neh2"]
+    ref = None
+    with chdir(d):
+        for t in ((4, 8, 1, 0, 0, 0), (2, 1, 0, 1, 0, 1), (4, 3, 1, 1, 0, 1), (4, 4, 0, 1, 2, 0)):
+            with sks.Solver(["par=run.par"], precision=prec) as s:
+                s.load_boundary_files()
+                s.set_tuning(*t)
+                out = s.run(c.nst)
+            if ref is None:
+                ref = out
+            for i in range(3):
+                assert np.array_equal(out[i], ref[i]), (t, i)
+        with sks.Solver(["par=run.par"], precision=prec) as s:
+            s.load_boundary_files()
+            with sks.Batch(prec) as b:
+                b.add(s)
+                got = b.run(c.nst)[0]
+                b.remove(s)
+    for i in range(3):
+        assert np.array_equal(got[i], ref[i]), i
 
 
 @pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])

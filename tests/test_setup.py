@@ -137,7 +137,9 @@ def test_errors_are_status_codes(tmp_path):
         assert _err(["par=run.par", "semmodel=nope"]) == -2
         assert _err(["par=run.par", "rec_file=nope"]) == -2
         assert _err(["par=run.par", "msource=1"]) == -4             # ERR_UNSUPPORTED
-        assert _err(["par=run.par", "atten=2"]) == -4
+        assert _err(["par=run.par", "atten=2", "ass=0"]) == -1       # the taper needs ass > 0
+        with sks.Setup(["par=run.par", "atten=4", "ass=0.9"]) as su:   # the boundary taper is supported
+            assert su.info()["nx"] > 0
         assert _err(["par=run.par", "hpn=9"]) == -1                 # ERR_ARG
         with open("bad.par", "w") as f:
             f.write("".join(line for line in open("run.par") if not line.startswith("nex=")))
