@@ -86,8 +86,9 @@ int sks_load_boundary_files(sks_solver *s);
 int sks_set_boundary(sks_solver *s, const float *psv, int32_t nrec_psv,
                      const float *sh, int32_t nrec_sh);
 
-/* Boundary records generated on the device instead of read: an upgoing plane
- * P-SV (SV polarisation) and SH wave in the bottom layer, velocity vs (km/s),
+/* Boundary records generated on the device instead of read, each evaluated
+ * where the boundary interpolation reads it (the run holds no record table):
+ * an upgoing plane P-SV (SV polarisation) and SH wave in the bottom layer, velocity vs (km/s),
  * ray parameter p (s/km), Ricker pulse of dominant frequency f0 (Hz) centred
  * at 1.5/f0 s, sampled every dp (the par file's) on the interface row and
  * column at their GLL node positions (as the reference's generator places
@@ -148,9 +149,11 @@ int sks_layered_series(const sks_stack_layer_t *layers, int32_t n, const sks_lay
                        int64_t nt, double *out);
 
 /* Boundary records from the layered stack, on the device, in the layout
- * and at the node positions of sks_set_boundary_plane_wave.  Each value is
- * a series above evaluated at t - p x - eta z (cubic Lagrange between
- * samples dp/4 apart). */
+ * and at the node positions of sks_set_boundary_plane_wave, evaluated where
+ * the interpolation reads them (the run holds the mode series, not a record
+ * table).  Each value is a series above evaluated at t - p x - eta z (cubic
+ * Lagrange between samples dp/4 apart).  All boundary setters refuse a solver
+ * that is already a batch member (SKS_ERR_STATE). */
 int sks_set_boundary_layered_wave(sks_solver *s, const sks_stack_layer_t *layers, int32_t n,
                                   const sks_layered_wave_t *wave);
 

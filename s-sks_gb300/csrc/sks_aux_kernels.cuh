@@ -6,11 +6,114 @@
 
 namespace sks {
 
+// coordinate of grid point j along a row or column of degree-4 elements of
+// size eh: element j/4, GLL node j%4 at e*eh + (xi + 1)*eh/2 -- the node
+// positions of the reference's boundary-trace generator
+// (semsyn/src/aserpsv_sem.c:887-920), in the host generator's operation order
+__device__ __forceinline__ double gll_pos(int j, double eh)
+{
+    const double xi[4] = {-1.0, -0.6546536707079771, 0.0, 0.6546536707079771};
+    return __dadd_rn(__dmul_rn((double)(j >> 2), eh), __ddiv_rn(__dmul_rn(__dadd_rn(xi[j & 3], 1.0), eh), 2.0));
+}
+
+// position of value c of a record on the interface line: family 0 (P-SV:
+// u_bot(nx), w_bot(nx), u_left(nz), w_left(nz)) or 1 (SH: v_bot(nx),
+// v_left(nz)); `vert` marks the w values
+__device__ __forceinline__ void line_point(const RecSource& g, int fam, int c, double& x, double& z, bool& vert)
+{
+    const double line = gll_pos(g.nbl, g.eh);                      // height of row nbl = x of column nbl
+    int part, j;
+    if (!fam) {
+        part = (c >= 2 * g.nx) ? 1 : 0;
+        j = part ? (c - 2 * g.nx) % g.nz : c % g.nx;
+        vert = part ? (c - 2 * g.nx) >= g.nz : c >= g.nx;
+    } else {
+        part = c >= g.nx ? 1 : 0;
+        j = part ? c - g.nx : c;
+        vert = false;
+    }
+    x = part ? line : gll_pos(j, g.eh);
+    z = part ? gll_pos(j, g.eh) : line;
+}
+
+// Ricker pulse of the plane-wave generator, explicitly rounded FP64
+// operations (only exp may round differently from a host evaluation)
+__device__ __forceinline__ double ricker_at(double t, double pf)
+{
+    const double x = __dmul_rn(pf, t);
+    const double a = __dmul_rn(x, x);
+    return __dmul_rn(__dsub_rn(1.0, __dmul_rn(2.0, a)), exp(-a));
+}
+
+// Record r, value c of an upgoing plane P-SV / SH wave with a Ricker pulse in
+// the bottom layer (velocity vs, ray parameter p, dominant frequency f0),
+// sampled every dp at the line's GLL node positions: time r*dp, delay
+// tau = p*x + eta*z, eta = sqrt(1/vs^2 - p^2); SV polarisation
+// (eta*vs, -p*vs), z up; the w values hold -u_z, as the boundary files do.
+__device__ __forceinline__ float plane_record(const RecSource& g, int fam, int r, int c)
+{
+    const double eta = sqrt(fmax(__dsub_rn(__ddiv_rn(1.0, __dmul_rn(g.vs, g.vs)), __dmul_rn(g.p, g.p)), 0.0));
+    const double delay = __ddiv_rn(1.5, g.f0);
+    const double pf = __dmul_rn(3.141592653589793, g.f0);
+    double x, z;
+    bool vert;
+    line_point(g, fam, c, x, z, vert);
+    const double tau = __dadd_rn(__dmul_rn(g.p, x), __dmul_rn(eta, z));
+    const double rk = ricker_at(__dsub_rn(__dsub_rn(__dmul_rn((double)r, g.dp), delay), tau), pf);
+    if (fam) return (float)__dmul_rn(g.sh_amp, rk);
+    const double ux = __dmul_rn(__dmul_rn(g.sv_amp, eta), g.vs), uz = __dmul_rn(__dmul_rn(-g.sv_amp, g.p), g.vs);
+    return (float)(vert ? __dmul_rn(-uz, rk) : __dmul_rn(ux, rk));
+}
+
+// a series sampled every dt, periodic in nt samples, at time t: cubic
+// Lagrange through the four samples around t
+__device__ __forceinline__ double series_at(const double* __restrict__ f, int64_t nt, double t_over_dt)
+{
+    const double fl = floor(t_over_dt);
+    const double d = t_over_dt - fl;
+    int64_t i0 = (int64_t)fl % nt;
+    if (i0 < 0) i0 += nt;
+    const int64_t im = i0 == 0 ? nt - 1 : i0 - 1, i1 = i0 + 1 < nt ? i0 + 1 : i0 + 1 - nt,
+                  i2 = i0 + 2 < nt ? i0 + 2 : i0 + 2 - nt;
+    const double wm = -d * (d - 1.0) * (d - 2.0) / 6.0;
+    const double w0 = (d + 1.0) * (d - 1.0) * (d - 2.0) / 2.0;
+    const double w1 = -(d + 1.0) * d * (d - 2.0) / 2.0;
+    const double w2 = (d + 1.0) * d * (d - 1.0) / 6.0;
+    return wm * f[im] + w0 * f[i0] + w1 * f[i1] + w2 * f[i2];
+}
+
+// Record r, value c from the upgoing P, SV and SH series a layered stack
+// leaves in the bottom medium (vp0, vs0): each series at t - p x - eta_m z.
+// Displacement: P (p vp0, eta_p vp0), SV (eta_s vs0, -p vs0), SH u_y.
+__device__ __forceinline__ float layered_record(const RecSource& g, int fam, int r, int c)
+{
+    const double ep = sqrt(fmax(1.0 / (g.vp0 * g.vp0) - g.p * g.p, 0.0));
+    const double es = sqrt(fmax(1.0 / (g.vs0 * g.vs0) - g.p * g.p, 0.0));
+    double x, z;
+    bool vert;
+    line_point(g, fam, c, x, z, vert);
+    const double t = (double)r * g.dp;
+    if (fam) return (float)series_at(g.ser + 2 * g.nt, g.nt, (t - g.p * x - es * z) / g.dts);
+    const double fp = series_at(g.ser, g.nt, (t - g.p * x - ep * z) / g.dts);
+    const double fs = series_at(g.ser + g.nt, g.nt, (t - g.p * x - es * z) / g.dts);
+    return (float)(vert ? -(fp * ep * g.vp0 - fs * g.p * g.vs0) : fp * g.p * g.vp0 + fs * es * g.vs0);
+}
+
+// record r, value c of family fam as the interpolation reads it
+__device__ __forceinline__ double record_at(const RecSource& g, const float* __restrict__ rec, int fam, int n, int r,
+                                            int c)
+{
+    if (g.kind == REC_PLANE) return (double)plane_record(g, fam, r, c);
+    if (g.kind == REC_LAYERED) return (double)layered_record(g, fam, r, c);
+    return (double)rec[(int64_t)r * n + c];
+}
+
 // Boundary-trace interpolation of one step (interpl.c:16-54) into one row of
 // L = mtotal + shtotal values: four taps of FP32 records with FP64 weights,
 // then the |g| >= 10 guard of sem2d_psvsh.c:432-444 (sequential, ends read 0).
 // Called by a whole block.
-__device__ __forceinline__ void interp_row(double* __restrict__ out, int it, const float* __restrict__ rpsv, int mtotal,
+__device__ __forceinline__ void interp_row(double* __restrict__ out, int it, const RecSource& g,
+                                           const float* __restrict__ rpsv, int mtotal,
                                            const float* __restrict__ rsh, int shtotal,
                                            const int32_t* __restrict__ tap_psv, const double* __restrict__ w_psv,
                                            const int32_t* __restrict__ tap_sh, const double* __restrict__ w_sh,
@@ -32,7 +135,7 @@ __device__ __forceinline__ void interp_row(double* __restrict__ out, int it, con
             double s = 0.0;
 #pragma unroll
             for (int j = 0; j < 4; j++)
-                if (t[j] >= 0) s = fma(w[j], (double)rec[(int64_t)t[j] * n + i], s);
+                if (t[j] >= 0) s = fma(w[j], record_at(g, rec, fam, n, t[j], i), s);
             o[i] = s;
             if (!(s < 10.0 && s > -10.0)) anybad = 1;
         }
@@ -55,7 +158,7 @@ __device__ __forceinline__ void interp_row(double* __restrict__ out, int it, con
 
 // Interpolation for a chunk of steps: row r of Gout (r = 1..nsteps) is step s0+r-1.
 static __global__ void __launch_bounds__(256) k_interp(double* __restrict__ Gout, int L, int s0, int nsteps,
-                                                const float* __restrict__ rpsv, int mtotal,
+                                                const RecSource g, const float* __restrict__ rpsv, int mtotal,
                                                 const float* __restrict__ rsh, int shtotal,
                                                 const int32_t* __restrict__ tap_psv, const double* __restrict__ w_psv,
                                                 const int32_t* __restrict__ tap_sh, const double* __restrict__ w_sh)
@@ -63,7 +166,7 @@ static __global__ void __launch_bounds__(256) k_interp(double* __restrict__ Gout
     const int r = blockIdx.x;
     if (r >= nsteps) return;
     __shared__ int bad[2];
-    interp_row(Gout + (int64_t)(r + 1) * L, s0 + r, rpsv, mtotal, rsh, shtotal, tap_psv, w_psv, tap_sh, w_sh, bad);
+    interp_row(Gout + (int64_t)(r + 1) * L, s0 + r, g, rpsv, mtotal, rsh, shtotal, tap_psv, w_psv, tap_sh, w_sh, bad);
 }
 
 // One value triple of the interface-line increments: g(step of G row r+1) -
@@ -110,6 +213,7 @@ __global__ void __launch_bounds__(256) k_line_delta(T* __restrict__ Dl, const do
 struct BatchAux {
     double* G;                     // interpolation rows [(chunk+2)][L]
     void* dl;                      // line increments [chunk+1][nline][3] in the form's type
+    RecSource rs;                  // the records' source (tables below, or a generator)
     const float* rec_psv;
     const float* rec_sh;
     const int32_t* tap_psv;
@@ -133,8 +237,8 @@ static __global__ void __launch_bounds__(256) k_interp_batch(const BatchAux* __r
     const int ni = min(st.it0 + st.n + 1, a.nt_sem) - st.it0;
     if (r >= ni) return;
     __shared__ int bad[2];
-    interp_row(a.G + (int64_t)(r + 1) * a.L, st.it0 + r, a.rec_psv, a.mtotal, a.rec_sh, a.shtotal, a.tap_psv, a.w_psv,
-               a.tap_sh, a.w_sh, bad);
+    interp_row(a.G + (int64_t)(r + 1) * a.L, st.it0 + r, a.rs, a.rec_psv, a.mtotal, a.rec_sh, a.shtotal, a.tap_psv,
+               a.w_psv, a.tap_sh, a.w_sh, bad);
 }
 
 // Batched line increments: blocks (x, m) stride over member m's rows.
@@ -272,131 +376,6 @@ __global__ void __launch_bounds__(128) k_record(const T* __restrict__ u, int64_t
     out[r] = vx;
     out[ntrace + r] = vy;
     out[2 * ntrace + r] = vz;
-}
-
-// Analytic boundary records of an upgoing plane P-SV / SH wave with a Ricker
-// pulse in the bottom layer (velocity vs, ray parameter p, dominant frequency
-// f0), sampled every dp on the interface row (height nbl*h) and column
-// (x = nbl*h): record r, time r*dp, delay tau = p*x + eta*z, eta =
-// sqrt(1/vs^2 - p^2); SV polarisation (eta*vs, -p*vs), z up.  Layout as the
-// boundary files hold it: P-SV [u_bot(nx), w_bot(nx), u_left(nz), w_left(nz)],
-// SH [v_bot(nx), v_left(nz)].  Explicitly rounded FP64 operations, so only exp
-// may round differently from a host evaluation of the same formula.
-__device__ __forceinline__ double ricker_at(double t, double pf)
-{
-    const double x = __dmul_rn(pf, t);
-    const double a = __dmul_rn(x, x);
-    return __dmul_rn(__dsub_rn(1.0, __dmul_rn(2.0, a)), exp(-a));
-}
-
-// coordinate of grid point j along a row or column of degree-4 elements of
-// size eh: element j/4, GLL node j%4 at e*eh + (xi + 1)*eh/2 -- the node
-// positions of the reference's boundary-trace generator
-// (semsyn/src/aserpsv_sem.c:887-920), in the host generator's operation order
-__device__ __forceinline__ double gll_pos(int j, double eh)
-{
-    const double xi[4] = {-1.0, -0.6546536707079771, 0.0, 0.6546536707079771};
-    return __dadd_rn(__dmul_rn((double)(j >> 2), eh), __ddiv_rn(__dmul_rn(__dadd_rn(xi[j & 3], 1.0), eh), 2.0));
-}
-
-static __global__ void __launch_bounds__(256) k_plane_wave(float* __restrict__ psv, float* __restrict__ sh, int nrec_psv,
-                                                    int nrec_sh, int nx, int nz, double eh, int nbl, double vs,
-                                                    double p, double f0, double dp, double sv_amp, double sh_amp)
-{
-    const int mtotal = 2 * (nx + nz), shtotal = nx + nz;
-    const double eta = sqrt(fmax(__dsub_rn(__ddiv_rn(1.0, __dmul_rn(vs, vs)), __dmul_rn(p, p)), 0.0));
-    const double delay = __ddiv_rn(1.5, f0);
-    const double pf = __dmul_rn(3.141592653589793, f0);
-    const double line = gll_pos(nbl, eh);                          // height of row nbl = x of column nbl
-    const double zb = __dmul_rn(eta, line);
-    const double xl = __dmul_rn(p, line);
-    const double ux = __dmul_rn(__dmul_rn(sv_amp, eta), vs), uz = __dmul_rn(__dmul_rn(-sv_amp, p), vs);
-    const int64_t n1 = (int64_t)nrec_psv * mtotal, n2 = (int64_t)nrec_sh * shtotal;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n1 + n2; i += (int64_t)gridDim.x * blockDim.x) {
-        const bool fam_sh = i >= n1;
-        const int64_t k = fam_sh ? i - n1 : i;
-        const int L = fam_sh ? shtotal : mtotal;
-        const int r = (int)(k / L), c = (int)(k - (int64_t)r * L);
-        const double t = __dmul_rn((double)r, dp);
-        double tau;
-        int part;                          // 0: bottom line, 1: left column
-        int j;
-        if (!fam_sh) {
-            part = (c >= 2 * nx) ? 1 : 0;
-            j = part ? (c - 2 * nx) % nz : c % nx;
-        } else {
-            part = c >= nx ? 1 : 0;
-            j = part ? c - nx : c;
-        }
-        if (!part) tau = __dadd_rn(__dmul_rn(p, gll_pos(j, eh)), zb);
-        else tau = __dadd_rn(xl, __dmul_rn(eta, gll_pos(j, eh)));
-        const double rk = ricker_at(__dsub_rn(__dsub_rn(t, delay), tau), pf);
-        if (fam_sh) {
-            sh[k] = (float)__dmul_rn(sh_amp, rk);
-        } else {
-            const bool vert = part ? (c - 2 * nx) >= nz : c >= nx;
-            psv[k] = (float)(vert ? __dmul_rn(-uz, rk) : __dmul_rn(ux, rk));
-        }
-    }
-}
-
-// a series sampled every dt, periodic in nt samples, at time t: cubic
-// Lagrange through the four samples around t
-__device__ __forceinline__ double series_at(const double* __restrict__ f, int64_t nt, double t_over_dt)
-{
-    const double fl = floor(t_over_dt);
-    const double d = t_over_dt - fl;
-    int64_t i0 = (int64_t)fl % nt;
-    if (i0 < 0) i0 += nt;
-    const int64_t im = i0 == 0 ? nt - 1 : i0 - 1, i1 = i0 + 1 < nt ? i0 + 1 : i0 + 1 - nt,
-                  i2 = i0 + 2 < nt ? i0 + 2 : i0 + 2 - nt;
-    const double wm = -d * (d - 1.0) * (d - 2.0) / 6.0;
-    const double w0 = (d + 1.0) * (d - 1.0) * (d - 2.0) / 2.0;
-    const double w1 = -(d + 1.0) * d * (d - 2.0) / 2.0;
-    const double w2 = (d + 1.0) * d * (d - 1.0) / 6.0;
-    return wm * f[im] + w0 * f[i0] + w1 * f[i1] + w2 * f[i2];
-}
-
-// Boundary records of the upgoing P, SV and SH waves a layered stack leaves
-// in the bottom medium (vp0, vs0): the mode series ser[m*nt + i] (m = P, SV,
-// SH; sample i at i*dts) evaluated at t - p x - eta_m z on the interface row
-// and column (the node positions and record layout of k_plane_wave).
-// Displacement: P (p vp0, eta_p vp0), SV (eta_s vs0, -p vs0), SH u_y; the
-// records hold u_x and -u_z (P-SV), u_y (SH).
-static __global__ void __launch_bounds__(256) k_layered_wave(float* __restrict__ psv, float* __restrict__ sh,
-                                                      int nrec_psv, int nrec_sh, int nx, int nz, double eh, int nbl,
-                                                      const double* __restrict__ ser, int64_t nt, double dts,
-                                                      double vp0, double vs0, double p, double dp)
-{
-    const int mtotal = 2 * (nx + nz), shtotal = nx + nz;
-    const double ep = sqrt(fmax(1.0 / (vp0 * vp0) - p * p, 0.0));
-    const double es = sqrt(fmax(1.0 / (vs0 * vs0) - p * p, 0.0));
-    const double line = gll_pos(nbl, eh);
-    const int64_t n1 = (int64_t)nrec_psv * mtotal, n2 = (int64_t)nrec_sh * shtotal;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n1 + n2; i += (int64_t)gridDim.x * blockDim.x) {
-        const bool fam_sh = i >= n1;
-        const int64_t k = fam_sh ? i - n1 : i;
-        const int L = fam_sh ? shtotal : mtotal;
-        const int r = (int)(k / L), c = (int)(k - (int64_t)r * L);
-        const double t = (double)r * dp;
-        int part, j;
-        if (!fam_sh) {
-            part = (c >= 2 * nx) ? 1 : 0;
-            j = part ? (c - 2 * nx) % nz : c % nx;
-        } else {
-            part = c >= nx ? 1 : 0;
-            j = part ? c - nx : c;
-        }
-        const double x = part ? line : gll_pos(j, eh), z = part ? gll_pos(j, eh) : line;
-        if (fam_sh) {
-            sh[k] = (float)series_at(ser + 2 * nt, nt, (t - p * x - es * z) / dts);
-        } else {
-            const double fp = series_at(ser, nt, (t - p * x - ep * z) / dts);
-            const double fs = series_at(ser + nt, nt, (t - p * x - es * z) / dts);
-            const bool vert = part ? (c - 2 * nx) >= nz : c >= nx;
-            psv[k] = (float)(vert ? -(fp * ep * vp0 - fs * p * vs0) : fp * p * vp0 + fs * es * vs0);
-        }
-    }
 }
 
 }  // namespace sks

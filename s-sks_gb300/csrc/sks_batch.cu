@@ -121,6 +121,7 @@ BatchAux aux_desc(sks_solver* s)
     memset(&a, 0, sizeof a);
     a.G = s->G;
     a.dl = s->Dl;
+    a.rs = s->rs;
     a.rec_psv = s->rec_psv;
     a.rec_sh = s->rec_sh;
     a.tap_psv = s->tap_psv;

@@ -71,8 +71,11 @@ struct sks_solver {
     bool slot_busy[2];
     double* G;                 // [(chunk+2)][mtotal+shtotal]
     void* Dl;                  // [chunk+1][nline][3] line increments in the form's type
-    float* rec_psv;            // boundary records
+    float* rec_psv;            // boundary records (tables: files or caller memory)
     float* rec_sh;
+    sks::RecSource rs;         // where the interpolation takes record values from
+    double* ser;               // the layered generator's mode series [3][ser_n]
+    size_t ser_n;
     int32_t* tap_psv;
     int32_t* tap_sh;
     double* w_psv;

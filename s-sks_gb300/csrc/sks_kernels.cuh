@@ -66,6 +66,20 @@ struct Geo {
     T dt2_Je;                     // sdt^2 / Je   (M^-1 dt^2 = dt2_Je / (rho Wx Wz))
 };
 
+// Where the boundary records the interpolation reads come from: the record
+// tables (files or caller memory), or a device generator evaluated at each
+// record the interpolation reads, so generated runs hold no record table.
+enum { REC_TABLE = 0, REC_PLANE = 1, REC_LAYERED = 2 };
+struct RecSource {
+    int kind;
+    int nx, nz, nbl;                   // the grid and the interface line
+    double eh, dp, p;                  // element size, record step, ray parameter
+    double vs, f0, sv_amp, sh_amp;     // REC_PLANE: the half-space wave
+    const double* ser;                 // REC_LAYERED: mode series [3][nt], samples dts apart
+    int64_t nt;
+    double dts, vp0, vs0;              //   the top medium of the stack
+};
+
 template <typename T>
 struct Field {
     const T* __restrict__ uc;     // u^n: (u_x, u_z) pairs [np], then u_y [np]

@@ -71,7 +71,9 @@ extern "C" int sks_line_increments_noalloc(const float* rec_psv, const float* re
     // rows 1..nsteps+1 of the scratch hold g(step) for the nsteps+1 steps the
     // taps and weights describe; every row read below is written first, so
     // nothing needs clearing between calls
-    sks::k_interp<<<nsteps + 1, 256, 0, st>>>(scratch, L, 0, nsteps + 1, rec_psv, mtotal, rec_sh, shtotal,
+    sks::RecSource tables{};
+    tables.kind = sks::REC_TABLE;
+    sks::k_interp<<<nsteps + 1, 256, 0, st>>>(scratch, L, 0, nsteps + 1, tables, rec_psv, mtotal, rec_sh, shtotal,
                                               tap_psv, w_psv, tap_sh, w_sh);
     const int nline = (nx - nbl) + (nz - nbl - 1);
     const int64_t tot = (int64_t)nsteps * nline;

@@ -52,8 +52,10 @@ struct Request {
 };
 
 // device bytes a request will hold, from its model (an upper bound of what
-// the solver, its boundary records and its whole-run seismograms allocate)
-int64_t estimate_bytes(const sks_model& m, int precision)
+// the solver, its boundary records and its whole-run seismograms allocate);
+// rec_bytes: the record tables, or a generator's own (none for the plane
+// wave, the mode series for a layered stack)
+int64_t estimate_bytes(const sks_model& m, int precision, int64_t rec_bytes)
 {
     const int64_t np = (int64_t)m.nx * m.nz;
     const int64_t el = precision == SKS_FP64 ? 8 : 4;
@@ -65,7 +67,7 @@ int64_t estimate_bytes(const sks_model& m, int precision)
     if (precision == SKS_FP32C) b += 6 * np * 4;            // (d, c) pairs
     b += 2 * np + np / 8 + 64;                              // material index, receiver bitmap
     b += nb * 9 * el + (int64_t)m.nmat * 16 * el;           // Stacey coefficients, material table
-    b += ((int64_t)m.nrec_psv * m.mtotal + (int64_t)m.nrec_sh * m.shtotal) * 4;   // boundary records
+    b += rec_bytes;                                                              // boundary records
     b += (int64_t)std::max(1, m.nst) * 3 * std::max(1, m.ntrace) * 4;          // whole-run seismograms
     b += (int64_t)2 * 64 * 3 * std::max(1, m.ntrace) * 4;                        // chunk seismograms
     b += (int64_t)66 * L * 8 + (int64_t)65 * nline * 3 * el;                     // interpolation rows, increments
@@ -323,7 +325,21 @@ int submit(sks_server* v, sks_setup* su, int precision, const sks_plane_wave_t* 
         r->lw = *lw;
     }
     r->out[0] = su_out; r->out[1] = sv_out; r->out[2] = sw_out;
-    r->est_bytes = estimate_bytes(su->m, precision);
+    int64_t rec_bytes = ((int64_t)su->m.nrec_psv * su->m.mtotal + (int64_t)su->m.nrec_sh * su->m.shtotal) * 4;
+    if (pw) rec_bytes = 0;
+    if (layers) {
+        const sks_model& m = su->m;
+        const double xmax = (double)(m.nx - 1) * m.h + m.eh, zmax = (double)(m.nz - 1) * m.h + m.eh;
+        const double span = (double)std::max(m.nrec_psv, m.nrec_sh) * m.dp + lw->p * xmax + zmax / layers[0].vs;
+        const int64_t nt = sks_layered_series_length(layers, n, lw->p, lw->f0, m.dp / 4.0, span);
+        if (nt < 0) {
+            delete r;
+            sks_setup_close(su);
+            return (int)nt;
+        }
+        rec_bytes = 24 * nt;
+    }
+    r->est_bytes = estimate_bytes(su->m, precision, rec_bytes);
     r->nst = su->m.nst;
     r->ntrace = su->m.ntrace;
     r->points = (int64_t)su->m.nx * su->m.nz;

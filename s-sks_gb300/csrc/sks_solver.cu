@@ -139,13 +139,14 @@ void free_device(sks_solver* s)
     void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc, s->taper,
                   s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seisbuf[0], s->seisbuf[1], s->G, s->Dl, s->rec_psv, s->rec_sh,
                   s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt, s->items, s->seis_full,
-                  s->pipe_ctl, s->snaps};
+                  s->pipe_ctl, s->snaps, s->ser};
     for (void* p : ps)
         if (p) cudaFree(p);
     s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = s->taper = nullptr;
     s->mid = nullptr; s->rec_off = nullptr; s->recbits = nullptr; s->rec_sorted = nullptr; s->rec_idx = nullptr;
     s->seis = nullptr; s->seisbuf[0] = s->seisbuf[1] = nullptr; s->G = nullptr; s->Dl = nullptr;
     s->rec_psv = s->rec_sh = nullptr; s->tap_psv = s->tap_sh = nullptr; s->w_psv = s->w_sh = nullptr;
+    s->ser = nullptr; s->ser_n = 0; s->rs.kind = REC_TABLE;
     s->seam_lo = s->seam_hi = nullptr; s->seam_cnt = nullptr; s->seam_bytes = 0; s->seam_cnt_n = 0;
     s->items = nullptr; s->items_n = 0;
     s->seis_full = nullptr;
@@ -486,7 +487,7 @@ int run_chunk(sks_solver* s, int it0, int n)
             CK(cudaMemcpyAsync(s->G, s->G + (size_t)s->g_last * L, sizeof(double) * L, cudaMemcpyDeviceToDevice, st));
         {
             KTimer t(s, SKS_KC_INTERP);
-            k_interp<<<ni, 256, 0, st>>>(s->G, L, it0, ni, s->rec_psv, m.mtotal, s->rec_sh, m.shtotal,
+            k_interp<<<ni, 256, 0, st>>>(s->G, L, it0, ni, s->rs, s->rec_psv, m.mtotal, s->rec_sh, m.shtotal,
                                          s->tap_psv, s->w_psv, s->tap_sh, s->w_sh);
         }
         s->g_last = n;     // row of step it0+n-1: the previous step of the next chunk
@@ -719,23 +720,58 @@ int alloc_records(sks_solver* s)
 
 }  // namespace
 
+namespace {
+
+// release the record tables and the mode series (a generator replaces them)
+void free_records(sks_solver* s)
+{
+    const sks_model& m = s->m;
+    if (s->rec_psv) { cudaFree(s->rec_psv); s->device_bytes -= (int64_t)(sizeof(float) * (size_t)s->nrec_psv_loaded * m.mtotal); }
+    if (s->rec_sh) { cudaFree(s->rec_sh); s->device_bytes -= (int64_t)(sizeof(float) * (size_t)s->nrec_sh_loaded * m.shtotal); }
+    s->rec_psv = s->rec_sh = nullptr;
+    s->nrec_psv_loaded = s->nrec_sh_loaded = 0;
+}
+
+void free_series(sks_solver* s)
+{
+    if (s->ser) { cudaFree(s->ser); s->device_bytes -= (int64_t)(sizeof(double) * 3 * s->ser_n); }
+    s->ser = nullptr;
+    s->ser_n = 0;
+}
+
+// the generator's part of a record source that the grid fixes
+RecSource grid_source(const sks_solver* s, int kind)
+{
+    const sks_model& m = s->m;
+    RecSource g;
+    memset(&g, 0, sizeof g);
+    g.kind = kind;
+    g.nx = m.nx;
+    g.nz = m.nz;
+    g.nbl = s->nbl;
+    g.eh = m.eh;
+    g.dp = m.dp;
+    return g;
+}
+
+}  // namespace
+
 extern "C" int sks_set_boundary_plane_wave(sks_solver* s, const sks_plane_wave_t* pw)
 {
     if (!s || !pw) return set_err(SKS_ERR_ARG, "NULL argument");
     if (!(pw->vs > 0.0) || !(pw->f0 > 0.0) || !(pw->p >= 0.0)) return set_err(SKS_ERR_ARG, "plane wave needs vs > 0, f0 > 0, p >= 0");
-    const sks_model& m = s->m;
+    if (s->batch) return set_err(SKS_ERR_STATE, "the solver is a member of a batch: set its boundary before adding it");
     cudaSetDevice(s->device);
-    int rc = alloc_records(s);
-    if (rc) return rc;
-    const double sh_amp = m.psv_only ? 0.0 : pw->sh_amp;
-    const int64_t tot = (int64_t)m.nrec_psv * m.mtotal + (int64_t)m.nrec_sh * m.shtotal;
-    if (tot > 0) {
-        const int blocks = (int)std::min<int64_t>((tot + 255) / 256, (int64_t)s->sms * 16);
-        k_plane_wave<<<blocks, 256, 0, s->stream>>>(s->rec_psv, s->rec_sh, m.nrec_psv, m.nrec_sh, m.nx, m.nz, m.eh, s->nbl,
-                                                    pw->vs, pw->p, pw->f0, m.dp, pw->sv_amp, sh_amp);
-        CK(cudaGetLastError());
-    }
     CK(cudaStreamSynchronize(s->stream));
+    free_records(s);
+    free_series(s);
+    RecSource g = grid_source(s, REC_PLANE);
+    g.p = pw->p;
+    g.vs = pw->vs;
+    g.f0 = pw->f0;
+    g.sv_amp = pw->sv_amp;
+    g.sh_amp = s->m.psv_only ? 0.0 : pw->sh_amp;
+    s->rs = g;
     s->boundary_ready = true;
     return SKS_OK;
 }
@@ -745,6 +781,7 @@ extern "C" int sks_set_boundary_layered_wave(sks_solver* s, const sks_stack_laye
 {
     if (!s || !layers || !w) return set_err(SKS_ERR_ARG, "NULL argument");
     if (n < 2) return set_err(SKS_ERR_ARG, "layered wave: at least 2 media (top, half-space)");
+    if (s->batch) return set_err(SKS_ERR_STATE, "the solver is a member of a batch: set its boundary before adding it");
     const sks_model& m = s->m;
     // the series: samples dp/4 apart over the records' span plus the largest
     // delay along the line (p x + eta z at the far corner, slowest mode)
@@ -765,21 +802,22 @@ extern "C" int sks_set_boundary_layered_wave(sks_solver* s, const sks_stack_laye
     int rc = sks_layered_series(layers, n, &ww, dts, nt, ser.data());
     if (rc) return rc;
     cudaSetDevice(s->device);
-    rc = alloc_records(s);
-    if (rc) return rc;
-    double* dser = nullptr;
-    CK(cudaMalloc(&dser, sizeof(double) * (size_t)nt * 3));
-    cudaError_t e = cudaMemcpyAsync(dser, ser.data(), sizeof(double) * (size_t)nt * 3, cudaMemcpyHostToDevice, s->stream);
-    const int64_t tot = (int64_t)m.nrec_psv * m.mtotal + (int64_t)m.nrec_sh * m.shtotal;
-    if (e == cudaSuccess && tot > 0) {
-        const int blocks = (int)std::min<int64_t>((tot + 255) / 256, (int64_t)s->sms * 16);
-        k_layered_wave<<<blocks, 256, 0, s->stream>>>(s->rec_psv, s->rec_sh, m.nrec_psv, m.nrec_sh, m.nx, m.nz, m.eh,
-                                                      s->nbl, dser, nt, dts, layers[0].vp, layers[0].vs, w->p, m.dp);
-        e = cudaGetLastError();
+    CK(cudaStreamSynchronize(s->stream));
+    free_records(s);
+    if (s->ser_n != (size_t)nt) {
+        free_series(s);
+        if ((rc = dmalloc(s, &s->ser, 3 * (size_t)nt))) return rc;
+        s->ser_n = (size_t)nt;
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    cudaFree(dser);
-    if (e != cudaSuccess) return set_err(SKS_ERR_CUDA, "layered wave: %s", cudaGetErrorString(e));
+    CK(cudaMemcpy(s->ser, ser.data(), sizeof(double) * 3 * (size_t)nt, cudaMemcpyHostToDevice));
+    RecSource g = grid_source(s, REC_LAYERED);
+    g.p = w->p;
+    g.ser = s->ser;
+    g.nt = nt;
+    g.dts = dts;
+    g.vp0 = layers[0].vp;
+    g.vs0 = layers[0].vs;
+    s->rs = g;
     s->boundary_ready = true;
     return SKS_OK;
 }
@@ -787,6 +825,7 @@ extern "C" int sks_set_boundary_layered_wave(sks_solver* s, const sks_stack_laye
 extern "C" int sks_set_boundary(sks_solver* s, const float* psv, int32_t nrec_psv, const float* sh, int32_t nrec_sh)
 {
     if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    if (s->batch) return set_err(SKS_ERR_STATE, "the solver is a member of a batch: set its boundary before adding it");
     const sks_model& m = s->m;
     if (nrec_psv < m.nrec_psv) return set_err(SKS_ERR_BOUNDARY, "the run reads %d P-SV records, %d given", m.nrec_psv, nrec_psv);
     if (!m.psv_only && nrec_sh < m.nrec_sh) return set_err(SKS_ERR_BOUNDARY, "the run reads %d SH records, %d given", m.nrec_sh, nrec_sh);
@@ -804,6 +843,9 @@ extern "C" int sks_set_boundary(sks_solver* s, const float* psv, int32_t nrec_ps
         else CK(cudaMemcpyAsync(s->rec_sh, sh, nsh * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     }
     CK(cudaStreamSynchronize(s->stream));
+    free_series(s);
+    s->rs = RecSource{};
+    s->rs.kind = REC_TABLE;
     s->boundary_ready = true;
     return SKS_OK;
 }
@@ -1239,7 +1281,7 @@ extern "C" int sks_line_increments(sks_solver* s, int32_t it0, int32_t nsteps, d
         return set_err(SKS_ERR_NOMEM, "cudaMalloc for the boundary increments: %s", cudaGetErrorString(e));
     }
     // rows 1..nd+1 of G: steps it0..it0+nd (k_interp writes row r+1 for step it0+r)
-    k_interp<<<nd + 1, 256, 0, s->stream>>>(G, L, it0, nd + 1, s->rec_psv, m.mtotal, s->rec_sh, m.shtotal,
+    k_interp<<<nd + 1, 256, 0, s->stream>>>(G, L, it0, nd + 1, s->rs, s->rec_psv, m.mtotal, s->rec_sh, m.shtotal,
                                              s->tap_psv, s->w_psv, s->tap_sh, s->w_sh);
     const int64_t tot = (int64_t)nd * nline;
     k_line_delta<double><<<(unsigned)((tot + 255) / 256), 256, 0, s->stream>>>(D, G + L, L, nd, m.nx, m.nz, s->nbl, m.mtotal);

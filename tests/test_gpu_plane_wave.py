@@ -73,3 +73,30 @@ def test_plane_wave_rejects_bad_parameters(tmp_path):
     with pytest.raises(sks.SksError):
         s.run(5)                                   # still no boundary records
     s.close()
+
+
+def test_generated_records_hold_no_table(tmp_path):
+    """The generators are evaluated where the interpolation reads a record, so
+    a generated run holds no record table: its device memory is the table's
+    size below that of the same run fed from caller memory."""
+    d, c, vs = _case(tmp_path)
+    with chdir(d):
+        a = sks.Solver(["par=run.par"], precision=sks.FP32C)
+        b = sks.Solver(["par=run.par"], precision=sks.FP32C)
+    i = a.info()
+    nbl = i["neh"] * i["hpn"]
+    nrec = max(i["nrec_psv"], i["nrec_sh"])
+    psv, sh = synth.plane_wave_records(i["nx"], i["nz"], i["h"], nbl, vs, c.p, c.f0, c.sdt, 0, nrec,
+                                       c.sv_amp, c.sh_amp, eh=i["eh"])
+    a.set_boundary(psv[:i["nrec_psv"]], sh[:i["nrec_sh"]])
+    b.set_boundary_plane_wave(vs, c.p, c.f0, c.sv_amp, c.sh_amp)
+    table = 4 * (i["nrec_psv"] * i["mtotal"] + i["nrec_sh"] * i["shtotal"])
+    assert a.info()["device_bytes"] - b.info()["device_bytes"] == table
+    # and back: records from memory replace the generator
+    b.set_boundary(psv[:i["nrec_psv"]], sh[:i["nrec_sh"]])
+    assert b.info()["device_bytes"] == a.info()["device_bytes"]
+    ua, ub = a.run(c.nst), b.run(c.nst)
+    for k in range(3):
+        assert np.array_equal(ua[k], ub[k])
+    a.close()
+    b.close()
