@@ -135,7 +135,12 @@ __device__ __forceinline__ void interp_row(double* __restrict__ out, int it, con
             double s = 0.0;
 #pragma unroll
             for (int j = 0; j < 4; j++)
-                if (t[j] >= 0) s = fma(w[j], record_at(g, rec, fam, n, t[j], i), s);
+                // a zero weight adds exactly nothing to a generated (finite)
+                // record: skip its evaluation (with dp = sdt the weights are
+                // (0, 1, 0, 0)); table records keep every tap, as a non-finite
+                // value in a file must reach the guard below
+                if (t[j] >= 0 && (w[j] != 0.0 || g.kind == REC_TABLE))
+                    s = fma(w[j], record_at(g, rec, fam, n, t[j], i), s);
             o[i] = s;
             if (!(s < 10.0 && s > -10.0)) anybad = 1;
         }
