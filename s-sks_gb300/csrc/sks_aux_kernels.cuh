@@ -6,14 +6,18 @@
 
 namespace sks {
 
-// coordinate of grid point j along a row or column of degree-4 elements of
-// size eh: element j/4, GLL node j%4 at e*eh + (xi + 1)*eh/2 -- the node
-// positions of the reference's boundary-trace generator
-// (semsyn/src/aserpsv_sem.c:887-920), in the host generator's operation order
-__device__ __forceinline__ double gll_pos(int j, double eh)
+// coordinate of grid point j along a row or column of degree-deg elements
+// of size eh (deg 4 or 5): element j/deg, GLL node j%deg at
+// e*eh + (xi + 1)*eh/2 -- the node positions of the reference's
+// boundary-trace generator (semsyn/src/aserpsv_sem.c:887-920), in the host
+// generator's operation order
+__device__ __forceinline__ double gll_pos(int j, double eh, int deg)
 {
-    const double xi[4] = {-1.0, -0.6546536707079771, 0.0, 0.6546536707079771};
-    return __dadd_rn(__dmul_rn((double)(j >> 2), eh), __ddiv_rn(__dmul_rn(__dadd_rn(xi[j & 3], 1.0), eh), 2.0));
+    const double xi4[4] = {-1.0, -0.6546536707079771, 0.0, 0.6546536707079771};
+    const double xi5[5] = {-1.0, -0.7650553239294647, -0.2852315164806451, 0.2852315164806451, 0.7650553239294647};
+    const int e = deg == 5 ? j / 5 : j >> 2, a = deg == 5 ? j - 5 * e : j & 3;
+    const double xi = deg == 5 ? xi5[a] : xi4[a];
+    return __dadd_rn(__dmul_rn((double)e, eh), __ddiv_rn(__dmul_rn(__dadd_rn(xi, 1.0), eh), 2.0));
 }
 
 // position of value c of a record on the interface line: family 0 (P-SV:
@@ -21,7 +25,7 @@ __device__ __forceinline__ double gll_pos(int j, double eh)
 // v_left(nz)); `vert` marks the w values
 __device__ __forceinline__ void line_point(const RecSource& g, int fam, int c, double& x, double& z, bool& vert)
 {
-    const double line = gll_pos(g.nbl, g.eh);                      // height of row nbl = x of column nbl
+    const double line = gll_pos(g.nbl, g.eh, g.deg);               // height of row nbl = x of column nbl
     int part, j;
     if (!fam) {
         part = (c >= 2 * g.nx) ? 1 : 0;
@@ -32,8 +36,8 @@ __device__ __forceinline__ void line_point(const RecSource& g, int fam, int c, d
         j = part ? c - g.nx : c;
         vert = false;
     }
-    x = part ? line : gll_pos(j, g.eh);
-    z = part ? gll_pos(j, g.eh) : line;
+    x = part ? line : gll_pos(j, g.eh, g.deg);
+    z = part ? gll_pos(j, g.eh, g.deg) : line;
 }
 
 // Ricker pulse of the plane-wave generator, explicitly rounded FP64
@@ -45,24 +49,39 @@ __device__ __forceinline__ double ricker_at(double t, double pf)
     return __dmul_rn(__dsub_rn(1.0, __dmul_rn(2.0, a)), exp(-a));
 }
 
-// Record r, value c of an upgoing plane P-SV / SH wave with a Ricker pulse in
-// the bottom layer (velocity vs, ray parameter p, dominant frequency f0),
-// sampled every dp at the line's GLL node positions: time r*dp, delay
-// tau = p*x + eta*z, eta = sqrt(1/vs^2 - p^2); SV polarisation
+// An upgoing plane P-SV / SH wave with a Ricker pulse in the bottom layer
+// (velocity vs, ray parameter p, dominant frequency f0), sampled every dp at
+// the line's GLL node positions: value c of record r is amp_c R(r dp - 1.5/f0
+// - tau_c), tau = p*x + eta*z, eta = sqrt(1/vs^2 - p^2); SV polarisation
 // (eta*vs, -p*vs), z up; the w values hold -u_z, as the boundary files do.
+// The per-value delay and amplitude are tabulated once (k_plane_line).
+__device__ __forceinline__ double plane_eta(const RecSource& g)
+{
+    return sqrt(fmax(__dsub_rn(__ddiv_rn(1.0, __dmul_rn(g.vs, g.vs)), __dmul_rn(g.p, g.p)), 0.0));
+}
+
+static __global__ void __launch_bounds__(256) k_plane_line(RecSource g, double* __restrict__ lt)
+{
+    const int mtotal = 2 * (g.nx + g.nz), L = mtotal + g.nx + g.nz;
+    const double eta = plane_eta(g);
+    const double ux = __dmul_rn(__dmul_rn(g.sv_amp, eta), g.vs), uz = __dmul_rn(__dmul_rn(-g.sv_amp, g.p), g.vs);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
+        const int fam = i >= mtotal ? 1 : 0, c = fam ? i - mtotal : i;
+        double x, z;
+        bool vert;
+        line_point(g, fam, c, x, z, vert);
+        lt[i] = __dadd_rn(__dmul_rn(g.p, x), __dmul_rn(eta, z));
+        lt[L + i] = fam ? g.sh_amp : (vert ? -uz : ux);
+    }
+}
+
 __device__ __forceinline__ float plane_record(const RecSource& g, int fam, int r, int c)
 {
-    const double eta = sqrt(fmax(__dsub_rn(__ddiv_rn(1.0, __dmul_rn(g.vs, g.vs)), __dmul_rn(g.p, g.p)), 0.0));
+    const int mtotal = 2 * (g.nx + g.nz), L = mtotal + g.nx + g.nz, i = fam ? mtotal + c : c;
     const double delay = __ddiv_rn(1.5, g.f0);
     const double pf = __dmul_rn(3.141592653589793, g.f0);
-    double x, z;
-    bool vert;
-    line_point(g, fam, c, x, z, vert);
-    const double tau = __dadd_rn(__dmul_rn(g.p, x), __dmul_rn(eta, z));
-    const double rk = ricker_at(__dsub_rn(__dsub_rn(__dmul_rn((double)r, g.dp), delay), tau), pf);
-    if (fam) return (float)__dmul_rn(g.sh_amp, rk);
-    const double ux = __dmul_rn(__dmul_rn(g.sv_amp, eta), g.vs), uz = __dmul_rn(__dmul_rn(-g.sv_amp, g.p), g.vs);
-    return (float)(vert ? __dmul_rn(-uz, rk) : __dmul_rn(ux, rk));
+    const double rk = ricker_at(__dsub_rn(__dsub_rn(__dmul_rn((double)r, g.dp), delay), g.lt[i]), pf);
+    return (float)__dmul_rn(g.lt[L + i], rk);
 }
 
 // a series sampled every dt, periodic in nt samples, at time t: cubic

@@ -366,6 +366,7 @@ extern "C" int sks_batch_add(sks_batch* b, sks_solver* s)
     if (s->precision != b->precision) return set_err(SKS_ERR_ARG, "the solver's form differs from the batch's");
     if (s->device != b->device) return set_err(SKS_ERR_ARG, "the solver is on device %d, the batch on %d", s->device, b->device);
     if (s->snaps) return set_err(SKS_ERR_UNSUPPORTED, "snapshots (plot_snap=1) are taken by sks_run, not in batches");
+    if (s->m.hpn != N) return set_err(SKS_ERR_UNSUPPORTED, "hpn=%d: batches run GLL degree %d", s->m.hpn, N);
     cudaSetDevice(b->device);
     const sks_model& m = s->m;
     if (!s->seis_full) {

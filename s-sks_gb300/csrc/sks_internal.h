@@ -74,8 +74,8 @@ struct sks_solver {
     float* rec_psv;            // boundary records (tables: files or caller memory)
     float* rec_sh;
     sks::RecSource rs;         // where the interpolation takes record values from
-    double* ser;               // the layered generator's mode series [3][ser_n]
-    size_t ser_n;
+    double* ser;               // generator tables: the plane wave's line delays and amplitudes
+    size_t ser_n;              //   [2][L], or the layered stack's mode series [3][nt]; doubles held
     int32_t* tap_psv;
     int32_t* tap_sh;
     double* w_psv;
@@ -132,10 +132,11 @@ SKS_HIDDEN bool batch_running(const sks_batch* b);
 SKS_HIDDEN std::vector<sks_solver*>& batch_members(sks_batch* b);
 SKS_HIDDEN int batch_set_priority(sks_batch* b, bool high);
 
-template <typename T>
-Coef<T> make_coef(const sks_model& m)
+template <typename T, int DEG = N>
+Coef<T, DEG> make_coef(const sks_model& m)
 {
-    Coef<T> k;
+    constexpr int NP = DEG + 1;
+    Coef<T, DEG> k;
     for (int j = 0; j < NP; j++)
         for (int i = 0; i < NP; i++) {
             k.D[j * NP + i] = (T)m.dlagP[j * NP + i];

@@ -36,10 +36,15 @@
 
 namespace sks {
 
-constexpr int N = 4;          // GLL degree compiled for
+constexpr int N = 4;          // GLL degree of the default instantiation
 constexpr int NP = N + 1;     // points per element edge
 constexpr int TEX = 6;        // elements per warp tile in x
 constexpr int TW = TEX * N;   // grid columns per warp tile
+
+// The kernels are templates on the degree DEG (default 4; 5 is instantiated
+// too): DEG+1 lanes per element and 30 / (DEG+1) elements per warp, so both
+// degrees fill lanes 0..29 and leave 30, 31 idle.
+__host__ __device__ constexpr int tex_of(int deg) { return 30 / (deg + 1); }
 constexpr int MAT_STRIDE = 16;
 
 // GLL tables of degree N, the same for every mesh.  The element size drops out
@@ -47,8 +52,9 @@ constexpr int MAT_STRIDE = 16;
 // (eh/2)^2, so K = sum C (l' u) l' w w with unscaled derivatives.  The tables
 // hold l'_i(xi_j) and l'_i(xi_j) w_j without the 2/eh and eh/2 factors, and
 // one kernel argument serves every instance of a batch.
-template <typename T>
+template <typename T, int DEG = N>
 struct Coef {
+    static constexpr int NP = DEG + 1;
     T D[NP * NP];    // D[j*NP+i]  = l'_i(xi_j)
     T DWs[NP * NP];  // DWs[j*NP+i] = l'_i(xi_j) * w_j
     T w[NP];         // GLL weights
@@ -72,9 +78,10 @@ struct Geo {
 enum { REC_TABLE = 0, REC_PLANE = 1, REC_LAYERED = 2 };
 struct RecSource {
     int kind;
-    int nx, nz, nbl;                   // the grid and the interface line
+    int nx, nz, nbl, deg;              // the grid, the interface line, the GLL degree (4 or 5)
     double eh, dp, p;                  // element size, record step, ray parameter
     double vs, f0, sv_amp, sh_amp;     // REC_PLANE: the half-space wave
+    const double* lt;                  //   per line value (P-SV then SH): delay p x + eta z [L], amplitude [L]
     const double* ser;                 // REC_LAYERED: mode series [3][nt], samples dts apart
     int64_t nt;
     double dts, vp0, vs0;              //   the top medium of the stack
@@ -161,8 +168,10 @@ __device__ __forceinline__ void store_u(T* __restrict__ U, int np, int g, const 
     U[2 * np + g] = v[1];
 }
 
+template <int DEG = N>
 __device__ __forceinline__ int64_t stacey_index(int ix, int iz, int nx, int nz)
 {
+    constexpr int N = DEG;
     if (ix == 0) return iz;
     if (iz == 0) return (int64_t)nz + ix;
     if (ix == nx - 1) return (int64_t)nz + nx + iz;
@@ -287,8 +296,8 @@ __device__ __forceinline__ void taper_point(const Field<T>& F, const Geo<T>& G, 
 
 // update one owned point, sample it if it is a receiver, then add the next
 // step's boundary increment if it lies on the interface line
-template <typename T, bool LF, bool TP = false>
-__device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G, const Coef<T>& k,
+template <typename T, bool LF, bool TP = false, int DEG = N>
+__device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G, const Coef<T, DEG>& k,
                                              int ix, int iz, const T u[3], const T K[3], T rinv,
                                              T wxi, T wzi, const Aux<T, LF>& x, const PointFlags& pf)
 {
@@ -301,7 +310,7 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
 #pragma unroll
             for (int c = 0; c < 3; c++) un[c] = (-mdt2 * K[c] + (T)2 * u[c]) - x.a[c];
         } else {
-            const T* p = F.stc + stacey_index(ix, iz, G.nx, G.nz) * 9;
+            const T* p = F.stc + stacey_index<DEG>(ix, iz, G.nx, G.nz) * 9;
 #pragma unroll
             for (int c = 0; c < 3; c++) un[c] = (-p[3 * c] * K[c] + p[3 * c + 1] * u[c]) - p[3 * c + 2] * x.a[c];
         }
@@ -311,7 +320,7 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
 #pragma unroll
             for (int c = 0; c < 3; c++) dn[c] = fma(-mdt2, K[c], x.a[c]);
         } else {
-            const T* p = F.stc + stacey_index(ix, iz, G.nx, G.nz) * 9;
+            const T* p = F.stc + stacey_index<DEG>(ix, iz, G.nx, G.nz) * 9;
 #pragma unroll
             for (int c = 0; c < 3; c++) dn[c] = p[3 * c + 2] * x.a[c] - p[3 * c] * K[c];
         }
@@ -391,19 +400,20 @@ template <typename T>
 constexpr int cap_warps(int cap) { return cap == 0 ? 0 : (sizeof(T) == 4 ? (cap == 1 ? 16 : 20) : (cap == 1 ? 8 : 12)); }
 
 // shared memory of one CTA tile
-template <typename T, int NW>
+template <typename T, int NW, int DEG = N>
 struct TileShared {
-    T xch[2][NW][N][3];     // force of a warp's last column, for the next warp
+    T xch[2][NW][DEG][3];   // force of a warp's last column, for the next warp
     T xtop[NW][3];          // the same for the band's top row
     int second_arrival;
 };
 
 // One CTA tile: element column cx (S = 6*NW-1 owned elements), band cz of
 // element rows [ez0, ez1).
-template <typename T, bool ANISO, bool LF, int NW, bool ZS, bool CG = false, bool TP = false>
-__device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, const Coef<T>& k, int cx, int cz,
-                                          int ez0, int ez1, TileShared<T, NW>& sh)
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, bool CG = false, bool TP = false, int DEG = N>
+__device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, const Coef<T, DEG>& k, int cx, int cz,
+                                          int ez0, int ez1, TileShared<T, NW, DEG>& sh)
 {
+    constexpr int N = DEG, NP = DEG + 1, TEX = tex_of(DEG);
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     constexpr int S = TEX * NW - 1;                // owned elements per CTA
@@ -566,7 +576,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
                 }
                 if (own_x) {
                     const T wzi = b > 0 ? k.winv[b] : (ez == 0 ? k.winv[0] : k.winv2);
-                    finish_point<T, LF, TP>(F, G, k, ix, ez * N + b, u[b], kt, rinv[b], wxi, wzi, aux[b], pfl);
+                    finish_point<T, LF, TP, DEG>(F, G, k, ix, ez * N + b, u[b], kt, rinv[b], wxi, wzi, aux[b], pfl);
                 }
             }
             if (seam_row0) {
@@ -584,7 +594,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
 #pragma unroll
                         for (int c = 0; c < 3; c++)
                             K[c] = (__ldcg(lo + c) + __ldcg(hi + c)) + (__ldcg(lo + 3 + c) + __ldcg(hi + 3 + c));
-                        finish_point<T, LF, TP>(F, G, k, ix, ez0 * N, u[0], K, rinv[0], wxi, k.winv2, aux[0], pfl);
+                        finish_point<T, LF, TP, DEG>(F, G, k, ix, ez0 * N, u[0], K, rinv[0], wxi, k.winv2, aux[0], pfl);
                     }
                 }
             }
@@ -611,7 +621,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
             if (own_x) {
                 Aux<T, LF> x;
                 load_aux<T, LF, CG>(F, G.np, (int64_t)iz * nx + ix, x);
-                finish_point<T, LF, TP>(F, G, k, ix, iz, u[N], kt, rinvN, wxi, k.winv[0], x, pfl);
+                finish_point<T, LF, TP, DEG>(F, G, k, ix, iz, u[N], kt, rinvN, wxi, k.winv[0], x, pfl);
             }
         } else {
             if (own_x) {
@@ -633,7 +643,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
                         K[c] = (lft[c] + __ldcg(hi + c)) + (kc[c] + __ldcg(hi + 3 + c));
                     Aux<T, LF> x;
                     load_aux<T, LF, CG>(F, G.np, (int64_t)iz * nx + ix, x);
-                    finish_point<T, LF, TP>(F, G, k, ix, iz, u[N], K, rinvN, wxi, k.winv2, x, pfl);
+                    finish_point<T, LF, TP, DEG>(F, G, k, ix, iz, u[N], K, rinvN, wxi, k.winv2, x, pfl);
                 }
             }
         }
@@ -643,11 +653,11 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
 // The step of one mesh: CTA b takes tile b of the band table, or of the
 // regular ncx x ncz grid.  The arguments are plain by-value kernel
 // parameters: marking them __grid_constant__ measured 4 % slower.
-template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false>
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false, int DEG = N>
 __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
-k_step(Field<T> F, Geo<T> G, Coef<T> k)
+k_step(Field<T> F, Geo<T> G, Coef<T, DEG> k)
 {
-    __shared__ TileShared<T, NW> sh;
+    __shared__ TileShared<T, NW, DEG> sh;
     int cx, cz, ez0, ez1;
     if (G.items) {
         const int4 it = G.items[blockIdx.x];
@@ -656,7 +666,7 @@ k_step(Field<T> F, Geo<T> G, Coef<T> k)
         cx = blockIdx.x % G.ncx; cz = blockIdx.x / G.ncx;
         ez0 = cz * G.HZ; ez1 = min(ez0 + G.HZ, G.nez);
     }
-    step_tile<T, ANISO, LF, NW, ZS, false, TP>(F, G, k, cx, cz, ez0, ez1, sh);
+    step_tile<T, ANISO, LF, NW, ZS, false, TP, DEG>(F, G, k, cx, cz, ez0, ez1, sh);
 }
 
 // ---------------------------------------------------------------------------
@@ -693,12 +703,12 @@ struct BatchHeader {
 
 // Persistent CTAs stride over the batch's tiles (item = member, cx | cz<<16,
 // ez0, ez1); launch j of a chunk advances each member with j < n by one step.
-template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false>
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false, int DEG = N>
 __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
 k_step_batch(const BatchMember<T>* __restrict__ mem, const BatchState* __restrict__ state,
-             const int4* __restrict__ items, const BatchHeader* __restrict__ hdr, int j, Coef<T> k)
+             const int4* __restrict__ items, const BatchHeader* __restrict__ hdr, int j, Coef<T, DEG> k)
 {
-    __shared__ TileShared<T, NW> sh;
+    __shared__ TileShared<T, NW, DEG> sh;
     __shared__ __align__(16) Field<T> sF;
     __shared__ __align__(16) Geo<T> sG;
     __shared__ int s_go;
@@ -732,7 +742,7 @@ k_step_batch(const BatchMember<T>* __restrict__ mem, const BatchState* __restric
             __syncthreads();
         }
         if (s_go)
-            step_tile<T, ANISO, LF, NW, ZS, false, TP>(sF, sG, k, it.y & 0xffff, it.y >> 16, it.z, it.w, sh);
+            step_tile<T, ANISO, LF, NW, ZS, false, TP, DEG>(sF, sG, k, it.y & 0xffff, it.y >> 16, it.z, it.w, sh);
         __syncthreads();
     }
 }
@@ -804,11 +814,11 @@ __device__ __forceinline__ void st_release(int* p, int v)
 
 constexpr int PIPE_SPIN_LIMIT = 1 << 22;   // polls of one wait (with 128 ns sleeps: about a second)
 
-template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false>
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false, int DEG = N>
 __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
-k_step_pipe(Field<T> F, Geo<T> G, Coef<T> k, PipeChunk C, PipeCtl ctl)
+k_step_pipe(Field<T> F, Geo<T> G, Coef<T, DEG> k, PipeChunk C, PipeCtl ctl)
 {
-    __shared__ TileShared<T, NW> sh;
+    __shared__ TileShared<T, NW, DEG> sh;
     __shared__ __align__(16) Field<T> sF;
     __shared__ int s_claim, s_step, s_next, s_fail;
     const int ntiles = G.ncx * G.ncz;
@@ -856,7 +866,7 @@ k_step_pipe(Field<T> F, Geo<T> G, Coef<T> k, PipeChunk C, PipeCtl ctl)
         }
         __syncthreads();
         if (s_fail) break;
-        step_tile<T, ANISO, LF, NW, ZS, true, TP>(sF, G, k, cx, cz, cz * G.HZ, min(cz * G.HZ + G.HZ, G.nez), sh);
+        step_tile<T, ANISO, LF, NW, ZS, true, TP, DEG>(sF, G, k, cx, cz, cz * G.HZ, min(cz * G.HZ + G.HZ, G.nez), sh);
         // the CTA's stores are ordered before thread 0's fence by the barrier
         // (fences are cumulative), so one fence publishes the whole tile
         __syncthreads();
@@ -886,13 +896,13 @@ struct BatchPipeCtl {
     int* done;             // per tile: steps of the chunk it has finished
 };
 
-template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false>
+template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false, int DEG = N>
 __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
 k_step_batch_pipe(const BatchMember<T>* __restrict__ mem, const BatchState* __restrict__ state,
                   const int4* __restrict__ items, const BatchHeader* __restrict__ hdr, int nsteps, BatchPipeCtl ctl,
-                  Coef<T> k)
+                  Coef<T, DEG> k)
 {
-    __shared__ TileShared<T, NW> sh;
+    __shared__ TileShared<T, NW, DEG> sh;
     __shared__ __align__(16) Field<T> sF;
     __shared__ __align__(16) Geo<T> sG;
     __shared__ int s_claim, s_next, s_fail, s_go, s_m, s_j;
@@ -955,7 +965,7 @@ k_step_batch_pipe(const BatchMember<T>* __restrict__ mem, const BatchState* __re
         }
         __syncthreads();
         if (s_fail) break;
-        if (s_go) step_tile<T, ANISO, LF, NW, ZS, true, TP>(sF, sG, k, cx, cz, it.z, it.w, sh);
+        if (s_go) step_tile<T, ANISO, LF, NW, ZS, true, TP, DEG>(sF, sG, k, cx, cz, it.z, it.w, sh);
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();                // publishes the whole tile (see k_step_pipe)
@@ -1001,6 +1011,19 @@ int batch_occupancy_f64(const StepVariant& v, bool aniso);
 // resident CTAs per SM of a variant (cudaOccupancyMaxActiveBlocksPerMultiprocessor)
 int step_occupancy_f32(const StepVariant& v, bool aniso);
 int step_occupancy_f64(const StepVariant& v, bool aniso);
+// GLL degree 5 (single solves; 4 warps, register cap 0 or 1)
+int step_occupancy_f32_d5(const StepVariant& v, bool aniso);
+cudaError_t launch_step_f32_d5(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                               const Field<float>& F, const Geo<float>& G, const Coef<float, 5>& k);
+int pipe_occupancy_f32_d5(const StepVariant& v, bool aniso);
+cudaError_t launch_pipe_f32_d5(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<float>& F,
+                               const Geo<float>& G, const Coef<float, 5>& k, const PipeChunk& C, const PipeCtl& ctl);
+int step_occupancy_f64_d5(const StepVariant& v, bool aniso);
+cudaError_t launch_step_f64_d5(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                               const Field<double>& F, const Geo<double>& G, const Coef<double, 5>& k);
+int pipe_occupancy_f64_d5(const StepVariant& v, bool aniso);
+cudaError_t launch_pipe_f64_d5(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<double>& F,
+                               const Geo<double>& G, const Coef<double, 5>& k, const PipeChunk& C, const PipeCtl& ctl);
 // the same with the boundary taper compiled in (the entry points above call
 // these for a variant with taper set)
 int step_occupancy_f32_tp(const StepVariant& v, bool aniso);

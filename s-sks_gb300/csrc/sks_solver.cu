@@ -273,15 +273,37 @@ int upload_tables(sks_solver* s)
 // waves CTAs, each column split into bands of near-equal height, so every
 // SM carries the same work (no partly filled last wave).  The band-seam
 // buffers grow to fit and their counters restart at 0.
+// resident CTAs per SM of the solver's step / pipelined variant (form and degree)
+int step_occ(const sks_solver* s, const StepVariant& v)
+{
+    const bool a = s->m.anisotropic != 0;
+    if (s->m.hpn == 5) return s->precision == SKS_FP64 ? step_occupancy_f64_d5(v, a) : step_occupancy_f32_d5(v, a);
+    return s->precision == SKS_FP64 ? step_occupancy_f64(v, a) : step_occupancy_f32(v, a);
+}
+
+int pipe_occ(const sks_solver* s, const StepVariant& v)
+{
+    const bool a = s->m.anisotropic != 0;
+    if (s->m.hpn == 5) return s->precision == SKS_FP64 ? pipe_occupancy_f64_d5(v, a) : pipe_occupancy_f32_d5(v, a);
+    return s->precision == SKS_FP64 ? pipe_occupancy_f64(v, a) : pipe_occupancy_f32(v, a);
+}
+
+// the tunings compiled for a degree: every one for 4; for 5, 4 warps per CTA
+// and register cap 0 or 1
+bool tuning_compiled(int hpn, int NW, int CAP) { return hpn == 4 || (NW == 4 && CAP <= 1); }
+
 int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES, int PIPE)
 {
     if (PIPE && WAVES) return set_err(SKS_ERR_ARG, "pipeline=1 needs waves=0");
+    if (!tuning_compiled(s->m.hpn, NW, CAP))
+        return set_err(SKS_ERR_UNSUPPORTED, "GLL degree %d runs with 4 warps per CTA and register cap 0 or 1", s->m.hpn);
     s->NW = NW;
     s->ZS = ZS;
     s->CAP = CAP;
     s->WAVES = WAVES;
     s->PIPE = PIPE;
-    s->ncx = (s->m.nex + (TEX * NW - 1) - 1) / (TEX * NW - 1);
+    const int owned = tex_of(s->m.hpn) * NW - 1;
+    s->ncx = (s->m.nex + owned - 1) / owned;
     const int nez = s->m.nez;
     if (WAVES <= 0) {
         s->HZ = std::max(1, std::min(HZ, nez));
@@ -289,8 +311,7 @@ int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES, int PIPE
         s->nblocks = s->ncx * s->ncz;
     } else {
         const StepVariant v{NW, ZS, CAP, s->m.nh_att > 0};
-        const int occ = s->precision == SKS_FP64 ? step_occupancy_f64(v, s->m.anisotropic != 0)
-                                                 : step_occupancy_f32(v, s->m.anisotropic != 0);
+        const int occ = step_occ(s, v);
         int64_t target = (int64_t)s->sms * occ * WAVES;
         target = std::max<int64_t>(s->ncx, std::min<int64_t>(target, (int64_t)s->ncx * nez));
         std::vector<int4> it;
@@ -321,8 +342,7 @@ int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES, int PIPE
     }
     if (PIPE) {
         const StepVariant pv{NW, ZS, CAP, s->m.nh_att > 0};
-        const int occ = s->precision == SKS_FP64 ? pipe_occupancy_f64(pv, s->m.anisotropic != 0)
-                                                 : pipe_occupancy_f32(pv, s->m.anisotropic != 0);
+        const int occ = pipe_occ(s, pv);
         s->pipe_blocks = std::max(1, std::min(s->sms * occ, s->ncx * s->ncz));
         const size_t need = 2 + (size_t)s->ncx * s->ncz;
         if (need > s->pipe_ctl_n) {
@@ -375,17 +395,28 @@ int step_impl(sks_solver* s, int it, const T* dline, float* seis_row)
         F.snap = k >= 0 ? s->snaps + (size_t)k * s->snap_size : nullptr;
     }
     Geo<T> G = make_geo<T>(s);
-    static thread_local Coef<T> k;
-    k = make_coef<T>(m);
     {
         KTimer t(s, SKS_KC_ELEMENT);
         const StepVariant v{s->NW, s->ZS, s->CAP, s->m.nh_att > 0};
-        if (sizeof(T) == 4)
-            launch_step_f32(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<float>*)&F,
-                            *(const Geo<float>*)&G, *(const Coef<float>*)&k);
-        else
-            launch_step_f64(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<double>*)&F,
-                            *(const Geo<double>*)&G, *(const Coef<double>*)&k);
+        if (m.hpn == 5) {
+            static thread_local Coef<T, 5> k5;
+            k5 = make_coef<T, 5>(m);
+            if (sizeof(T) == 4)
+                launch_step_f32_d5(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<float>*)&F,
+                                   *(const Geo<float>*)&G, *(const Coef<float, 5>*)&k5);
+            else
+                launch_step_f64_d5(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<double>*)&F,
+                                   *(const Geo<double>*)&G, *(const Coef<double, 5>*)&k5);
+        } else {
+            static thread_local Coef<T> k;
+            k = make_coef<T>(m);
+            if (sizeof(T) == 4)
+                launch_step_f32(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<float>*)&F,
+                                *(const Geo<float>*)&G, *(const Coef<float>*)&k);
+            else
+                launch_step_f64(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<double>*)&F,
+                                *(const Geo<double>*)&G, *(const Coef<double>*)&k);
+        }
     }
     s->cur = 1 - s->cur;
     return SKS_OK;
@@ -438,8 +469,6 @@ int pipe_impl(sks_solver* s, int it1, int cnt, int i0)
     const size_t nline = (size_t)(m.nx - s->nbl) + (m.nz - s->nbl - 1);
     Field<T> F = make_field<T>(s);
     Geo<T> G = make_geo<T>(s);
-    static thread_local Coef<T> k;
-    k = make_coef<T>(m);
     PipeChunk C;
     C.U[0] = s->U[0];
     C.U[1] = s->U[1];
@@ -462,12 +491,25 @@ int pipe_impl(sks_solver* s, int it1, int cnt, int i0)
         KTimer t(s, SKS_KC_ELEMENT);
         const StepVariant v{s->NW, s->ZS, s->CAP, s->m.nh_att > 0};
         cudaError_t e;
-        if (sizeof(T) == 4)
-            e = launch_pipe_f32(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<float>*)&F,
-                                *(const Geo<float>*)&G, *(const Coef<float>*)&k, C, ctl);
-        else
-            e = launch_pipe_f64(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<double>*)&F,
-                                *(const Geo<double>*)&G, *(const Coef<double>*)&k, C, ctl);
+        if (m.hpn == 5) {
+            static thread_local Coef<T, 5> k5;
+            k5 = make_coef<T, 5>(m);
+            if (sizeof(T) == 4)
+                e = launch_pipe_f32_d5(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<float>*)&F,
+                                       *(const Geo<float>*)&G, *(const Coef<float, 5>*)&k5, C, ctl);
+            else
+                e = launch_pipe_f64_d5(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<double>*)&F,
+                                       *(const Geo<double>*)&G, *(const Coef<double, 5>*)&k5, C, ctl);
+        } else {
+            static thread_local Coef<T> k;
+            k = make_coef<T>(m);
+            if (sizeof(T) == 4)
+                e = launch_pipe_f32(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<float>*)&F,
+                                    *(const Geo<float>*)&G, *(const Coef<float>*)&k, C, ctl);
+            else
+                e = launch_pipe_f64(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<double>*)&F,
+                                    *(const Geo<double>*)&G, *(const Coef<double>*)&k, C, ctl);
+        }
         CK(e);
     }
     s->cur = (it1 + cnt - 1) & 1;
@@ -547,7 +589,7 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
     delete su;
     int rc = SKS_OK;
     const sks_model& m = s->m;
-    if (m.hpn != N) { sks_model_free(&s->m); delete s; return set_err(SKS_ERR_UNSUPPORTED, "hpn=%d: the kernels are built for GLL degree %d", m.hpn, N); }
+    if (m.hpn != 4 && m.hpn != 5) { sks_model_free(&s->m); delete s; return set_err(SKS_ERR_UNSUPPORTED, "hpn=%d: the kernels are built for GLL degrees 4 and 5", m.hpn); }
     s->precision = precision;
     s->device = device;
     s->nbl = m.neh * m.hpn;
@@ -574,7 +616,7 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         // not used on large meshes: with fewer CTA slots than twice the
         // element columns its bands differ in height by up to 2x (FP64, 64 M
         // points: 30.5 ms against 21.1).
-        const int ncx4 = (m.nex + (TEX * 4 - 1) - 1) / (TEX * 4 - 1);
+        const int ncx4 = (m.nex + (tex_of(m.hpn) * 4 - 1) - 1) / (tex_of(m.hpn) * 4 - 1);
         const int64_t pts = (int64_t)m.nx * m.nz;
         int rcg;
         if (pts <= ((int64_t)2 << 20))
@@ -734,7 +776,7 @@ void free_records(sks_solver* s)
 
 void free_series(sks_solver* s)
 {
-    if (s->ser) { cudaFree(s->ser); s->device_bytes -= (int64_t)(sizeof(double) * 3 * s->ser_n); }
+    if (s->ser) { cudaFree(s->ser); s->device_bytes -= (int64_t)(sizeof(double) * s->ser_n); }
     s->ser = nullptr;
     s->ser_n = 0;
 }
@@ -749,6 +791,7 @@ RecSource grid_source(const sks_solver* s, int kind)
     g.nx = m.nx;
     g.nz = m.nz;
     g.nbl = s->nbl;
+    g.deg = m.hpn;
     g.eh = m.eh;
     g.dp = m.dp;
     return g;
@@ -771,6 +814,15 @@ extern "C" int sks_set_boundary_plane_wave(sks_solver* s, const sks_plane_wave_t
     g.f0 = pw->f0;
     g.sv_amp = pw->sv_amp;
     g.sh_amp = s->m.psv_only ? 0.0 : pw->sh_amp;
+    // the line's delays and amplitudes, once: [2][L] doubles in the series buffer
+    const size_t L = (size_t)s->m.mtotal + s->m.shtotal;
+    int rc;
+    if ((rc = dmalloc(s, &s->ser, 2 * L))) return rc;
+    s->ser_n = 2 * L;
+    k_plane_line<<<(unsigned)((L + 255) / 256), 256, 0, s->stream>>>(g, s->ser);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    g.lt = s->ser;
     s->rs = g;
     s->boundary_ready = true;
     return SKS_OK;
@@ -804,10 +856,10 @@ extern "C" int sks_set_boundary_layered_wave(sks_solver* s, const sks_stack_laye
     cudaSetDevice(s->device);
     CK(cudaStreamSynchronize(s->stream));
     free_records(s);
-    if (s->ser_n != (size_t)nt) {
+    if (s->ser_n != 3 * (size_t)nt) {
         free_series(s);
         if ((rc = dmalloc(s, &s->ser, 3 * (size_t)nt))) return rc;
-        s->ser_n = (size_t)nt;
+        s->ser_n = 3 * (size_t)nt;
     }
     CK(cudaMemcpy(s->ser, ser.data(), sizeof(double) * 3 * (size_t)nt, cudaMemcpyHostToDevice));
     RecSource g = grid_source(s, REC_LAYERED);
@@ -1237,6 +1289,7 @@ extern "C" int sks_autotune(sks_solver* s, int32_t steps, sks_tuning_t* best)
                 const int hz = cand < nhz ? hzs[cand] : 0, wv = cand < nhz ? 0 : cand - nhz + 1;
                 if (wv == 0 && hz > m.nez && hz != hzs[0]) continue;
                 if (pipe && wv) continue;
+                if (!tuning_compiled(m.hpn, nw, cap)) continue;
                 if ((rc = snap_restore(s, snap))) break;
                 if ((rc = set_grid(s, nw, hz, zs, cap, wv, pipe))) break;
                 // one untimed step, then the timed ones

@@ -190,7 +190,7 @@ def write_case(case: Case, d: str, absolute: bool = False) -> dict:
     if case.write_records:
         write_plane_wave(os.path.join(d, "greenfile"), os.path.join(d, "shgreenfile"),
                          nx=nx, nz=nz, h=h, nbl=nbl, vs=vs_b, p=case.p, f0=case.f0,
-                         dp=dp, nt=nt, sv_amp=case.sv_amp, sh_amp=case.sh_amp, eh=float(eh_eff))
+                         dp=dp, nt=nt, sv_amp=case.sv_amp, sh_amp=case.sh_amp, eh=float(eh_eff), deg=N)
     name = (lambda f: os.path.join(os.path.abspath(d), f)) if absolute else (lambda f: f)
     par = {
         "greenfile": name("greenfile"), "shgreenfile": name("shgreenfile"), "raymodel": name("raymodel"),
@@ -217,27 +217,34 @@ def ricker(t: np.ndarray, f0: float) -> np.ndarray:
 
 
 GLL4 = (-1.0, -0.6546536707079771, 0.0, 0.6546536707079771, 1.0)    # GLL points of degree 4
+GLL5 = (-1.0, -0.7650553239294647, -0.2852315164806451, 0.2852315164806451, 0.7650553239294647, 1.0)
+GLL_POINTS = {4: GLL4, 5: GLL5}
 
 
-def gll_positions(n: int, eh: float) -> np.ndarray:
-    """Coordinates of grid points 0..n-1 along a row or column of degree-4
-    elements of size eh: point 4e+m at e*eh + (xi_m + 1)*eh/2, the node
+def gll_positions(n: int, eh: float, deg: int = 4) -> np.ndarray:
+    """Coordinates of grid points 0..n-1 along a row or column of degree-deg
+    elements of size eh: point deg*e+m at e*eh + (xi_m + 1)*eh/2, the node
     positions the reference's boundary-trace generator uses
     (semsyn/src/aserpsv_sem.c:887-920, Grid_Point)."""
-    e, m = np.divmod(np.arange(n), 4)
-    return e * eh + (np.array(GLL4)[m] + 1.0) * eh / 2.0
+    if deg in GLL_POINTS:
+        xi = np.array(GLL_POINTS[deg])
+    else:                                        # +-1 and the roots of P_deg'
+        inner = np.sort(np.polynomial.legendre.Legendre.basis(deg).deriv().roots().real)
+        xi = np.concatenate([[-1.0], inner, [1.0]])
+    e, m = np.divmod(np.arange(n), deg)
+    return e * eh + (xi[m] + 1.0) * eh / 2.0
 
 
-def plane_wave_records(nx, nz, h, nbl, vs, p, f0, dp, r0, r1, sv_amp=1.0, sh_amp=0.0, eh=None):
+def plane_wave_records(nx, nz, h, nbl, vs, p, f0, dp, r0, r1, sv_amp=1.0, sh_amp=0.0, eh=None, deg=4):
     """Records r0..r1-1 of the boundary traces (float32, time-major), the
     plane wave timed at the GLL node positions of the line (eh: the element
-    size, 4h when not given)."""
-    eh = 4.0 * h if eh is None else eh
+    size, deg*h when not given; deg: the GLL degree)."""
+    eh = deg * h if eh is None else eh
     eta = math.sqrt(max(1.0 / vs ** 2 - p ** 2, 0.0))
     delay = 1.5 / f0
-    xb = gll_positions(nx, eh)                 # bottom line, at the height of row nbl
-    zl = gll_positions(nz, eh)                 # left column, at the position of column nbl
-    line = gll_positions(nbl + 1, eh)[nbl]
+    xb = gll_positions(nx, eh, deg)            # bottom line, at the height of row nbl
+    zl = gll_positions(nz, eh, deg)            # left column, at the position of column nbl
+    line = gll_positions(nbl + 1, eh, deg)[nbl]
     tau_b = p * xb + eta * line
     tau_l = p * line + eta * zl
     t = (np.arange(r0, r1) * dp)[:, None]
@@ -250,11 +257,11 @@ def plane_wave_records(nx, nz, h, nbl, vs, p, f0, dp, r0, r1, sv_amp=1.0, sh_amp
 
 
 def write_plane_wave(psv_path, sh_path, *, nx, nz, h, nbl, vs, p, f0, dp, nt,
-                     sv_amp=1.0, sh_amp=0.0, chunk=1024, eh=None):
+                     sv_amp=1.0, sh_amp=0.0, chunk=1024, eh=None, deg=4):
     with open(psv_path, "wb") as fp, open(sh_path, "wb") as fs:
         for r0 in range(0, nt, chunk):
             psv, sh = plane_wave_records(nx, nz, h, nbl, vs, p, f0, dp, r0, min(nt, r0 + chunk),
-                                         sv_amp, sh_amp, eh)
+                                         sv_amp, sh_amp, eh, deg)
             fp.write(psv.tobytes())
             fs.write(sh.tobytes())
 

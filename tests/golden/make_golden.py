@@ -73,6 +73,10 @@ CASES = {
     "psvsh_atten": dict(prog="sem2d_psvsh", case=lambda: synth.Case(
         nex=14, nez=9, eh=2.0, sdt=0.01, nst=720, layers=aniso_layers(18.0, 40.0), p=0.05, f0=1.0,
         sv_amp=3.0, sh_amp=1.5, neh=2, ntrace=7, rec_x0=1.0, rec_dx=4.0, extra={"atten": 4, "ass": "0.9"})),
+    # GLL degree 5, the reference's default hpn (records at the degree-5 node positions)
+    "psvsh_hpn5": dict(prog="sem2d_psvsh", case=lambda: synth.Case(
+        nex=12, nez=7, eh=2.5, sdt=0.01, nst=640, layers=aniso_layers(17.5, 50.0), p=0.05, f0=1.0,
+        sv_amp=1.0, sh_amp=0.6, hpn=5, ntrace=7, rec_x0=1.0, rec_dx=4.0)),
     # snapshots (plot_snap): the reference's text files out1..outK
     "psvsh_snap": dict(prog="sem2d_psvsh", words=["plot_snap=1", "startsnap=40", "incresnap=60"],
                        case=lambda: synth.Case(

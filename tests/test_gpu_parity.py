@@ -58,6 +58,10 @@ CASES = {
     "atten1": lambda: synth.Case(nex=18, nez=9, eh=2.0, sdt=0.01, nst=760, layers=_aniso_layers(18.0, tilt=0.0),
                                  p=0.05, f0=1.0, sv_amp=1.0, sh_amp=0.7, ntrace=9, rec_x0=0.5, rec_dx=3.7,
                                  extra={"atten": 1}),
+    # GLL degree 5 (the reference's default hpn): 5 elements per warp
+    "hpn5_aniso": lambda: synth.Case(nex=23, nez=8, eh=2.0, sdt=0.008, nst=900, layers=_aniso_layers(16.0),
+                                     p=0.05, f0=1.0, sv_amp=1.0, sh_amp=0.5, hpn=5, ntrace=9, rec_x0=1.0,
+                                     rec_dx=4.5, semmodel_full=True),
     "flat0_raymodel_xbeg": lambda: synth.Case(nex=20, nez=8, eh=2.0, sdt=0.01, nst=700,
                                               layers=synth.layered_two(16.0, 5.0), p=0.04, f0=1.0, flat=0,
                                               readpars=0, get_rec=0, ntrace=6, sh_amp=0.4,
@@ -148,6 +152,35 @@ def test_taper_under_every_grid_and_in_a_batch(casedirs, prec):
                 b.remove(s)
     for i in range(3):
         assert np.array_equal(got[i], ref[i]), i
+
+
+@pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])
+def test_degree5_tunings_bit_identical_and_refusals(casedirs, prec):
+    """Degree 5 compiles 4-warp CTAs with register cap 0 or 1: every such grid
+    (seams or halo rows, per-step or pipelined, balanced waves) gives the same
+    bits; other tunings and batches are refused."""
+    d, c, _ = casedirs["hpn5_aniso"]
+    ref = None
+    with chdir(d):
+        for t in ((4, 3, 0, 0, 0, 0), (4, 1, 1, 1, 0, 0), (4, 8, 0, 1, 0, 1), (4, 2, 1, 0, 0, 1), (4, 4, 0, 1, 2, 0)):
+            with sks.Solver(["par=run.par"], precision=prec) as s:
+                s.load_boundary_files()
+                s.set_tuning(*t)
+                out = s.run(c.nst)
+            if ref is None:
+                ref = out
+            for i in range(3):
+                assert np.array_equal(out[i], ref[i]), (t, i)
+        with sks.Solver(["par=run.par"], precision=prec) as s:
+            for bad in ((2, 4, 0, 1, 0, 0), (4, 4, 0, 2, 0, 0)):
+                with pytest.raises(sks.SksError):
+                    s.set_tuning(*bad)
+            s.load_boundary_files()
+            with sks.Batch(prec) as b:
+                with pytest.raises(sks.SksError):
+                    b.add(s)
+        with pytest.raises(sks.SksError):
+            sks.Solver(["par=run.par", "hpn=6"], precision=prec)
 
 
 @pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])

@@ -17,22 +17,22 @@ from util import chdir
 pytestmark = pytest.mark.gpu
 
 
-def _case(tmp_path, psv_only=False, sh_amp=0.6):
+def _case(tmp_path, psv_only=False, sh_amp=0.6, hpn=4):
     H = 12.002
     layers = [synth.SemLayer(H - 6, synth.iso_cij(8.1, 4.5, 3.4), 3.4),
               synth.SemLayer(H - 3, synth.hexagonal_cij(8.1, 4.5, 3.4, 0.05, 30.0, 15.0), 3.4),
               synth.SemLayer(H + 1, synth.iso_cij(6.4, 3.6, 2.8), 2.8)]
     c = synth.Case(nex=29, nez=12, eh=1.0, sdt=0.005, nst=700, layers=layers, p=0.044, f0=1.3, sv_amp=1.0,
                    sh_amp=sh_amp, ntrace=13, rec_dx=2.0, semmodel_full=True, write_records=False,
-                   psv_only=psv_only)
+                   psv_only=psv_only, hpn=hpn)
     d = str(tmp_path)
     synth.write_case(c, d)
     return d, c, float(np.sqrt(layers[0].C[3, 3] / layers[0].rho))
 
 
-@pytest.mark.parametrize("psv_only", [False, True])
-def test_device_records_match_host_generator(tmp_path, psv_only):
-    d, c, vs = _case(tmp_path, psv_only)
+@pytest.mark.parametrize("psv_only,hpn", [(False, 4), (True, 4), (False, 5)])
+def test_device_records_match_host_generator(tmp_path, psv_only, hpn):
+    d, c, vs = _case(tmp_path, psv_only, hpn=hpn)
     sh_amp = 0.0 if psv_only else c.sh_amp
     with chdir(d):
         host = sks.Solver(["par=run.par"], precision=sks.FP64)
@@ -41,7 +41,7 @@ def test_device_records_match_host_generator(tmp_path, psv_only):
     nbl = i["neh"] * i["hpn"]
     nrec = max(i["nrec_psv"], i["nrec_sh"])
     psv, sh = synth.plane_wave_records(i["nx"], i["nz"], i["h"], nbl, vs, c.p, c.f0, c.sdt, 0, nrec,
-                                       c.sv_amp, sh_amp, eh=i["eh"])
+                                       c.sv_amp, sh_amp, eh=i["eh"], deg=hpn)
     host.set_boundary(psv[:i["nrec_psv"]], None if psv_only else sh[:i["nrec_sh"]])
     dev.set_boundary_plane_wave(vs, c.p, c.f0, c.sv_amp, sh_amp)
     # interpolated FP64 increments of the interface line: one float32 ulp of a record at most
@@ -78,7 +78,8 @@ def test_plane_wave_rejects_bad_parameters(tmp_path):
 def test_generated_records_hold_no_table(tmp_path):
     """The generators are evaluated where the interpolation reads a record, so
     a generated run holds no record table: its device memory is the table's
-    size below that of the same run fed from caller memory."""
+    size below that of the same run fed from caller memory, less the line's
+    delays and amplitudes (two doubles per line value)."""
     d, c, vs = _case(tmp_path)
     with chdir(d):
         a = sks.Solver(["par=run.par"], precision=sks.FP32C)
@@ -91,7 +92,8 @@ def test_generated_records_hold_no_table(tmp_path):
     a.set_boundary(psv[:i["nrec_psv"]], sh[:i["nrec_sh"]])
     b.set_boundary_plane_wave(vs, c.p, c.f0, c.sv_amp, c.sh_amp)
     table = 4 * (i["nrec_psv"] * i["mtotal"] + i["nrec_sh"] * i["shtotal"])
-    assert a.info()["device_bytes"] - b.info()["device_bytes"] == table
+    line = 16 * (i["mtotal"] + i["shtotal"])
+    assert a.info()["device_bytes"] - b.info()["device_bytes"] == table - line
     # and back: records from memory replace the generator
     b.set_boundary(psv[:i["nrec_psv"]], sh[:i["nrec_sh"]])
     assert b.info()["device_bytes"] == a.info()["device_bytes"]
