@@ -72,8 +72,8 @@ typedef struct {
  * boundary-trace files are NOT read here (see sks_load_boundary_files).
  * Options the reference has that this library does not run return
  * SKS_ERR_UNSUPPORTED: msource=1 (explosive source), and GLL degrees other
- * than hpn = 4 or 5 (degree 5, the reference's default, runs single solves
- * with 4-warp CTAs; batches take degree 4).  atten>0 (with ass) runs the
+ * than hpn = 4 or 5 (degree 5, the reference's default, runs with 4-warp
+ * CTAs, register cap 0 or 1; a batch's members share one degree).  atten>0 (with ass) runs the
  * reference's boundary taper (atten_wave2, sem2d_psvsh.c:1780-1822). */
 int sks_open_par(int argc, const char *const *argv, int precision, int device,
                  sks_solver **out);

@@ -34,6 +34,7 @@ struct sks_batch {
     int chunk = 64;
     bool aniso = false;                   // the step variant: any member anisotropic
     bool taper = false;                   // ... any member with the boundary taper (atten > 0)
+    int deg = 0;                          // ... the members' GLL degree (the captured graph's)
     int grid = 0;                         // persistent CTAs of a step launch
     // device tables (capacity `cap` members, `items_cap` tiles)
     void* dmem = nullptr;                 // BatchMember<T>[cap]
@@ -63,6 +64,13 @@ struct sks_batch {
 namespace {
 
 bool member_aniso(const sks_solver* s) { return s->m.anisotropic != 0; }
+
+// the members' GLL degree (they share one; 4 while the batch is empty)
+int batch_deg(const sks_batch* b) { return b->mem.empty() ? N : b->mem[0]->m.hpn; }
+
+// the tunings compiled for a degree: every one for 4; for 5, 4 warps per CTA
+// and register cap 0 or 1
+bool batch_tuning_compiled(int deg, int NW, int CAP) { return deg == N || (NW == 4 && CAP <= 1); }
 
 int nline_of(const sks_solver* s) { return (s->m.nx - s->nbl) + (s->m.nz - s->nbl - 1); }
 
@@ -162,9 +170,11 @@ int build_tables(sks_batch* b)
             for (int cx = 0; cx < s->ncx; cx++)
                 items.push_back(make_int4(i, cx | (cz << 16), cz * s->HZ, std::min((cz + 1) * s->HZ, s->m.nez)));
     }
-    if (aniso != b->aniso || taper != b->taper) {
+    const int deg = batch_deg(b);
+    if (aniso != b->aniso || taper != b->taper || deg != b->deg) {
         b->aniso = aniso;
         b->taper = taper;
+        b->deg = deg;
         b->graph_dirty = true;
     }
     if (n > b->cap) {
@@ -219,6 +229,15 @@ template <typename T>
 cudaError_t launch_steps(sks_batch* b, int j)
 {
     const StepVariant v{b->NW, b->ZS, b->CAP, b->taper};
+    if (batch_deg(b) == 5) {
+        static thread_local Coef<T, 5> k5;
+        k5 = make_coef<T, 5>(b->mem[0]->m);
+        if (sizeof(T) == 4)
+            return launch_batch_f32_d5(v, b->aniso, b->grid, b->stream, (const BatchMember<float>*)b->dmem, b->dstate,
+                                       b->ditems, b->dhdr, j, *(const Coef<float, 5>*)&k5);
+        return launch_batch_f64_d5(v, b->aniso, b->grid, b->stream, (const BatchMember<double>*)b->dmem, b->dstate,
+                                   b->ditems, b->dhdr, j, *(const Coef<double, 5>*)&k5);
+    }
     static thread_local Coef<T> k;
     k = make_coef<T>(b->mem[0]->m);     // GLL tables: the same for every member
     if (sizeof(T) == 4)
@@ -238,6 +257,15 @@ cudaError_t launch_pipe_chunk(sks_batch* b, int nsteps)
     cudaError_t e = cudaMemsetAsync(b->dpipe, 0, sizeof(int) * (2 + b->items_cap), b->stream);
     if (e != cudaSuccess) return e;
     const BatchPipeCtl ctl{b->dpipe, b->dpipe + 1, b->dpipe + 2};
+    if (batch_deg(b) == 5) {
+        static thread_local Coef<T, 5> k5;
+        k5 = make_coef<T, 5>(b->mem[0]->m);
+        if (sizeof(T) == 4)
+            return launch_batch_pipe_f32_d5(v, b->aniso, b->grid, b->stream, (const BatchMember<float>*)b->dmem,
+                                            b->dstate, b->ditems, b->dhdr, nsteps, ctl, *(const Coef<float, 5>*)&k5);
+        return launch_batch_pipe_f64_d5(v, b->aniso, b->grid, b->stream, (const BatchMember<double>*)b->dmem, b->dstate,
+                                        b->ditems, b->dhdr, nsteps, ctl, *(const Coef<double, 5>*)&k5);
+    }
     if (sizeof(T) == 4)
         return launch_batch_pipe_f32(v, b->aniso, b->grid, b->stream, (const BatchMember<float>*)b->dmem, b->dstate,
                                      b->ditems, b->dhdr, nsteps, ctl, *(const Coef<float>*)&k);
@@ -250,8 +278,14 @@ void set_persistent_grid(sks_batch* b)
 {
     const StepVariant v{b->NW, b->ZS, b->CAP, b->taper};
     int occ;
-    if (b->PIPE) occ = b->precision == SKS_FP64 ? batch_pipe_occupancy_f64(v, b->aniso) : batch_pipe_occupancy_f32(v, b->aniso);
-    else occ = b->precision == SKS_FP64 ? batch_occupancy_f64(v, b->aniso) : batch_occupancy_f32(v, b->aniso);
+    const bool f64 = b->precision == SKS_FP64;
+    if (batch_deg(b) == 5) {
+        if (b->PIPE) occ = f64 ? batch_pipe_occupancy_f64_d5(v, b->aniso) : batch_pipe_occupancy_f32_d5(v, b->aniso);
+        else occ = f64 ? batch_occupancy_f64_d5(v, b->aniso) : batch_occupancy_f32_d5(v, b->aniso);
+    } else {
+        if (b->PIPE) occ = f64 ? batch_pipe_occupancy_f64(v, b->aniso) : batch_pipe_occupancy_f32(v, b->aniso);
+        else occ = f64 ? batch_occupancy_f64(v, b->aniso) : batch_occupancy_f32(v, b->aniso);
+    }
     b->grid = b->sms * occ;
 }
 
@@ -366,7 +400,11 @@ extern "C" int sks_batch_add(sks_batch* b, sks_solver* s)
     if (s->precision != b->precision) return set_err(SKS_ERR_ARG, "the solver's form differs from the batch's");
     if (s->device != b->device) return set_err(SKS_ERR_ARG, "the solver is on device %d, the batch on %d", s->device, b->device);
     if (s->snaps) return set_err(SKS_ERR_UNSUPPORTED, "snapshots (plot_snap=1) are taken by sks_run, not in batches");
-    if (s->m.hpn != N) return set_err(SKS_ERR_UNSUPPORTED, "hpn=%d: batches run GLL degree %d", s->m.hpn, N);
+    if (s->m.hpn != 4 && s->m.hpn != 5) return set_err(SKS_ERR_UNSUPPORTED, "hpn=%d: batches run GLL degrees 4 and 5", s->m.hpn);
+    if (!b->mem.empty() && s->m.hpn != batch_deg(b))
+        return set_err(SKS_ERR_ARG, "hpn=%d: the batch's members are of GLL degree %d", s->m.hpn, batch_deg(b));
+    if (!batch_tuning_compiled(s->m.hpn, b->NW, b->CAP))
+        return set_err(SKS_ERR_UNSUPPORTED, "GLL degree %d needs a batch tuning of 4 warps and register cap 0 or 1", s->m.hpn);
     cudaSetDevice(b->device);
     const sks_model& m = s->m;
     if (!s->seis_full) {
@@ -530,6 +568,8 @@ extern "C" int sks_batch_set_tuning(sks_batch* b, const sks_tuning_t* t)
     if (t->band_rows < 1) return set_err(SKS_ERR_ARG, "band_rows=%d must be positive", t->band_rows);
     if (t->waves != 0) return set_err(SKS_ERR_ARG, "a batch uses plain bands (waves=0)");
     if (t->pipeline != 0 && t->pipeline != 1) return set_err(SKS_ERR_ARG, "pipeline=%d: 0 or 1", t->pipeline);
+    if (!batch_tuning_compiled(batch_deg(b), t->warps_per_block, t->register_cap))
+        return set_err(SKS_ERR_UNSUPPORTED, "GLL degree %d runs with 4 warps per CTA and register cap 0 or 1", batch_deg(b));
     if (b->running) return set_err(SKS_ERR_STATE, "the batch is running");
     cudaSetDevice(b->device);
     cudaStreamSynchronize(b->stream);
@@ -594,6 +634,7 @@ extern "C" int sks_batch_autotune(sks_batch* b, int32_t steps, sks_tuning_t* bes
         for (int zs = 0; zs < 2 && !rc; zs++)
             for (int cap = 0; cap < 3 && !rc; cap++)
                 for (int hz : hzs) {
+                    if (!batch_tuning_compiled(batch_deg(b), nw, cap)) continue;
                     sks_tuning_t t = {nw, hz, zs, cap, 0, 0, 0.f, pipe};
                     if ((rc = sks_batch_set_tuning(b, &t))) break;
                     rc = b->precision == SKS_FP64 ? build_tables<double>(b) : build_tables<float>(b);

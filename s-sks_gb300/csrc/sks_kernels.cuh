@@ -1011,7 +1011,25 @@ int batch_occupancy_f64(const StepVariant& v, bool aniso);
 // resident CTAs per SM of a variant (cudaOccupancyMaxActiveBlocksPerMultiprocessor)
 int step_occupancy_f32(const StepVariant& v, bool aniso);
 int step_occupancy_f64(const StepVariant& v, bool aniso);
-// GLL degree 5 (single solves; 4 warps, register cap 0 or 1)
+// GLL degree 5 (4 warps, register cap 0 or 1)
+int batch_occupancy_f32_d5(const StepVariant& v, bool aniso);
+cudaError_t launch_batch_f32_d5(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                                const BatchMember<float>* mem, const BatchState* state, const int4* items,
+                                const BatchHeader* hdr, int j, const Coef<float, 5>& k);
+int batch_pipe_occupancy_f32_d5(const StepVariant& v, bool aniso);
+cudaError_t launch_batch_pipe_f32_d5(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                                     const BatchMember<float>* mem, const BatchState* state, const int4* items,
+                                     const BatchHeader* hdr, int nsteps, const BatchPipeCtl& ctl,
+                                     const Coef<float, 5>& k);
+int batch_occupancy_f64_d5(const StepVariant& v, bool aniso);
+cudaError_t launch_batch_f64_d5(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                                const BatchMember<double>* mem, const BatchState* state, const int4* items,
+                                const BatchHeader* hdr, int j, const Coef<double, 5>& k);
+int batch_pipe_occupancy_f64_d5(const StepVariant& v, bool aniso);
+cudaError_t launch_batch_pipe_f64_d5(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
+                                     const BatchMember<double>* mem, const BatchState* state, const int4* items,
+                                     const BatchHeader* hdr, int nsteps, const BatchPipeCtl& ctl,
+                                     const Coef<double, 5>& k);
 int step_occupancy_f32_d5(const StepVariant& v, bool aniso);
 cudaError_t launch_step_f32_d5(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,
                                const Field<float>& F, const Geo<float>& G, const Coef<float, 5>& k);

@@ -208,14 +208,26 @@ void admit(sks_server* v, const bool idle[2])
         int64_t room = v->budget - v->in_use;
         int64_t pts[2] = {v->active_points[0], v->active_points[1]};
         bool blocked[2] = {!idle[0], !idle[1]};
+        // a form's batch runs one GLL degree: a request of another degree
+        // waits (in order) until the form's running requests have left
+        int deg[2] = {0, 0};
+        for (int f = 0; f < 2; f++)
+            if (!v->active[f].empty()) deg[f] = v->active[f][0]->s->m.hpn;
         for (auto it = v->queue.begin(); it != v->queue.end() && !(blocked[0] && blocked[1]);) {
             Request* r = *it;
             const int f = r->precision;
             if (blocked[f]) { ++it; continue; }
+            const int rd = r->su ? r->su->m.hpn : 0;
+            if (deg[f] && rd && rd != deg[f]) {
+                blocked[f] = true;
+                ++it;
+                continue;
+            }
             const bool fits_work = pts[f] == 0 || pts[f] + r->points <= v->max_points[f];
             if (r->est_bytes <= room && fits_work) {
                 room -= r->est_bytes;
                 pts[f] += r->points;
+                if (rd) deg[f] = rd;
                 take.push_back(r);
                 it = v->queue.erase(it);
                 continue;

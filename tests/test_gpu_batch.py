@@ -171,3 +171,44 @@ def test_batch_rejects_mixed_forms_and_double_membership(cases):
         s.set_tuning(4, 3, 0, 1, 0)
         s.close()
         s64.close()
+
+
+@pytest.mark.parametrize("prec,tuning", [(sks.FP64, (4, 3, 1, 0, 0)), (sks.FP32C, (4, 3, 0, 1, 0)),
+                                         (sks.FP32C, (4, 4, 1, 1, 1))])
+def test_degree5_batch_matches_members_alone(cases, tmp_path, prec, tuning):
+    """Members of GLL degree 5 (the reference's default hpn) in a batch equal
+    their solo runs; a batch holds one degree and degree 5's compiled tunings."""
+    dirs, nst = [], []
+    for i, (nex, nez, eh, sdt, n) in enumerate(((23, 7, 2.0, 0.008, 700), (14, 6, 2.5, 0.01, 560))):
+        d = str(tmp_path / f"d5_{i}")
+        H = nez * eh + 0.002
+        c = synth.Case(nex=nex, nez=nez, eh=eh, sdt=sdt, nst=n, layers=_layers(H, True), p=0.045, f0=1.0,
+                       sv_amp=1.0, sh_amp=0.4, hpn=5, ntrace=7, rec_dx=3.0, semmodel_full=True)
+        synth.write_case(c, d)
+        dirs.append(d)
+        nst.append(n)
+    ref = []
+    for d, n in zip(dirs, nst):
+        s = _open(d, prec)
+        s.set_tuning(*tuning[:4], 0, tuning[4])
+        ref.append(s.run(n))
+        s.close()
+    assert all(max(np.abs(x).max() for x in r) > 0.05 for r in ref)
+    with sks.Batch(prec) as b:
+        sol = [_open(d, prec) for d in dirs]
+        for s in sol:
+            b.add(s)
+        b.set_tuning(*tuning)
+        with pytest.raises(sks.SksError):
+            b.set_tuning(2, 3, 0, 1, 0)                 # not compiled for degree 5
+        other = _open(cases[0], prec)                    # degree 4
+        with pytest.raises(sks.SksError):
+            b.add(other)
+        other.close()
+        outs = b.run(max(nst))
+        for i, s in enumerate(sol):
+            for c in range(3):
+                assert np.array_equal(outs[i][c], ref[i][c]), f"member {i} component {c}"
+        for s in sol:
+            b.remove(s)
+            s.close()

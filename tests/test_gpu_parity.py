@@ -158,7 +158,7 @@ def test_taper_under_every_grid_and_in_a_batch(casedirs, prec):
 def test_degree5_tunings_bit_identical_and_refusals(casedirs, prec):
     """Degree 5 compiles 4-warp CTAs with register cap 0 or 1: every such grid
     (seams or halo rows, per-step or pipelined, balanced waves) gives the same
-    bits; other tunings and batches are refused."""
+    bits; other tunings are refused, and so is degree 6."""
     d, c, _ = casedirs["hpn5_aniso"]
     ref = None
     with chdir(d):
@@ -177,8 +177,8 @@ def test_degree5_tunings_bit_identical_and_refusals(casedirs, prec):
                     s.set_tuning(*bad)
             s.load_boundary_files()
             with sks.Batch(prec) as b:
-                with pytest.raises(sks.SksError):
-                    b.add(s)
+                b.add(s)                                # batches take degree 5 too
+                b.remove(s)
         with pytest.raises(sks.SksError):
             sks.Solver(["par=run.par", "hpn=6"], precision=prec)
 

@@ -204,3 +204,29 @@ def test_layered_requests_are_the_same_alone_and_served(tmp_path):
             assert np.array_equal(got[c], alone[i][c]), f"request {i} component {c}"
         srv.release(rid)
     srv.close()
+
+
+def test_mixed_degrees_are_served_in_turn(tmp_path):
+    """A form's batch runs one GLL degree at a time: requests of degree 4 and
+    5 arriving mixed all complete, the other degree waiting for the batch to
+    drain, and each equals its solo run."""
+    reqs = []
+    for k, hpn in enumerate((4, 5, 4, 5)):
+        d = str(tmp_path / f"deg{k}")
+        nez, eh = 8, 2.0
+        H = nez * eh + 0.002
+        c = synth.Case(nex=20 + 3 * k, nez=nez, eh=eh, sdt=0.008, nst=300 + 40 * k, layers=_layers(H, True),
+                       p=0.045, f0=1.0, sv_amp=1.0, sh_amp=0.3, hpn=hpn, ntrace=5, rec_dx=4.0, semmodel_full=True,
+                       write_records=False)
+        synth.write_case(c, d)
+        pw = (float(np.sqrt(c.layers[0].C[3, 3] / c.layers[0].rho)), c.p, c.f0, 1.0, 0.3)
+        reqs.append((d, sks.FP32C, pw, c.nst))
+    alone = [_alone(*r) for r in reqs]
+    srv, ids, _ = _serve(reqs, 0, arrivals=[0, 0, 1, 1])
+    for i, rid in ids.items():
+        assert srv.info(rid)["state"] == sks.REQ_DONE, (i, srv.info(rid))
+        got = srv.result(rid)
+        for c in range(3):
+            assert np.array_equal(got[c], alone[i][c]), f"request {i} component {c}"
+        srv.release(rid)
+    srv.close()
