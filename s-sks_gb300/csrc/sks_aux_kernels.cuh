@@ -101,21 +101,35 @@ __device__ __forceinline__ double series_at(const double* __restrict__ f, int64_
     return wm * f[im] + w0 * f[i0] + w1 * f[i1] + w2 * f[i2];
 }
 
-// Record r, value c from the upgoing P, SV and SH series a layered stack
-// leaves in the bottom medium (vp0, vs0): each series at t - p x - eta_m z.
-// Displacement: P (p vp0, eta_p vp0), SV (eta_s vs0, -p vs0), SH u_y.
-__device__ __forceinline__ float layered_record(const RecSource& g, int fam, int r, int c)
+// The upgoing P, SV and SH series a layered stack leaves in the bottom medium
+// (vp0, vs0), each at t - p x - eta_m z: displacement P (p vp0, eta_p vp0),
+// SV (eta_s vs0, -p vs0), SH u_y; the w values hold -u_z.  Per line value the
+// two delays and the P and S coefficients are tabulated once (k_layered_line).
+static __global__ void __launch_bounds__(256) k_layered_line(RecSource g, double* __restrict__ lt)
 {
+    const int mtotal = 2 * (g.nx + g.nz), L = mtotal + g.nx + g.nz;
     const double ep = sqrt(fmax(1.0 / (g.vp0 * g.vp0) - g.p * g.p, 0.0));
     const double es = sqrt(fmax(1.0 / (g.vs0 * g.vs0) - g.p * g.p, 0.0));
-    double x, z;
-    bool vert;
-    line_point(g, fam, c, x, z, vert);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
+        const int fam = i >= mtotal ? 1 : 0, c = fam ? i - mtotal : i;
+        double x, z;
+        bool vert;
+        line_point(g, fam, c, x, z, vert);
+        lt[i] = g.p * x + ep * z;
+        lt[L + i] = g.p * x + es * z;
+        lt[2 * L + i] = fam ? 0.0 : (vert ? -ep * g.vp0 : g.p * g.vp0);
+        lt[3 * L + i] = fam ? 1.0 : (vert ? g.p * g.vs0 : es * g.vs0);
+    }
+}
+
+__device__ __forceinline__ float layered_record(const RecSource& g, int fam, int r, int c)
+{
+    const int mtotal = 2 * (g.nx + g.nz), L = mtotal + g.nx + g.nz, i = fam ? mtotal + c : c;
     const double t = (double)r * g.dp;
-    if (fam) return (float)series_at(g.ser + 2 * g.nt, g.nt, (t - g.p * x - es * z) / g.dts);
-    const double fp = series_at(g.ser, g.nt, (t - g.p * x - ep * z) / g.dts);
-    const double fs = series_at(g.ser + g.nt, g.nt, (t - g.p * x - es * z) / g.dts);
-    return (float)(vert ? -(fp * ep * g.vp0 - fs * g.p * g.vs0) : fp * g.p * g.vp0 + fs * es * g.vs0);
+    if (fam) return (float)series_at(g.ser + 2 * g.nt, g.nt, (t - g.lt[L + i]) / g.dts);
+    const double fp = series_at(g.ser, g.nt, (t - g.lt[i]) / g.dts);
+    const double fs = series_at(g.ser + g.nt, g.nt, (t - g.lt[L + i]) / g.dts);
+    return (float)(fp * g.lt[2 * L + i] + fs * g.lt[3 * L + i]);
 }
 
 // record r, value c of family fam as the interpolation reads it

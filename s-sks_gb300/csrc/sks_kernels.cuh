@@ -82,7 +82,8 @@ struct RecSource {
     double eh, dp, p;                  // element size, record step, ray parameter
     double vs, f0, sv_amp, sh_amp;     // REC_PLANE: the half-space wave
     const double* lt;                  //   per line value (P-SV then SH): delay p x + eta z [L], amplitude [L]
-    const double* ser;                 // REC_LAYERED: mode series [3][nt], samples dts apart
+    const double* ser;                 // REC_LAYERED: mode series [3][nt], samples dts apart; lt: per line
+                                       //   value tau_p, tau_s [L] each, then the P and S coefficients [L] each
     int64_t nt;
     double dts, vp0, vs0;              //   the top medium of the stack
 };

@@ -338,7 +338,8 @@ int submit(sks_server* v, sks_setup* su, int precision, const sks_plane_wave_t* 
     }
     r->out[0] = su_out; r->out[1] = sv_out; r->out[2] = sw_out;
     int64_t rec_bytes = ((int64_t)su->m.nrec_psv * su->m.mtotal + (int64_t)su->m.nrec_sh * su->m.shtotal) * 4;
-    if (pw) rec_bytes = 0;
+    const int64_t Lline = (int64_t)su->m.mtotal + su->m.shtotal;
+    if (pw) rec_bytes = 16 * Lline;                      // the line's delays and amplitudes
     if (layers) {
         const sks_model& m = su->m;
         const double xmax = (double)(m.nx - 1) * m.h + m.eh, zmax = (double)(m.nz - 1) * m.h + m.eh;
@@ -349,7 +350,7 @@ int submit(sks_server* v, sks_setup* su, int precision, const sks_plane_wave_t* 
             sks_setup_close(su);
             return (int)nt;
         }
-        rec_bytes = 24 * nt;
+        rec_bytes = 24 * nt + 32 * Lline;                 // mode series, line delays and coefficients
     }
     r->est_bytes = estimate_bytes(su->m, precision, rec_bytes);
     r->nst = su->m.nst;

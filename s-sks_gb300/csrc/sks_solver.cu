@@ -856,10 +856,12 @@ extern "C" int sks_set_boundary_layered_wave(sks_solver* s, const sks_stack_laye
     cudaSetDevice(s->device);
     CK(cudaStreamSynchronize(s->stream));
     free_records(s);
-    if (s->ser_n != 3 * (size_t)nt) {
+    // the mode series [3][nt], then the line's delays and coefficients [4][L]
+    const size_t L = (size_t)m.mtotal + m.shtotal, need = 3 * (size_t)nt + 4 * L;
+    if (s->ser_n != need) {
         free_series(s);
-        if ((rc = dmalloc(s, &s->ser, 3 * (size_t)nt))) return rc;
-        s->ser_n = 3 * (size_t)nt;
+        if ((rc = dmalloc(s, &s->ser, need))) return rc;
+        s->ser_n = need;
     }
     CK(cudaMemcpy(s->ser, ser.data(), sizeof(double) * 3 * (size_t)nt, cudaMemcpyHostToDevice));
     RecSource g = grid_source(s, REC_LAYERED);
@@ -869,6 +871,10 @@ extern "C" int sks_set_boundary_layered_wave(sks_solver* s, const sks_stack_laye
     g.dts = dts;
     g.vp0 = layers[0].vp;
     g.vs0 = layers[0].vs;
+    k_layered_line<<<(unsigned)((L + 255) / 256), 256, 0, s->stream>>>(g, s->ser + 3 * (size_t)nt);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    g.lt = s->ser + 3 * (size_t)nt;
     s->rs = g;
     s->boundary_ready = true;
     return SKS_OK;
