@@ -47,6 +47,7 @@ def _lib(fp64: bool) -> C.CDLL:
         L.oracle_material.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.oracle_mass.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.oracle_receivers.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+        L.oracle_field.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.oracle_snapshot.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_int)]
         L.oracle_destroy.argtypes = [C.c_void_p]
         L.oracle_destroy.restype = None
@@ -91,6 +92,12 @@ class Oracle:
         off = np.zeros(max(1, self.ntrace), np.int64)
         self.L.oracle_receivers(self.h, off.ctypes.data_as(C.POINTER(C.c_longlong)))
         return off[: self.ntrace]
+
+    def field(self) -> np.ndarray:
+        """The newest displacement u^n as [nz][nx][3] float64 (x, y, z components)."""
+        out = np.zeros(self.nx * self.nz * 3)
+        self.L.oracle_field(self.h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out.reshape(self.nz, self.nx, 3)
 
     def snapshot(self, k: int):
         """(step, [nx/2][nz/2][2] float32) of snapshot k (plot_snap), or None."""

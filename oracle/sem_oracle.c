@@ -1090,6 +1090,18 @@ int oracle_snapshot(void *hv, int k, float *out, int *dims)
     return o->ist + k * o->incre;
 }
 
+/* the newest displacement u^n (after the last step run) as [nx*nz][3] = (x, y, z),
+ * for whole-wavefield comparisons at sizes where the seismograms see little */
+int oracle_field(void *hv, double *out3)
+{
+    OracleHandle *h = (OracleHandle *)hv;
+    size_t np = (size_t)h->o.nx * h->o.nz, g;
+    int c;
+    for (g = 0; g < np; g++)
+        for (c = 0; c < 3; c++) out3[3 * g + c] = (double)h->o.u[g].u[c];
+    return h->it;
+}
+
 /* per-point material as 15 coefficients + rho and the Stacey/mass arrays, for set-up checks */
 int oracle_material(void *hv, double *out16)
 {

@@ -129,6 +129,7 @@ class Case:
     psv_only: bool = False
     flat: int = 1
     write_records: bool = True     # False: no greenfile/shgreenfile (records generated on the device)
+    record_t0: int = 0             # the file's record 0 is the plane wave's record record_t0 (pulse earlier)
     extra: dict = field(default_factory=dict)
 
     @property
@@ -190,7 +191,8 @@ def write_case(case: Case, d: str, absolute: bool = False) -> dict:
     if case.write_records:
         write_plane_wave(os.path.join(d, "greenfile"), os.path.join(d, "shgreenfile"),
                          nx=nx, nz=nz, h=h, nbl=nbl, vs=vs_b, p=case.p, f0=case.f0,
-                         dp=dp, nt=nt, sv_amp=case.sv_amp, sh_amp=case.sh_amp, eh=float(eh_eff), deg=N)
+                         dp=dp, nt=nt, sv_amp=case.sv_amp, sh_amp=case.sh_amp, eh=float(eh_eff), deg=N,
+                         r_first=case.record_t0)
     name = (lambda f: os.path.join(os.path.abspath(d), f)) if absolute else (lambda f: f)
     par = {
         "greenfile": name("greenfile"), "shgreenfile": name("shgreenfile"), "raymodel": name("raymodel"),
@@ -257,10 +259,11 @@ def plane_wave_records(nx, nz, h, nbl, vs, p, f0, dp, r0, r1, sv_amp=1.0, sh_amp
 
 
 def write_plane_wave(psv_path, sh_path, *, nx, nz, h, nbl, vs, p, f0, dp, nt,
-                     sv_amp=1.0, sh_amp=0.0, chunk=1024, eh=None, deg=4):
+                     sv_amp=1.0, sh_amp=0.0, chunk=1024, eh=None, deg=4, r_first=0):
+    """Records r_first .. r_first+nt-1 of the plane wave as the files' records 0 .. nt-1."""
     with open(psv_path, "wb") as fp, open(sh_path, "wb") as fs:
-        for r0 in range(0, nt, chunk):
-            psv, sh = plane_wave_records(nx, nz, h, nbl, vs, p, f0, dp, r0, min(nt, r0 + chunk),
+        for r0 in range(r_first, r_first + nt, chunk):
+            psv, sh = plane_wave_records(nx, nz, h, nbl, vs, p, f0, dp, r0, min(r_first + nt, r0 + chunk),
                                          sv_amp, sh_amp, eh, deg)
             fp.write(psv.tobytes())
             fs.write(sh.tobytes())
@@ -286,10 +289,13 @@ def layered_aniso(H: float, crust_km=35.0, aniso_km=100.0, strength=0.04, az=45.
 
 
 def config_isotropic_psv(nst=6000) -> Case:
-    """400x200 km, 200x100 elements of 2 km, crust over mantle, SV p=0.045, 0.2 Hz."""
+    """The plain isotropic P-SV case: 400x200 km, 200x100 elements of 2 km, GLL
+    degree 4, a 35 km crust over the mantle, SV plane wave p=0.045 s/km, Ricker
+    0.2 Hz, dt 10 ms, 101 receivers every 4 km, Stacey on the sides and bottom;
+    P-SV only (the reference's `sem2d` program: no SH record file)."""
     H = 200.0
     return Case(nex=200, nez=100, eh=2.0, sdt=0.01, nst=nst, layers=layered_two(H),
-                p=0.045, f0=0.2, ntrace=101, rec_x0=0.0, rec_dx=4.0)
+                p=0.045, f0=0.2, ntrace=101, rec_x0=0.0, rec_dx=4.0, psv_only=True)
 
 
 def config_aniso_3c(nst=24000) -> Case:
