@@ -47,7 +47,7 @@ FULL_STEPS = 24000
 # written: 124 B (FP32C), 200 B (FP64).  The kernels move less than that (the
 # material is a 2-byte index into a table and the inverse mass is rebuilt from
 # GLL weights): 74 B per point in both forms (LAYOUT_BYTES_PER_POINT).
-BYTES_PER_POINT = {"fp32c": 124, "fp64": 200}
+BYTES_PER_POINT = {"fp32c": 124, "fp64": 200, "fp64_iso": 96}
 # algorithmic flops per grid-point update of the anisotropic step (an FMA is 2
 # flops, an n-term dot product 2n-1): per element row a GLL column does, for
 # each of its 5 rows, the x and z derivatives of 3 components (54), one strain
@@ -55,7 +55,8 @@ BYTES_PER_POINT = {"fp32c": 124, "fp64": 200}
 # z-flux scaling (3) and the z-divergence into 5 rows (30): 166 x 5 = 830, an
 # element's 5 columns 4150, over its 16 unique points 259.4; plus assembly
 # (1.5) and the 3-level update (15)
-FLOPS_PER_POINT_ANISO = 276
+# isotropic: the 5x5 stress is 9 flops instead of 45, so 130 x 5 x 5 / 16 + 16.5
+FLOPS_PER_POINT = {"aniso": 276, "iso": 220}
 LAYOUT_BYTES_PER_POINT = {"fp32c": 74, "fp64": 74}
 WORKLOAD = ("anisotropic 3-component SKS solve: 800x300 elements of 1 km, GLL degree 4, "
             "3,844,401 points, 100 km hexagonal layer (4 %, azimuth 45, tilt 20), dt 5 ms, 201 receivers")
@@ -157,10 +158,23 @@ def run_fixed(d: str, precision: int, steps: int, warmup: int, gpu: int, tuning)
     return {"steps": n, "ms_per_step": ms / n, "updates_per_s": npts * n / (ms / 1e3), "tuning": t}
 
 
-def run_form(d: str, precision: int, steps: int, warmup: int, gpu: int, clocks: bool = False) -> dict:
-    """Device-resident timing of one form: autotune (state restored), W
-    warm-up steps, K timed steps (CUDA events on the solver's stream), then a
-    second pass of K steps with per-kernel event timing for the roofline."""
+REF_MAX_STEPS = 30   # the reference arm's timed steps at most (about 0.3 s each per process)
+REF_MAX_WARMUP = 5
+REPEATS = 5          # repetitions of the timed window (median reported, spread beside it)
+
+
+def _spread(rates: list) -> dict:
+    return {"median": statistics.median(rates), "min": min(rates), "max": max(rates), "repeats": len(rates)}
+
+
+def run_form(d: str, precision: int, steps: int, warmup: int, gpu: int, clocks: bool = False,
+             repeats: int = REPEATS) -> dict:
+    """Device-resident timing of one form.  Autotune (state restored), one
+    warm-up pass, then R repetitions of the same window: steps 1..K of the
+    solve (reset and the initialising step 0 before each, untimed), CUDA
+    events on the solver's stream.  The median repetition is the value.  A
+    last pass of the same window brackets every kernel launch with events (for
+    the roofline)."""
     import sks
     cwd = os.getcwd()
     os.chdir(d)
@@ -170,18 +184,24 @@ def run_form(d: str, precision: int, steps: int, warmup: int, gpu: int, clocks: 
         info = s.info()
         lib_run_noout(s, warmup)
         tuning = s.autotune(16)
-        l0 = s.launches()
+        s.reset()
+        lib_run_noout(s, 1 + max(warmup, steps))       # warm-up pass over the window
         ck = Clocks(gpu) if clocks else None
         if ck:
             ck.__enter__()
-        n = lib_run_noout(s, steps)
+        times, launches = [], 0
+        for _ in range(repeats):
+            s.reset()
+            lib_run_noout(s, 1)
+            l0 = s.launches()
+            n = lib_run_noout(s, steps)
+            times.append(s.last_run_ms())
+            launches = s.launches() - l0
         if ck:
             ck.__exit__(None, None, None)
-        ms = s.last_run_ms()
-        launches = s.launches() - l0
-        # kernel-level pass: every launch bracketed by events
+        # kernel-level pass over the same window: every launch bracketed by events
         s.reset()
-        lib_run_noout(s, warmup)
+        lib_run_noout(s, 1)
         s.enable_kernel_timing(True)
         lib_run_noout(s, steps)
         kt = s.kernel_timing()
@@ -189,8 +209,10 @@ def run_form(d: str, precision: int, steps: int, warmup: int, gpu: int, clocks: 
     finally:
         os.chdir(cwd)
     npts = info["nx"] * info["nz"]
+    ms = statistics.median(times)
     res = {"steps": n, "ms": ms, "ms_per_step": ms / n, "points": npts, "tuning": tuning,
-           "updates_per_s": npts * n / (ms / 1e3), "launches": launches, "kernels": kt, "info": info}
+           "updates_per_s": npts * n / (ms / 1e3), "launches": launches, "kernels": kt, "info": info,
+           "spread": _spread([npts * n / (t / 1e3) for t in times])}
     if ck:
         res["clocks"] = ck.summary()
     return res
@@ -205,16 +227,21 @@ def lib_run_noout(s, steps: int) -> int:
     return n
 
 
-def run_e2e(d: str, precision: int, steps: int, warmup: int, gpu: int, tuning=None) -> dict:
-    """Through the C ABI with host buffers: upload the run's boundary records from
-    pinned memory, run, read the seismograms back; wall-clock timed.  The
-    tuning found for the device-resident run is reused (set before timing)."""
+def run_e2e(d: str, precision: int, steps: int, warmup: int, gpu: int, tuning=None,
+            repeats: int = REPEATS) -> dict:
+    """Through the C ABI with host buffers, over the window of run_form from
+    the solve's start: upload the boundary records from pinned memory, run
+    steps 0..K (step 0 initialises; K updates are counted), read the
+    seismograms back; wall-clock timed, one warm-up pass, then R repetitions
+    (median reported).  The solver is opened (host set-up, device allocation)
+    before the timed region.  The tuning found for the device-resident run is
+    reused."""
     import ctypes as C
     import sks
     cwd = os.getcwd()
     os.chdir(d)
     try:
-        s = sks.Solver(["par=run.par", f"nst={steps}"], precision=precision, device=gpu)
+        s = sks.Solver(["par=run.par", f"nst={steps + 1}"], precision=precision, device=gpu)
         if tuning:
             s.set_tuning(tuning["warps_per_block"], tuning["band_rows"], tuning["zseam"], tuning["register_cap"],
                          tuning["waves"], tuning.get("pipeline", 0))
@@ -224,26 +251,94 @@ def run_e2e(d: str, precision: int, steps: int, warmup: int, gpu: int, tuning=No
         psv.numpy()[:] = np.fromfile("greenfile", np.float32, count=npsv)
         sh.numpy()[:] = np.fromfile("shgreenfile", np.float32, count=nsh)
         nt = info["ntrace"]
-        outs = [_pinned(steps * nt) for _ in range(3)]
+        outs = [_pinned((steps + 1) * nt) for _ in range(3)]
         fp = C.POINTER(C.c_float)
         ptr = lambda t: C.cast(t.data_ptr(), fp)
-        # warm-up pass (same calls), then the timed pass
-        for timed in (False, True):
+        walls = []
+        for rep in range(repeats + 1):                 # rep 0: warm-up
             s.reset()
             t0 = time.perf_counter()
             rc = sks.lib().sks_set_boundary(s.h, ptr(psv), info["nrec_psv"], ptr(sh), info["nrec_sh"])
             if rc < 0:
                 raise sks.SksError(rc, sks.lib().sks_last_error().decode())
-            n = sks.lib().sks_run(s.h, steps, ptr(outs[0]), ptr(outs[1]), ptr(outs[2]))
+            n = sks.lib().sks_run(s.h, steps + 1, ptr(outs[0]), ptr(outs[1]), ptr(outs[2]))
             if n < 0:
                 raise sks.SksError(n, sks.lib().sks_last_error().decode())
-            wall = time.perf_counter() - t0
+            n -= 1                                     # updates: step 0 only initialises
+            if rep:
+                walls.append(time.perf_counter() - t0)
         s.close()
     finally:
         os.chdir(cwd)
     npts = info["nx"] * info["nz"]
+    wall = statistics.median(walls)
     return {"value": npts * n / wall, "wall_s": wall, "h2d_bytes_per_step": (npsv + nsh) * 4 // max(1, n),
-            "d2h_bytes_per_step": 3 * nt * 4, "steps": n}
+            "d2h_bytes_per_step": 3 * nt * 4, "steps": n, "spread": _spread([npts * n / w for w in walls])}
+
+
+def run_plain(gpu: int, steps: int, warmup: int) -> dict:
+    """The plain isotropic P-SV case: 400 x 200 km as 200 x 100 elements of
+    2 km (801 x 401 = 321,201 points), GLL degree 4, crust over mantle, SV
+    plane wave p = 0.045 s/km, Ricker 0.2 Hz, dt 10 ms, 6000 steps, 101
+    receivers, P-SV only.  The FP64 form device-resident over a window of K
+    steps after autotuning (with its FP64 compute and HBM rooflines), then the
+    whole 6000-step solve of each form through the C ABI from the par file:
+    boundary files read, run, seismograms back in host memory, wall-clock;
+    solves per hour of each form and their ratio."""
+    import sks
+    import synth
+    c = synth.config_isotropic_psv()
+    d = tempfile.mkdtemp(prefix="sks_plain_")
+    out = {}
+    try:
+        synth.write_case(c, d)
+        cwd = os.getcwd()
+        os.chdir(d)
+        try:
+            for name, prec in (("fp64", sks.FP64), ("fp32c", sks.FP32C)):
+                s = sks.Solver(["par=run.par"], precision=prec, device=gpu)
+                s.load_boundary_files()
+                info = s.info()
+                lib_run_noout(s, warmup)
+                tun = s.autotune(16)
+                s.reset()
+                lib_run_noout(s, 1 + max(warmup, steps))
+                times = []
+                for _ in range(REPEATS):
+                    s.reset()
+                    lib_run_noout(s, 1)
+                    n = lib_run_noout(s, steps)
+                    times.append(s.last_run_ms())
+                s.reset()
+                lib_run_noout(s, 1)
+                s.enable_kernel_timing(True)
+                lib_run_noout(s, steps)
+                kt = s.kernel_timing()
+                s.enable_kernel_timing(False)
+                # the whole solve: records from the files, seismograms to host memory
+                s.reset()
+                t0 = time.perf_counter()
+                s.load_boundary_files()
+                seis = s.run(c.nst)
+                wall = time.perf_counter() - t0
+                s.close()
+                npts = info["nx"] * info["nz"]
+                ms = statistics.median(times)
+                km = kt["element"][0] / n
+                out[name] = {"updates_per_s": npts * n / (ms / 1e3), "ms_per_step": ms / n, "timed_steps": n,
+                             "spread": _spread([npts * n / (t / 1e3) for t in times]), "tuning": tun,
+                             "kernel_ms_per_step": km, "whole_solve_s": wall,
+                             "whole_solve_updates_per_s": npts * c.nst / wall,
+                             "solves_per_hour": 3600.0 / wall,
+                             "seismograms_finite": bool(all(np.isfinite(x).all() for x in seis))}
+        finally:
+            os.chdir(cwd)
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    out["points"] = npts
+    out["steps"] = c.nst
+    out["solves_per_hour_ratio_fp32c_over_fp64"] = out["fp32c"]["solves_per_hour"] / out["fp64"]["solves_per_hour"]
+    return out
 
 
 # ---------------------------------------------------------------- CPU side
@@ -480,16 +575,95 @@ def run_accuracy(gpu: int, nst: int = FULL_STEPS) -> dict:
             w = splitting.sks_window(a[0][:, r], c.sdt, 5.0)
             e64 = splitting.splitting(a[0][:, r], a[1][:, r], c.sdt, w, max_delay=3.0, dphi=0.25)
             e32 = splitting.splitting(b[0][:, r], b[1][:, r], c.sdt, w, max_delay=3.0, dphi=0.25)
-            sp.append({"receiver": r, "x_km": c.rec_x0 + r * c.rec_dx, "fp64": e64, "fp32c": e32,
+            sp.append({"receiver": r, "x_km": c.rec_x0 + r * c.rec_dx,
+                       "fp64_phi_deg": e64["phi_deg"], "fp64_delay_s": e64["delay_s"],
                        "dphi_deg": abs(e32["phi_deg"] - e64["phi_deg"]),
                        "ddelay_s": abs(e32["delay_s"] - e64["delay_s"])})
         out.update({"splitting": sp, "max_dphi_deg": max(x["dphi_deg"] for x in sp),
                     "max_ddelay_s": max(x["ddelay_s"] for x in sp), "steps": nst,
-                    "reference_form": "FP64 form (matches the FP64 oracle to rel L2 <= 1e-10 on the parity cases)",
+                    "reference_form": "the GPU FP64 form over the whole solve (the oracle would need hours here); "
+                                      "against the FP64 oracle itself: oracle_window",
                     "splitting_grid": {"dphi_deg": 0.25, "ddelay_s": c.sdt}})
     finally:
         shutil.rmtree(d, ignore_errors=True)
     return out
+
+
+WINDOW_STEPS = 240        # the anisotropic mesh's oracle window: 1.2 s
+WINDOW_RECORD_T0 = 400    # its records start 2 s into the plane wave, so the pulse enters inside it
+STATE_HDR = 88            # bytes of a saved solver state's header; int32 `cur` at byte 32
+
+
+def _oracle_window_worker(d: str, steps: int, out: str) -> None:
+    sys.path.insert(0, ROOT)
+    from oracle.oracle import Oracle
+    o = Oracle([f"par={os.path.join(d, 'run.par')}"], fp64=True)
+    o.run(steps)
+    np.save(out, o.field())
+    o.close()
+
+
+def _state_field(state, info, precision: int) -> np.ndarray:
+    """u^n of a saved solver state as [nz][nx][3] float64 (x, y, z)."""
+    import sks
+    n = info["nx"] * info["nz"]
+    cur = int(np.frombuffer(state[32:36].tobytes(), np.int32)[0])
+    dt = np.float64 if precision == sks.FP64 else np.float32
+    el = np.dtype(dt).itemsize
+    o = STATE_HDR + cur * 3 * n * el
+    buf = np.frombuffer(state[o:o + 3 * n * el].tobytes(), dt).astype(np.float64)
+    pairs = buf[:2 * n].reshape(n, 2)
+    return np.stack([pairs[:, 0], buf[2 * n:3 * n], pairs[:, 1]], axis=1).reshape(info["nz"], info["nx"], 3)
+
+
+class OracleWindow:
+    """Accuracy against the FP64 oracle on the anisotropic 3-component mesh
+    itself (3,844,401 points), over a window of 240 steps whose boundary
+    records start 2 s into the plane wave: the oracle (a checker) runs in a
+    spawned process on one host core while the GPU legs run; compare() solves
+    the same window in both GPU forms and returns the relative L2 of the whole
+    displacement field u^n at the window's end."""
+
+    def __init__(self):
+        import synth
+        self.d = tempfile.mkdtemp(prefix="sks_window_")
+        c = synth.config_aniso_3c(nst=WINDOW_STEPS)
+        c.record_t0 = WINDOW_RECORD_T0
+        synth.write_case(c, self.d, absolute=True)
+        self.out = os.path.join(self.d, "oracle_field.npy")
+        self.t0 = time.perf_counter()
+        self.proc = mp.get_context("spawn").Process(target=_oracle_window_worker,
+                                                    args=(self.d, WINDOW_STEPS, self.out))
+        self.proc.start()
+
+    def compare(self, gpu: int) -> dict:
+        import sks
+        try:
+            fields = {}
+            for name, prec in (("fp64", sks.FP64), ("fp32c", sks.FP32C)):
+                with sks.Solver([f"par={os.path.join(self.d, 'run.par')}"], precision=prec, device=gpu) as s:
+                    s.load_boundary_files()
+                    lib_run_noout(s, WINDOW_STEPS)
+                    fields[name] = _state_field(s.save_state(), s.info(), prec)
+            self.proc.join()
+            wall = time.perf_counter() - self.t0
+            if self.proc.exitcode != 0 or not os.path.exists(self.out):
+                return {"error": f"oracle process exit code {self.proc.exitcode}"}
+            ref = np.load(self.out)
+            nr = np.linalg.norm(ref)
+            out = {"steps": WINDOW_STEPS, "points": int(ref.shape[0] * ref.shape[1]),
+                   "records_from_s": WINDOW_RECORD_T0 * 0.005, "oracle_wall_s": wall,
+                   "what": "relative L2 of the 3-component displacement field u^n after the window, against "
+                           "the FP64 oracle (C restatement of the reference's loop, FP64 build)"}
+            for name, f in fields.items():
+                out[name] = {"field_rel_l2": float(np.linalg.norm(f - ref) / nr),
+                             "per_component": [float(np.linalg.norm(f[..., k] - ref[..., k]) /
+                                                     max(np.linalg.norm(ref[..., k]), 1e-300)) for k in range(3)]}
+            return out
+        finally:
+            if self.proc.is_alive():
+                self.proc.terminate()
+            shutil.rmtree(self.d, ignore_errors=True)
 
 
 def run_large(gpu: int, steps: int, warmup: int) -> dict:
@@ -539,12 +713,12 @@ def run_large(gpu: int, steps: int, warmup: int) -> dict:
 
 
 def _cpu_worker(args):
-    d, nsteps, fp64 = args
+    d, nsteps, fp64, warm = args
     sys.path.insert(0, ROOT)
     from oracle.oracle import Oracle
     os.chdir(d)
     o = Oracle(["par=run.par"], fp64=fp64)
-    o.run(1)                      # step 0 (initialisation only)
+    o.run(1 + warm)               # step 0 (initialisation only), then the warm-up steps
     t0 = time.perf_counter()
     o.run(nsteps)
     dt = time.perf_counter() - t0
@@ -553,20 +727,23 @@ def _cpu_worker(args):
     return pts * nsteps, dt
 
 
-def cpu_rate(d: str, nsteps: int, procs: int) -> dict:
-    """The oracle's float build (the reference's arithmetic restated) on the host
-    cores: `procs` independent single-threaded solves at once."""
+def cpu_rate(d: str, nsteps: int, procs: int, warm: int = 0) -> dict:
+    """The oracle's float build (the reference's arithmetic restated, bit-exact
+    to the reference binary) on the host cores: `procs` independent
+    single-threaded solves at once, each `warm` untimed steps then `nsteps`
+    timed ones."""
     from oracle import oracle as orc
     orc.build(None)
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs) as pool:
         t0 = time.perf_counter()
-        res = pool.map(_cpu_worker, [(d, nsteps, False)] * procs)
+        res = pool.map(_cpu_worker, [(d, nsteps, False, warm)] * procs)
         wall = time.perf_counter() - t0
     pts = sum(r[0] for r in res)
     per_proc = [r[0] / r[1] for r in res]
+    step_s = [r[1] / nsteps for r in res]
     return {"value": sum(per_proc), "per_process": statistics.median(per_proc), "wall_s": wall, "procs": procs,
-            "pts": pts}
+            "pts": pts, "s_per_step_median": statistics.median(step_s), "s_per_step_max": max(step_s)}
 
 
 # ---------------------------------------------------------------- main
@@ -614,6 +791,7 @@ def main() -> None:
     ap.add_argument("--tuning", default="", help="W,B,Z,C[,V[,P]]: warps per CTA, band rows, band seams, register cap, "
                     "waves, pipelined chunks")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-instance workload")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain isotropic P-SV FP64 workload")
     ap.add_argument("--batch-only", action="store_true", help="only the batched workload (one JSON object)")
     ap.add_argument("--batch-instances", type=int, default=64,
                     help="with --batch-only: the first N instances of the seeded batch (profiling a smaller batch)")
@@ -636,27 +814,35 @@ def main() -> None:
 
     if a.impl == "reference":
         # the reference's CPU path (float restatement, bit-exact to the
-        # reference binary) on every host core, rank 0 only
+        # reference binary) on every host core, rank 0 only.  A step here is
+        # one time step of the full mesh in each of the host's cores'
+        # independent solves; the run is capped so it ends within a minute.
         if rank != 0:
             return
         ncpu = os.cpu_count() or 1
+        ksteps = max(1, min(a.steps, REF_MAX_STEPS))
+        kwarm = max(1, min(a.warmup, REF_MAX_WARMUP))
         d = tempfile.mkdtemp(prefix="sks_ref_")
         try:
-            make_case(d, 8)
-            nsteps = max(1, min(a.cpu_steps, 3))
-            r = cpu_rate(d, nsteps, ncpu)
+            make_case(d, ksteps + kwarm + 8)
+            r = cpu_rate(d, ksteps, ncpu, kwarm)
         finally:
             shutil.rmtree(d, ignore_errors=True)
         v = r["value"]
-        npts = 3201 * 1201
         line = {"impl": "reference", "metric": "GLL-pt updates/s", "value": v, "unit": "GLL-pt updates/s",
-                "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": npts / v * 1e3,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic", "config": {"workload": WORKLOAD, "form": "reference float arithmetic"},
+                "n_gpus": a.gpus, "steps": ksteps, "warmup": kwarm,
+                "ms_per_step": r["s_per_step_median"] * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "form": "reference float arithmetic",
+                           "step": f"one time step of the 3,844,401-point mesh in each of {ncpu} independent "
+                                   "single-threaded solves running at once",
+                           "steps_requested": a.steps, "warmup_requested": a.warmup},
                 "cpu_baseline": {"value": v, "unit": "GLL-pt updates/s", "cores": ncpu, "kind": "port",
-                                 "sample": f"{nsteps} time steps of the full mesh in each of {ncpu} "
-                                           "independent single-threaded processes (oracle float build, "
-                                           "bit-exact to the reference binary)"},
+                                 "sample": f"{kwarm} untimed then {ksteps} timed time steps of the full mesh in "
+                                           f"each of {ncpu} independent single-threaded processes (oracle float "
+                                           "build, bit-exact to the reference binary; the reference sources are "
+                                           "not on the GPU host, so its binary cannot be built there)",
+                                 "per_process": r["per_process"], "s_per_step_max": r["s_per_step_max"]},
                 "e2e": {"value": v, "unit": "GLL-pt updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -691,6 +877,12 @@ def main() -> None:
             print(json.dumps({"serve": run_serve(gpu, float(r), a.serve_requests, fp64_frac=a.serve_fp64_fraction,
                                                  tuning32=t32)}), flush=True)
         return
+    orc_win = None
+    if rank == 0 and world == 1 and not a.no_cpu and not a.no_accuracy:
+        # part of the CPU-baseline leg: the FP64 oracle over the anisotropic
+        # mesh's window runs on a host core while the GPU legs run, as the
+        # checker of both forms (its result is only compared, never timed)
+        orc_win = OracleWindow()
     d = tempfile.mkdtemp(prefix="sks_bench_")
     try:
         nst = a.warmup + a.steps + 8
@@ -712,6 +904,9 @@ def main() -> None:
             cpu = cpu_rate(d, a.cpu_steps, 1)
     finally:
         shutil.rmtree(d, ignore_errors=True)
+    plain = None
+    if not a.no_plain:
+        plain = run_plain(gpu, min(a.steps, 600), a.warmup)
     batch = None
     if not a.no_batch:
         batch = run_batch(gpu, min(a.steps, 200), a.warmup)
@@ -724,6 +919,9 @@ def main() -> None:
     large = None
     if not a.no_large:
         large = run_large(gpu, min(a.steps, 300), a.warmup)
+    oracle_check = orc_win.compare(gpu) if orc_win else None
+    if accuracy and oracle_check:
+        accuracy["oracle_window"] = oracle_check
     if rank != 0:
         return
     npts = r32["points"]
@@ -745,13 +943,17 @@ def main() -> None:
     km64, kc64 = r64["kernels"]["element"]
     t64 = km64 / max(1, r64["steps"]) / 1e3
     total_k = sum(v[0] for v in r32["kernels"].values())
+    fp64_roof = npts * FLOPS_PER_POINT["aniso"] / t64 / 1e12
     line = {
         "metric": "GLL-pt updates/s", "value": value, "unit": "GLL-pt updates/s", "n_gpus": world,
         "steps": r32["steps"], "warmup": a.warmup, "ms_per_step": ms32 / r32["steps"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "form": "FP32 wavefield, Kahan-compensated leapfrog",
-                   "points_updated_per_step": npts,
-                   "points": npts, "l2": "working set > L2 (no flush)", "parallelism": f"replicas x{world}"},
+                   "points_updated_per_step": npts, "points": npts, "l2": "working set > L2 (no flush)",
+                   "window": f"steps 1..{r32['steps']} of the solve, timed {REPEATS} times from a reset and "
+                             "step 0 (median; spread in value_spread), after autotuning and a warm-up pass",
+                   "parallelism": f"replicas x{world}"},
+        "value_spread": r32["spread"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "k_step (element force + assembly + update + receivers + injection)",
@@ -760,17 +962,19 @@ def main() -> None:
                      "layout_bytes_per_point": LAYOUT_BYTES_PER_POINT["fp32c"],
                      "achieved_layout_bytes": achieved_layout, "frac_layout_bytes": achieved_layout / peak},
         "e2e": {"value": world * npts * e2e["steps"] / e2e_wall, "unit": "GLL-pt updates/s",
-                "h2d_bytes_per_step": e2e["h2d_bytes_per_step"], "d2h_bytes_per_step": e2e["d2h_bytes_per_step"]},
+                "h2d_bytes_per_step": e2e["h2d_bytes_per_step"], "d2h_bytes_per_step": e2e["d2h_bytes_per_step"],
+                "window": "steps 0..K from the solve's start, K updates counted (value's window plus the "
+                          "initialising step 0); records uploaded from pinned memory and seismograms read back "
+                          "inside the timed region; solver opened before it", "spread": e2e["spread"]},
         "gpu_launches": r32["launches"],
         "clocks": r32.get("clocks"),
         "fp64": {"value": v64, "unit": "GLL-pt updates/s", "ms_per_step": ms64 / r64["steps"],
-                 "steps": r64["steps"],
-                 "roofline": {"bound": "fp64 pipe", "achieved": npts * FLOPS_PER_POINT_ANISO / t64 / 1e12,
+                 "steps": r64["steps"], "spread": r64["spread"],
+                 "roofline": {"bound": "fp64 pipe", "achieved": fp64_roof,
                               "peak": fma_peaks["fp64"], "unit": "TFLOP/s",
-                              "frac": (npts * FLOPS_PER_POINT_ANISO / t64 / 1e12) / fma_peaks["fp64"]
-                              if fma_peaks["fp64"] else None,
+                              "frac": fp64_roof / fma_peaks["fp64"] if fma_peaks["fp64"] else None,
                               "peak_kind": "measured: FMA-chain probe of the FP64 pipe (sks_probe_fma_peak)",
-                              "flops_per_point": FLOPS_PER_POINT_ANISO, "kernel_ms_per_step": t64 * 1e3,
+                              "flops_per_point": FLOPS_PER_POINT["aniso"], "kernel_ms_per_step": t64 * 1e3,
                               "achieved_gbs": npts * BYTES_PER_POINT["fp64"] / t64 / 1e9,
                               "bytes_per_point": BYTES_PER_POINT["fp64"], "peak_gbs": peak,
                               "fp32_fma_peak_tflops": fma_peaks["fp32"]}},
@@ -780,6 +984,19 @@ def main() -> None:
         "kernel_ms": {k: v[0] for k, v in r32["kernels"].items()},
         "tuning": {"fp32c": r32["tuning"], "fp64": r64["tuning"]},
     }
+    if plain:
+        p64 = plain["fp64"]
+        t = p64["kernel_ms_per_step"] / 1e3
+        tf = plain["points"] * FLOPS_PER_POINT["iso"] / t / 1e12
+        p64["roofline"] = {"bound": "fp64 pipe", "achieved": tf, "peak": fma_peaks["fp64"], "unit": "TFLOP/s",
+                           "frac": tf / fma_peaks["fp64"] if fma_peaks["fp64"] else None,
+                           "flops_per_point": FLOPS_PER_POINT["iso"],
+                           "achieved_gbs": plain["points"] * BYTES_PER_POINT["fp64_iso"] / t / 1e9,
+                           "bytes_per_point": BYTES_PER_POINT["fp64_iso"], "peak_gbs": peak,
+                           "frac_hbm": plain["points"] * BYTES_PER_POINT["fp64_iso"] / t / 1e9 / peak}
+        plain["workload"] = ("plain isotropic P-SV case: 200x100 elements of 2 km, 321,201 points, crust over mantle, "
+                             "SV p 0.045 s/km, Ricker 0.2 Hz, dt 10 ms, 6000 steps, 101 receivers, P-SV only")
+        line["plain_fp64"] = plain
     if batch:
         pb = batch["points_per_step"] * BYTES_PER_POINT["fp32c"] / (batch["fp32c"]["ms_per_batch_step"] / 1e3) / 1e9
         batch["workload"] = ("64 seeded instances: nex U{200..1000}, nez U{100..400}, element 1-2 km, GLL degree 4, "
@@ -807,7 +1024,52 @@ def main() -> None:
         line["cpu_baseline"] = {"value": cpu["value"], "unit": "GLL-pt updates/s", "cores": 1, "kind": "port",
                                 "sample": f"{a.cpu_steps} time steps of the same mesh, one thread, oracle float "
                                           "build (bit-exact to the reference binary)"}
+        if oracle_check:
+            line["cpu_baseline"]["oracle_check"] = "accuracy.oracle_window: both GPU forms against the FP64 oracle"
+    line["summary"] = _summary(line)
     print(json.dumps(line))
+
+
+def _summary(line: dict) -> dict:
+    """The workloads' headline figures in a few hundred bytes, last in the line."""
+    r = lambda x, n=4: None if x is None else float(f"{x:.{n}g}")
+    out = {"c1_fp32c": {"value": r(line["value"]), "frac": r(line["roofline"]["frac"], 3),
+                        "frac_layout_bytes": r(line["roofline"]["frac_layout_bytes"], 3),
+                        "e2e": r(line["e2e"]["value"]), "solves_per_hour": r(line["solves_per_hour"]["fp32c"])},
+           "c1_fp64": {"value": r(line["fp64"]["value"]), "frac_fp64_pipe": r(line["fp64"]["roofline"]["frac"], 3),
+                       "solves_per_hour": r(line["solves_per_hour"]["fp64"])}}
+    out["c1_solves_per_hour_ratio"] = r(line["solves_per_hour"]["fp32c"] / line["solves_per_hour"]["fp64"], 3)
+    p = line.get("plain_fp64")
+    if p:
+        out["c0_plain"] = {"fp64_value": r(p["fp64"]["updates_per_s"]),
+                           "fp64_frac_fp64_pipe": r(p["fp64"]["roofline"]["frac"], 3),
+                           "fp64_solves_per_hour": r(p["fp64"]["solves_per_hour"]),
+                           "fp32c_solves_per_hour": r(p["fp32c"]["solves_per_hour"]),
+                           "ratio": r(p["solves_per_hour_ratio_fp32c_over_fp64"], 3)}
+    b = line.get("batch")
+    if b:
+        out["c2_batch"] = {"fp32c_value": r(b["fp32c"]["updates_per_s"]), "frac": r(b["fp32c"]["roofline"]["frac"], 3),
+                           "solves_per_hour": r(b["fp32c"]["full_solves"]["solves_per_hour"]),
+                           "fp64_value": r(b["fp64"]["updates_per_s"]),
+                           "ratio_fp32c_over_fp64": r(b["solves_per_hour_ratio_fp32c_full_over_fp64"], 3)}
+    sv = line.get("serve")
+    if sv:
+        lat = sv["latency_s"]
+        out["c3_serve"] = {"rate_per_s": sv["rate_per_s"], "completed": sv["completed"],
+                           "p50_s": r(lat["p50"], 3), "p99_s": r(lat["p99"], 3),
+                           "fp32c_p50_s": r(lat["fp32c"]["p50_s"], 3), "fp32c_p99_s": r(lat["fp32c"]["p99_s"], 3),
+                           "solves_per_hour": r(sv["solves_per_hour"]), "value": r(sv["updates_per_s"])}
+    acc = line.get("accuracy")
+    if acc:
+        out["c1_accuracy"] = {"fp32c_vs_fp64_rel_l2": {k: r(v, 3) for k, v in acc["rel_l2"].items()},
+                              "max_dphi_deg": acc["max_dphi_deg"], "max_ddelay_s": acc["max_ddelay_s"]}
+        ow = acc.get("oracle_window")
+        if ow:
+            out["c1_accuracy"]["vs_fp64_oracle_window"] = {k: r(ow[k]["field_rel_l2"], 3) for k in ("fp64", "fp32c")}
+    lg = line.get("large")
+    if lg:
+        out["c4_large"] = {"value": r(lg["updates_per_s"]), "frac": r(lg["roofline"]["frac"], 3)}
+    return out
 
 
 def _traffic_per_launch(points: int):

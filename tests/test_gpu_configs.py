@@ -20,6 +20,7 @@ The oracle needs minutes of CPU at these sizes; both oracle runs start in
 threads when the module's fixture is built (ctypes releases the GIL), so they
 overlap the GPU solves.
 """
+import os
 import threading
 
 import numpy as np
@@ -28,7 +29,7 @@ import pytest
 import sks
 import synth
 from oracle.oracle import Oracle
-from util import chdir, rel_l2, seis_err
+from util import rel_l2, seis_err
 
 pytestmark = pytest.mark.gpu
 
@@ -51,8 +52,8 @@ class _Background:
 
     def _run(self):
         try:
-            with chdir(self.d):
-                o = Oracle(["par=run.par"], fp64=True)
+            # absolute paths: the working directory is the process's, shared with the tests
+            o = Oracle([f"par={os.path.join(self.d, 'run.par')}"], fp64=True)
             seis = o.run(self.nsteps)
             field = o.field() if self.want_field else None
             o.close()
@@ -71,18 +72,18 @@ class _Background:
 def configs(tmp_path_factory):
     c0 = synth.config_isotropic_psv()
     d0 = str(tmp_path_factory.mktemp("c0_iso_psv"))
-    synth.write_case(c0, d0)
+    synth.write_case(c0, d0, absolute=True)
     c1 = synth.config_aniso_3c(nst=C1_STEPS)
     c1.record_t0 = C1_RECORD_T0
     d1 = str(tmp_path_factory.mktemp("c1_aniso_window"))
-    synth.write_case(c1, d1)
+    synth.write_case(c1, d1, absolute=True)
     return {"c0": (d0, c0, _Background(d0, c0.nst, False)),
             "c1": (d1, c1, _Background(d1, C1_STEPS, True))}
 
 
 def _gpu(d, prec, nsteps):
     """Seismograms and the final displacement [nz][nx][3] (x, y, z) of a GPU solve."""
-    with chdir(d), sks.Solver(["par=run.par"], precision=prec, device=0) as s:
+    with sks.Solver([f"par={os.path.join(d, 'run.par')}"], precision=prec, device=0) as s:
         s.load_boundary_files()
         seis = s.run(nsteps)
         info = s.info()
