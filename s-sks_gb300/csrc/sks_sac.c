@@ -71,12 +71,13 @@ int sks_sac_write(const char *path, int32_t npts, const float *data, const sks_s
     hi[I_IFTYPE] = SAC_ITIME;
     hi[I_LEVEN] = 1;
     {
-        /* kstnm: 8 characters, blank padded */
-        char k[8];
+        /* kstnm as uvw2sac fills it: a C string copy over the unset value
+         * (uvw2sac.c:381, strcpy into the "-12345  " of sac_null) -- the name,
+         * a NUL, then what is left of "-12345  "; 8 characters fill the field */
         size_t l = strlen(f->kstnm);
-        memset(k, ' ', 8);
-        memcpy(k, f->kstnm, l > 8 ? 8 : l);
-        memcpy(hc, k, 8);
+        if (l > 8) l = 8;
+        memcpy(hc, f->kstnm, l);
+        if (l < 8) hc[l] = '\0';
     }
     fp = fopen(path, "wb");
     if (!fp) return sks_internal_error_c(SKS_ERR_IO, "sac_write: cannot open the file");

@@ -31,7 +31,8 @@ def read_sac(path):
     c = raw[440:632]
     h = {k: float(f[v]) for k, v in FW.items()}
     h.update({k: int(i[v]) for k, v in IW.items()})
-    h["kstnm"] = c[:8].decode().strip()
+    h["kstnm"] = c[:8].split(b"\0")[0].decode().strip()
+    h["kstnm_raw"] = c[:8]
     h["kevnm"] = c[8:24].decode()
     h["kcmpnm"] = c[8 * 20:8 * 21].decode()
     data = np.frombuffer(raw[632:], np.float32)
@@ -48,7 +49,7 @@ def test_sac_write_layout(tmp_path):
     assert np.array_equal(d, x)
     assert h["delta"] == np.float32(0.02) and h["b"] == 0.0 and h["e"] == np.float32(0.34) and h["cmpaz"] == 90.0
     assert h["npts"] == 17 and h["iftype"] == 1 and h["leven"] == 1 and h["nvhdr"] == 6
-    assert h["kstnm"] == "ST1"
+    assert h["kstnm"] == "ST1" and h["kstnm_raw"] == b"ST1\x0045  "
     for k in ("depmin", "a", "mag", "stla", "evdp", "gcarc"):
         assert h[k] == -12345.0, k
     assert h["idep"] == -12345 and h["nzyear"] == -12345
@@ -129,3 +130,25 @@ def test_uvw2sac_program_and_refusals(tmp_path):
             sks.uvw2sac(words + ["nst=500"])                                   # more records than the files hold
     r = subprocess.run([PROG] + words + ["Conv_Source=1"], cwd=d, capture_output=True, text=True)
     assert r.returncode == 1 and "Conv_Source" in r.stderr
+
+
+@pytest.mark.parametrize("get_rec", [0, 1])
+def test_uvw2sac_byte_identical_to_the_reference_program(tmp_path, get_rec):
+    """Every file uvw2sac_gb300 writes -- the 18 SAC files, log.txt, pm.xy,
+    tt.txt -- is byte-identical to what the reference's uvw2sac writes from
+    the same inputs (tests/golden/uvw2sac.npz, made by make_golden_sac.py from
+    the program compiled out of semsyn/plot)."""
+    z = np.load(os.path.join(ROOT, "tests", "golden", "uvw2sac.npz"))
+    d = str(tmp_path)
+    for k in z.files:
+        if k.startswith("in/"):
+            z[k].tofile(os.path.join(d, k[3:]))
+    words = ["par=run.par", "zbeg=0", "idzplot=1", "zs=12.5", "Conv_Source=0", "tstart=3.5", "xmin=100.0",
+             "xbeg=3.0", f"get_rec={get_rec}"]
+    r = subprocess.run([PROG] + words, cwd=d, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    want = {k.split("/", 1)[1]: z[k].tobytes() for k in z.files if k.startswith(f"get_rec{get_rec}/")}
+    assert len(want) == 21
+    for name, data in want.items():
+        got = open(os.path.join(d, name), "rb").read()
+        assert got == data, name
