@@ -7,7 +7,6 @@ Stacey on/off, a GRT record step different from the SEM step with injection
 ending inside the run, Earth flattening, both receiver layouts, many warp-tile
 seams, runs split across calls, determinism and the drop-in CLI.
 """
-import glob
 import os
 import subprocess
 
@@ -18,7 +17,7 @@ import sks
 import synth
 from oracle.oracle import Oracle
 from golden.make_golden import extract
-from util import chdir, seis_err
+from util import chdir, seis_err, solver_fixtures
 
 pytestmark = pytest.mark.gpu
 
@@ -228,7 +227,7 @@ def test_cli_drop_in_writes_reference_files(casedirs):
     assert seis_err(got, ref) <= FP64_TOL
 
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = solver_fixtures()
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])

@@ -7,7 +7,6 @@ must reproduce them bit for bit; the FP64 build must stay within the FP32
 rounding noise of the reference.  Known answers of the GLL tables close the
 set.
 """
-import glob
 import os
 import tempfile
 
@@ -16,9 +15,9 @@ import pytest
 
 from golden.make_golden import extract
 from oracle.oracle import Oracle
-from util import chdir, rel_l2
+from util import chdir, rel_l2, solver_fixtures
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = solver_fixtures()
 # relative L2 of FP64 against the float reference: the reference's own FP32
 # rounding (measured 2e-6 .. 1e-5 on these cases)
 FP32_NOISE = 5e-5

@@ -4,7 +4,6 @@ sks_setup_open() is the set-up half of the reference's main(): par words,
 ray/SEM models, mesh, per-point materials, GLL tables, mass, Stacey matrix,
 receivers and the boundary-record schedule.  These tests need no GPU.
 """
-import glob
 import os
 import tempfile
 
@@ -15,9 +14,9 @@ import sks
 import synth
 from golden.make_golden import extract
 from oracle.oracle import Oracle
-from util import chdir
+from util import chdir, solver_fixtures
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = solver_fixtures()
 IDS = [os.path.basename(p)[:-4] for p in GOLDEN]
 
 

@@ -1,5 +1,6 @@
 """Shared helpers of the tests: synthetic cases in temp dirs, error norms."""
 import contextlib
+import glob
 import os
 
 import numpy as np
@@ -24,3 +25,14 @@ def chdir(d):
         yield
     finally:
         os.chdir(old)
+
+
+def solver_fixtures():
+    """The golden solver fixtures (tests/golden/*.npz holding a par file),
+    sorted; the uvw2sac fixture, which holds none, is left out."""
+    out = []
+    for p in sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))):
+        with np.load(p) as z:
+            if "in_run_par" in z.files:
+                out.append(p)
+    return out
