@@ -733,7 +733,7 @@ def cpu_rate(d: str, nsteps: int, procs: int, warm: int = 0) -> dict:
     single-threaded solves at once, each `warm` untimed steps then `nsteps`
     timed ones."""
     from oracle import oracle as orc
-    orc.build(None)
+    orc.build(with_reference=False)
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs) as pool:
         t0 = time.perf_counter()

@@ -71,9 +71,11 @@ typedef struct {
  * receiver file named there and builds the device state on `device`.  The
  * boundary-trace files are NOT read here (see sks_load_boundary_files).
  * Options the reference has that this library does not run return
- * SKS_ERR_UNSUPPORTED: msource=1 (explosive source), and GLL degrees other
- * than hpn = 4 or 5 (degree 5, the reference's default, runs with 4-warp
- * CTAs, register cap 0 or 1; a batch's members share one degree).  atten>0 (with ass) runs the
+ * SKS_ERR_UNSUPPORTED: msource=1 (explosive source).  Every GLL degree the
+ * reference accepts runs (hpn = 3..6, lagrange.c:323-328): degree 4 under
+ * every tuning, degrees 3, 5 (the reference's default) and 6 with 4-warp
+ * CTAs and register cap 0 or 1; batches and the serving loop run degrees 4
+ * and 5 (a batch's members share one degree).  atten>0 (with ass) runs the
  * reference's boundary taper (atten_wave2, sem2d_psvsh.c:1780-1822). */
 int sks_open_par(int argc, const char *const *argv, int precision, int device,
                  sks_solver **out);
@@ -290,6 +292,9 @@ int sks_line_increments(sks_solver *s, int32_t it0, int32_t nsteps, double *out)
  * boundary records (float32, 2*(nx+nz) and nx+nz values per record), the
  * four-tap schedule (tap_* record indices, -1 for an empty slot; w_* FP64
  * weights; 4 entries per step) covers nsteps+1 consecutive steps s..s+nsteps,
+ * and every tap that is not -1 must index a record the caller's rec_psv /
+ * rec_sh hold (the kernels read record tap without a bound; the caller's
+ * schedule is trusted as sks_setup_schedule writes it),
  * and out receives nsteps*nline*3 doubles: the increment g(s+k+1) - g(s+k)
  * of step s+k at every interface-line point (row nbl for ix >= nbl, then
  * column nbl for iz > nbl; nline = (nx-nbl)+(nz-nbl-1)).  The work is queued
@@ -299,8 +304,11 @@ int sks_line_increments(sks_solver *s, int32_t it0, int32_t nsteps, double *out)
  * It allocates nothing: the FP64 interpolated rows live in one fixed 8 MiB
  * scratch array inside the library, so (nsteps+2)*3*(nx+nz) must not exceed
  * 1048576 or the call fails with SKS_ERR_ARG.  The first call on a device
- * looks the scratch's device address up (cudaGetSymbolAddress) and keeps it;
- * make that first call before any stream capture.  All calls on a device
+ * looks the scratch's device address up (cudaGetSymbolAddress) and keeps it
+ * for that device's primary context, the one the CUDA runtime uses; a program
+ * that destroys that context (cudaDeviceReset) or calls from another driver
+ * API context must not call this entry again in that process.  Make that
+ * first call before any stream capture.  All calls on a device
  * share the scratch and it keeps the last call's contents (every value a call
  * reads is written by that call first); calls whose work overlaps on the GPU
  * (other streams, other host threads) race on it. */
@@ -309,8 +317,22 @@ int sks_line_increments_noalloc(const float *rec_psv, const float *rec_sh, int32
                                 const int32_t *tap_sh, const double *w_sh, int32_t nsteps,
                                 double *out, void *stream);
 
-/* Back to step 0 with a zero wavefield (boundary records are kept). */
+/* Back to step 0 with a zero wavefield (boundary records are kept); clears
+ * the non-finite flag. */
 int sks_reset(sks_solver *s);
+
+/* Wavefield health.  The step kernels flag a solve whose new displacement at
+ * any point is NaN or infinite (or, in the FP32C form, whose components'
+ * magnitudes sum past the largest float); the reference has no such check
+ * (its only guard replaces an interpolated boundary value outside (-10, 10),
+ * NaN included, by its neighbours' mean, sem2d_psvsh.c:432-444; a NaN with a
+ * non-finite neighbour, as in a whole NaN record, passes).  sks_run then returns
+ * SKS_ERR_NONFINITE after taking its steps (the seismograms are still
+ * written), and so does every later run until sks_reset or sks_state_load;
+ * sks_batch_run returns it when any member is flagged, and the serving loop
+ * fails that request alone.  Returns 1 while the solve is finite as of its
+ * last finished run, 0 once flagged. */
+int sks_wavefield_finite(const sks_solver *s);
 
 int sks_get_info(const sks_solver *s, sks_info_t *info);
 
@@ -406,11 +428,26 @@ double sks_last_run_ms(const sks_solver *s);
 int sks_enable_kernel_timing(sks_solver *s, int on);   /* also clears the sums */
 int sks_kernel_timing(const sks_solver *s, double *ms, int64_t *count);  /* arrays of SKS_KERNEL_CLASSES */
 
-/* Measured peak FMA throughput of the device's CUDA cores in TFLOP/s (an FMA
- * counts 2 flops), for precision SKS_FP64 (the FP64 pipe the FP64 form is
- * bound by) or SKS_FP32C (FP32): independent FMA chains on every SM, the best
- * of three event-timed launches after one untimed. */
+/* Measurement only, not part of a solve: the measured peak FMA throughput
+ * of the device's CUDA cores in TFLOP/s (an FMA counts 2 flops), for
+ * precision SKS_FP64 (the FP64 pipe the FP64 form is bound by) or SKS_FP32C
+ * (FP32): independent FMA chains on every SM, the best of three event-timed
+ * launches after one untimed.  The benchmark's FP64 compute roofline divides
+ * by it. */
 int sks_probe_fma_peak(int device, int precision, double *tflops);
+
+/* Tests of the failure path only, not part of a solve.  The pipelined chunks
+ * (tuning pipeline = 1) start a tile once its neighbours have finished the
+ * previous step; every such wait gives up after a bounded number of polls,
+ * sets an error flag that stops every CTA, and the run returns SKS_ERR_CUDA
+ * ("a wait for neighbouring tiles ran out") with the device still usable.
+ * These hooks make that happen on purpose: for the next sks_run (or the next
+ * batch run) only, tile `tile` of the chunk never marks a step finished and
+ * a wait gives up after spin_limit polls (128 ns apart).  The wavefield is
+ * then not meaningful; sks_reset (or sks_state_load) starts over.  The
+ * solver's tiles are numbered row by row over its CTA grid; a batch's over
+ * its members' tiles in member order. */
+int sks_test_stall_pipeline(sks_solver *s, int32_t tile, int32_t spin_limit);
 
 /* Destroys the solver; a batch member leaves its batch first. */
 void sks_destroy(sks_solver *s);
@@ -454,6 +491,8 @@ int sks_batch_get_tuning(const sks_batch *b, sks_tuning_t *t);
 int sks_batch_autotune(sks_batch *b, int32_t steps, sks_tuning_t *best);
 
 double sks_batch_last_run_ms(const sks_batch *b);     /* events on the batch's stream */
+/* The batch form of sks_test_stall_pipeline (tests of the failure path only). */
+int sks_batch_test_stall_pipeline(sks_batch *b, int32_t tile, int32_t spin_limit);
 int64_t sks_batch_kernel_launches(const sks_batch *b);
 /* Destroys the batch; the members stay open and leave it. */
 void sks_batch_destroy(sks_batch *b);
@@ -497,13 +536,20 @@ typedef struct {
 /* budget <= 0: 90 % of the device memory free at creation.  quantum_steps:
  * steps per scheduling round (64 = one chunk). */
 int sks_server_create(int device, int64_t device_budget_bytes, int32_t quantum_steps, sks_server **out);
+/* A form's tuning (as sks_batch_set_tuning).  A tuning other than 4 warps
+ * per CTA with register cap 0 or 1 cannot run GLL degree 5: it is refused
+ * (SKS_ERR_STATE) while the form has degree-5 requests queued or running,
+ * and afterwards degree-5 submissions of that form are refused. */
 int sks_server_set_tuning(sks_server *srv, int precision, const sks_tuning_t *t);
 int sks_server_set_active_points(sks_server *srv, int precision, int64_t max_points);
 /* Takes the set-up over (also on error).  pw: boundary records generated on
  * the device; NULL: read at admission from the files the par words name
  * (relative names resolved against the working directory at submission).
  * seis_u/v/w: nst*ntrace floats each, filled when the request is done (any
- * may be NULL); they must stay valid until then. */
+ * may be NULL); they must stay valid until then.  Served requests run GLL
+ * degrees 4 and 5; other degrees are refused here (SKS_ERR_UNSUPPORTED), as
+ * is degree 5 when the form's tuning cannot run it.  A request whose
+ * wavefield stops being finite fails alone with SKS_ERR_NONFINITE. */
 int sks_server_submit(sks_server *srv, sks_setup *su, int precision, const sks_plane_wave_t *pw,
                       float *seis_u, float *seis_v, float *seis_w, int64_t *id);
 /* Same with boundary records from a plane wave through a layered stack

@@ -21,11 +21,16 @@ BUILD = os.path.join(HERE, "_build")
 REF = os.path.join(HERE, "_ref")
 
 
-def build(reference_root: str | None = "/root/reference") -> None:
-    """Compile the restatement; also the reference binaries when its sources exist."""
+def build(reference_root: str | None = None, with_reference: bool = True) -> None:
+    """Compile the restatement; with_reference: also the reference binaries
+    (oracle/_ref) where the reference's sources are present.  Their location:
+    reference_root, else $SKS_REFERENCE_ROOT, else the Makefile's default."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True, capture_output=True)
-    if reference_root and os.path.isdir(os.path.join(reference_root, "semsyn", "src")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={reference_root}"], check=True, capture_output=True)
+    if not with_reference:
+        return
+    root = reference_root or os.environ.get("SKS_REFERENCE_ROOT")
+    cmd = ["make", "-s", "-C", HERE, "ref-if-present"] + ([f"REF={root}"] if root else [])
+    subprocess.run(cmd, check=True, capture_output=True)
 
 
 _libs: dict = {}
@@ -36,7 +41,7 @@ def _lib(fp64: bool) -> C.CDLL:
     if key not in _libs:
         path = os.path.join(BUILD, key)
         if not os.path.exists(path):
-            build(None)
+            build(with_reference=False)
         L = C.CDLL(path)
         L.oracle_create.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
         L.oracle_create.restype = C.c_void_p

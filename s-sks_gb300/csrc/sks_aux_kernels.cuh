@@ -7,16 +7,20 @@
 namespace sks {
 
 // coordinate of grid point j along a row or column of degree-deg elements
-// of size eh (deg 4 or 5): element j/deg, GLL node j%deg at
+// of size eh (deg 3..6): element j/deg, GLL node j%deg at
 // e*eh + (xi + 1)*eh/2 -- the node positions of the reference's
 // boundary-trace generator (semsyn/src/aserpsv_sem.c:887-920), in the host
-// generator's operation order
+// generator's operation order.  Nodes: +-1 and the roots of P'_deg
+// (3: +-1/sqrt(5); 4: 0, +-sqrt(3/7); 6: 0, +-sqrt((15 -+ 2 sqrt(15))/33)).
 __device__ __forceinline__ double gll_pos(int j, double eh, int deg)
 {
+    const double xi3[3] = {-1.0, -0.4472135954999579, 0.4472135954999579};
     const double xi4[4] = {-1.0, -0.6546536707079771, 0.0, 0.6546536707079771};
     const double xi5[5] = {-1.0, -0.7650553239294647, -0.2852315164806451, 0.2852315164806451, 0.7650553239294647};
-    const int e = deg == 5 ? j / 5 : j >> 2, a = deg == 5 ? j - 5 * e : j & 3;
-    const double xi = deg == 5 ? xi5[a] : xi4[a];
+    const double xi6[6] = {-1.0, -0.8302238962785669, -0.46884879347071423, 0.0, 0.46884879347071423,
+                           0.8302238962785669};
+    const int e = j / deg, a = j - deg * e;
+    const double xi = deg == 3 ? xi3[a] : deg == 5 ? xi5[a] : deg == 6 ? xi6[a] : xi4[a];
     return __dadd_rn(__dmul_rn((double)e, eh), __ddiv_rn(__dmul_rn(__dadd_rn(xi, 1.0), eh), 2.0));
 }
 

@@ -47,6 +47,11 @@ struct sks_batch {
     size_t items_cap = 0;
     int nitems = 0;
     BatchState* hstate = nullptr;         // pinned staging of the members' steps
+    int* herr = nullptr;                  // pinned: the pipelined chunks' wait-ran-out flag of the last run
+    // failure-path tests (sks_batch_test_stall_pipeline): for the next run,
+    // tile test_stall-1 never marks a step finished and a wait gives up after
+    // test_spins polls; 0 = off
+    int test_stall = 0, test_spins = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int graph_kernels = 0;                // kernels one graph launch runs
@@ -254,9 +259,13 @@ cudaError_t launch_pipe_chunk(sks_batch* b, int nsteps)
     const StepVariant v{b->NW, b->ZS, b->CAP, b->taper};
     static thread_local Coef<T> k;
     k = make_coef<T>(b->mem[0]->m);
-    cudaError_t e = cudaMemsetAsync(b->dpipe, 0, sizeof(int) * (2 + b->items_cap), b->stream);
+    // the claim counter and the done counters; the error flag stays set for
+    // the rest of a run once a wait ran out (batch_launch clears it)
+    cudaError_t e = cudaMemsetAsync(b->dpipe, 0, sizeof(int), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->dpipe + 2, 0, sizeof(int) * b->items_cap, b->stream);
     if (e != cudaSuccess) return e;
-    const BatchPipeCtl ctl{b->dpipe, b->dpipe + 1, b->dpipe + 2};
+    const BatchPipeCtl ctl{b->dpipe, b->dpipe + 1, b->dpipe + 2, b->test_stall ? b->test_spins : PIPE_SPIN_LIMIT,
+                           b->test_stall - 1};
     if (batch_deg(b) == 5) {
         static thread_local Coef<T, 5> k5;
         k5 = make_coef<T, 5>(b->mem[0]->m);
@@ -383,8 +392,10 @@ extern "C" int sks_batch_create(int precision, int device, sks_batch** out)
     e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev[0]);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev[1]);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&b->herr, sizeof(int));
     if (e != cudaSuccess) {
         if (b->stream) cudaStreamDestroy(b->stream);
+        if (b->herr) cudaFreeHost(b->herr);
         delete b;
         return set_err(SKS_ERR_CUDA, "batch stream/events: %s", cudaGetErrorString(e));
     }
@@ -472,12 +483,21 @@ int batch_launch(sks_batch* b, int32_t nsteps, float* const* su, float* const* s
         most = std::max(most, left);
     }
     CK(cudaMemcpyAsync(b->dstate, b->hstate, sizeof(BatchState) * n, cudaMemcpyHostToDevice, b->stream));
+    if (b->PIPE) CK(cudaMemsetAsync(b->dpipe + 1, 0, sizeof(int), b->stream));
     const int nchunks = (most + b->chunk - 1) / b->chunk;
     for (int c = 0; c < nchunks; c++) {
         CK(cudaGraphLaunch(b->exec, b->stream));
         b->launches += b->graph_kernels;
     }
     CK(cudaEventRecord(b->ev[1], b->stream));
+    // the run's flags: the pipelined chunks' and every member's wavefield flag
+    *b->herr = 0;
+    if (b->PIPE) CK(cudaMemcpyAsync(b->herr, b->dpipe + 1, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    for (int i = 0; i < n; i++) {
+        sks_solver* s = b->mem[i];
+        s->hflags[0] = 0;
+        CK(cudaMemcpyAsync(s->hflags, s->nonfinite, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    }
     b->running = true;
     // the new seismogram rows of each member into the caller's arrays
     for (int i = 0; i < n; i++) {
@@ -512,9 +532,12 @@ int batch_finish(sks_batch* b)
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
     b->last_ms = ms;
-    int err = 0;
-    if (b->PIPE) CK(cudaMemcpy(&err, b->dpipe + 1, sizeof(int), cudaMemcpyDeviceToHost));
-    int adv = 0;
+    const int err = b->PIPE ? *b->herr : 0;
+    if (b->test_stall) {
+        b->test_stall = 0;
+        b->graph_dirty = true;
+    }
+    int adv = 0, bad = -1;
     for (size_t i = 0; i < b->mem.size() && i < b->target.size(); i++) {
         sks_solver* s = b->mem[i];
         if (b->target[i] > s->step) {
@@ -523,8 +546,12 @@ int batch_finish(sks_batch* b)
             s->g_last = 0;
         }
         adv = std::max(adv, b->target[i] - b->start[i]);
+        if (bad < 0 && s->hflags[0]) bad = (int)i;
     }
     if (err) return set_err(SKS_ERR_CUDA, "pipelined batch chunk: a wait for neighbouring tiles ran out");
+    if (bad >= 0)
+        return set_err(SKS_ERR_NONFINITE, "member %d: the wavefield holds a non-finite displacement (sks_wavefield_finite "
+                       "names every such member)", bad);
     return adv;
 }
 
@@ -706,5 +733,23 @@ extern "C" void sks_batch_destroy(sks_batch* b)
     if (b->ev[0]) cudaEventDestroy(b->ev[0]);
     if (b->ev[1]) cudaEventDestroy(b->ev[1]);
     if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->herr) cudaFreeHost(b->herr);
     delete b;
+}
+
+extern "C" int sks_batch_test_stall_pipeline(sks_batch* b, int32_t tile, int32_t spin_limit)
+{
+    if (!b) return set_err(SKS_ERR_ARG, "batch is NULL");
+    if (b->running) return set_err(SKS_ERR_STATE, "the batch is running");
+    if (!b->PIPE) return set_err(SKS_ERR_STATE, "the batch does not run pipelined chunks (tuning pipeline=0)");
+    if (spin_limit < 1 || spin_limit > PIPE_SPIN_LIMIT) return set_err(SKS_ERR_ARG, "spin_limit=%d: 1..%d", spin_limit, PIPE_SPIN_LIMIT);
+    if (b->tables_dirty) {
+        const int rc = b->precision == SKS_FP64 ? build_tables<double>(b) : build_tables<float>(b);
+        if (rc) return rc;
+    }
+    if (tile < 0 || tile >= b->nitems) return set_err(SKS_ERR_ARG, "tile %d: 0..%d", tile, b->nitems - 1);
+    b->test_stall = tile + 1;
+    b->test_spins = spin_limit;
+    b->graph_dirty = true;
+    return SKS_OK;
 }

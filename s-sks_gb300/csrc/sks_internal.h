@@ -105,6 +105,18 @@ struct sks_solver {
     size_t snap_size;
     int nsnap;
     bool snap_taken[SKS_NSNAP];
+    // wavefield health: a device flag the step kernels set when a point's new
+    // displacement is not finite (cleared by sks_reset / sks_state_load), and
+    // pinned host words the end of a run copies the flags into: [0] that
+    // flag, [1] the pipelined chunks' wait-ran-out flag
+    int* nonfinite;
+    int* hflags;
+    // per element row: 1 when all its points are of isotropic materials
+    uint8_t* row_iso;
+    // failure-path tests (sks_test_stall_pipeline): for the next run, tile
+    // test_stall-1 of the pipelined chunks never marks a step finished and a
+    // wait gives up after test_spins polls; 0 = off
+    int test_stall, test_spins;
 };
 
 namespace sksi {
@@ -172,6 +184,8 @@ Field<T> make_field(sks_solver* s)
     F.seam_cnt = s->seam_cnt;
     F.snap = nullptr;
     F.snap_nzs = (s->m.nz + 1) / 2;
+    F.nonfinite = s->nonfinite;
+    F.row_iso = s->row_iso;
     return F;
 }
 

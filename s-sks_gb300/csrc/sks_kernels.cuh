@@ -41,9 +41,10 @@ constexpr int NP = N + 1;     // points per element edge
 constexpr int TEX = 6;        // elements per warp tile in x
 constexpr int TW = TEX * N;   // grid columns per warp tile
 
-// The kernels are templates on the degree DEG (default 4; 5 is instantiated
-// too): DEG+1 lanes per element and 30 / (DEG+1) elements per warp, so both
-// degrees fill lanes 0..29 and leave 30, 31 idle.
+// The kernels are templates on the degree DEG (default 4; 3, 5 and 6 are
+// instantiated too): DEG+1 lanes per element and 30 / (DEG+1) elements per
+// warp, so degrees 4 and 5 fill lanes 0..29 and leave 30, 31 idle, degrees 3
+// (7 elements of 4 lanes) and 6 (4 elements of 7 lanes) fill lanes 0..27.
 __host__ __device__ constexpr int tex_of(int deg) { return 30 / (deg + 1); }
 constexpr int MAT_STRIDE = 16;
 
@@ -126,6 +127,12 @@ struct Field {
     // the taper's zones in the struct's tail padding: atten (0: none; 1..4:
     // bottom, + left, + right, + top) in bits 0-2, nh = neh*hpn above them
     int taper_zones;
+    // set to 1 by any point whose new displacement is not finite (sticky;
+    // the host reads and clears it)
+    int* nonfinite;
+    // per element row: 1 when every point of its grid rows has an isotropic
+    // material (the anisotropic kernels take the isotropic stress there)
+    const uint8_t* __restrict__ row_iso;
 };
 
 // Displacement layout: the P-SV pair (u_x, u_z) of every point as one 2-vector
@@ -211,11 +218,15 @@ struct MatRow<T, false> {
 };
 
 // stress on the strain list (e11, e12=u_y,x, e13=u_z,x+u_x,z, e23=u_y,z, e33):
-// sigma_a = sum_b C[a][b] e_b in b order, as Stress_ij (sem2d_psvsh.c:1345-1380)
+// sigma_a = sum_b C[a][b] e_b in b order, as Stress_ij (sem2d_psvsh.c:1345-1380).
+// iso (anisotropic kernels, an element row of isotropic materials only): the
+// isotropic form, which gives the anisotropic sums' values for an isotropic
+// material (the zero entries' products add nothing; C33 = C11, C55 = C44 =
+// C66), with 7 operations instead of 25
 template <typename T, bool ANISO>
-__device__ __forceinline__ void stress(const MatRow<T, ANISO>& M, const T e[5], T s[5])
+__device__ __forceinline__ void stress(const MatRow<T, ANISO>& M, const T e[5], T s[5], bool iso = false)
 {
-    if (ANISO) {
+    if (ANISO && !iso) {
         const T* c = M.s;   // upper triangle: 0..4 row0, 5..8 row1, 9..11 row2, 12..13 row3, 14 row4
         s[0] = c[0] * e[0];  s[0] = fma(c[1], e[1], s[0]);  s[0] = fma(c[2], e[2], s[0]);  s[0] = fma(c[3], e[3], s[0]);  s[0] = fma(c[4], e[4], s[0]);
         s[1] = c[1] * e[0];  s[1] = fma(c[5], e[1], s[1]);  s[1] = fma(c[6], e[2], s[1]);  s[1] = fma(c[7], e[3], s[1]);  s[1] = fma(c[8], e[4], s[1]);
@@ -241,10 +252,11 @@ struct Aux {
 };
 
 template <typename T, bool LF, bool CG = false>
-__device__ __forceinline__ void load_aux(const Field<T>& F, int64_t np, int64_t g, Aux<T, LF>& x)
+__device__ __forceinline__ void load_aux(const Field<T>& F, int np, int g, Aux<T, LF>& x)
 {
+    // 32-bit offsets: 3*np < 2^31 (checked on the host)
     if constexpr (!LF) {
-        load_u<T, CG>(F.un, (int)np, (int)g, x.a);
+        load_u<T, CG>(F.un, np, g, x.a);
     } else {
 #pragma unroll
         for (int c = 0; c < 3; c++) {
@@ -295,15 +307,34 @@ __device__ __forceinline__ void taper_point(const Field<T>& F, const Geo<T>& G, 
     if (atten > 3 && iz >= nz - nh && ix < nx - nh && ix >= nh) scale(F.taper[iz - nz + nh]);
 }
 
+// A point's new displacement is bad when a component is NaN or infinite.
+// FP32: the magnitudes' sum is not below the largest finite float (also true
+// when finite components sum past it: a blown-up field).  FP64: an exponent
+// field of all ones, tested on the high words with integer instructions, so
+// the check takes nothing from the FP64 pipe the form is bound by.
+__device__ __forceinline__ bool not_finite3(const float v[3])
+{
+    return !(fabsf(v[0]) + fabsf(v[1]) + fabsf(v[2]) <= 3.402823466e38f);
+}
+__device__ __forceinline__ bool not_finite3(const double v[3])
+{
+    const unsigned e0 = (unsigned)__double2hiint(v[0]) & 0x7ff00000u;
+    const unsigned e1 = (unsigned)__double2hiint(v[1]) & 0x7ff00000u;
+    const unsigned e2 = (unsigned)__double2hiint(v[2]) & 0x7ff00000u;
+    return max(max(e0, e1), e2) == 0x7ff00000u;
+}
+
 // update one owned point, sample it if it is a receiver, then add the next
 // step's boundary increment if it lies on the interface line
+// plain: the CTA's tile holds no Stacey edge point, receiver, snapshot point,
+// interface-line point or taper zone (tile-uniform), so none of their tests runs
 template <typename T, bool LF, bool TP = false, int DEG = N>
 __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G, const Coef<T, DEG>& k,
                                              int ix, int iz, const T u[3], const T K[3], T rinv,
-                                             T wxi, T wzi, const Aux<T, LF>& x, const PointFlags& pf)
+                                             T wxi, T wzi, const Aux<T, LF>& x, const PointFlags& pf, bool plain)
 {
     const int g = iz * G.nx + ix;
-    const bool edge = pf.edge_x || iz == 0 || (iz == G.nz - 1 && pf.top_ok);
+    const bool edge = !plain && (pf.edge_x || iz == 0 || (iz == G.nz - 1 && pf.top_ok));
     T un[3], dn[3], cn[3];
     if (!LF) {
         if (!edge) {
@@ -336,6 +367,7 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
     if constexpr (TP) {
         if (F.taper_zones) taper_point<T, LF>(F, G, ix, iz, un, dn, cn);
     }
+    if (!plain) {
     // kirrecord_zhl: the field after the update, before the next injection
     if (iz >= F.rec_iz0 && iz <= F.rec_iz1 && ((__ldg(F.recbits + (g >> 5)) >> (g & 31)) & 1u)) {
         int lo = 0, hi = F.nrec;
@@ -371,6 +403,8 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
             }
         }
     }
+    }
+    if (not_finite3(un)) *F.nonfinite = 1;
     const int np = (int)G.np;
     store_u<T>(F.un, np, g, un);
     if constexpr (LF) {
@@ -418,10 +452,11 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     constexpr int S = TEX * NW - 1;                // owned elements per CTA
-    const int e = lane / NP, al = lane - e * NP;   // lanes 30,31: e = 6
+    constexpr int LANES = TEX * NP;                // lanes holding element columns (28 or 30)
+    const int e = lane / NP, al = lane - e * NP;   // lanes >= LANES: e = TEX
     const int q = TEX * w + e;                     // element within the CTA
     const int ex = cx * S - 1 + q;
-    const bool live = lane < 30 && ex >= 0 && ex < G.nex;
+    const bool live = lane < LANES && ex >= 0 && ex < G.nex;
     const int nx = G.nx;
     // lanes off the mesh read a valid column; their force never reaches a
     // live lane (shuffles stay inside an element, the left neighbour is masked)
@@ -436,6 +471,17 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
     pfl.top_ok = ix >= 1 && ix <= 3 * N;
     pfl.on_col = ix == G.nbl;
     pfl.row_ok = ix >= G.nbl;
+    // the tile's owned columns [ix0, ix1] and rows [iz0, iz1] miss every
+    // special point: no box edge (left, right, bottom, top), no receiver row,
+    // no snapshot this step, no interface line, no taper
+    bool plain;
+    {
+        const int ix0 = cx * S * N, ix1 = min((cx + 1) * S * N, nx - 1);
+        const int iz0 = ez0 * N, iz1 = ez1 * N;
+        plain = ix0 > 0 && ix1 < nx - 1 && iz0 > 0 && iz1 < G.nz - 1 && !F.snap &&
+                (F.rec_iz1 < iz0 || F.rec_iz0 > iz1) && !(TP && F.taper_zones) &&
+                !(F.inject_next && ((G.nbl >= iz0 && G.nbl <= iz1) || (G.nbl >= ix0 && G.nbl <= ix1)));
+    }
 
     // x contractions: the lane's own column term first, then the element's
     // other 4 columns in rotation (al+1, al+2, ... mod 5) by shuffle
@@ -486,10 +532,11 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
                 m[b] = F.mid[g];
             }
         }
+        const bool iso_row = ANISO && F.row_iso[ez];
         Aux<T, LF> aux[N];
         if (!halo && own_x) {
 #pragma unroll
-            for (int b = 0; b < N; b++) load_aux<T, LF, CG>(F, G.np, (int64_t)(ez * N + b) * nx + ix, aux[b]);
+            for (int b = 0; b < N; b++) load_aux<T, LF, CG>(F, np, (ez * N + b) * nx + ix, aux[b]);
         }
         T kk[NP][3];
 #pragma unroll
@@ -518,7 +565,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
             }
             rinv[bb] = M.s[15];
             T sg[5];
-            stress<T, ANISO>(M, ee, sg);
+            stress<T, ANISO>(M, ee, sg, iso_row);
             // x-divergence of row bb (a halo element row only needs its top row)
             if (!halo || bb == N) {
 #pragma unroll
@@ -548,7 +595,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
         rinvN = rinv[N];
         if (!halo) {
             // the last column of each warp goes to the next warp
-            if (lane == 29) {
+            if (lane == LANES - 1) {
 #pragma unroll
                 for (int b = 0; b < N; b++)
 #pragma unroll
@@ -577,7 +624,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
                 }
                 if (own_x) {
                     const T wzi = b > 0 ? k.winv[b] : (ez == 0 ? k.winv[0] : k.winv2);
-                    finish_point<T, LF, TP, DEG>(F, G, k, ix, ez * N + b, u[b], kt, rinv[b], wxi, wzi, aux[b], pfl);
+                    finish_point<T, LF, TP, DEG>(F, G, k, ix, ez * N + b, u[b], kt, rinv[b], wxi, wzi, aux[b], pfl, plain);
                 }
             }
             if (seam_row0) {
@@ -595,7 +642,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
 #pragma unroll
                         for (int c = 0; c < 3; c++)
                             K[c] = (__ldcg(lo + c) + __ldcg(hi + c)) + (__ldcg(lo + 3 + c) + __ldcg(hi + 3 + c));
-                        finish_point<T, LF, TP, DEG>(F, G, k, ix, ez0 * N, u[0], K, rinv[0], wxi, k.winv2, aux[0], pfl);
+                        finish_point<T, LF, TP, DEG>(F, G, k, ix, ez0 * N, u[0], K, rinv[0], wxi, k.winv2, aux[0], pfl, plain);
                     }
                 }
             }
@@ -604,7 +651,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
     }
     // the band's top row: the box's top (complete now) or a seam with the band above
     if (ez1 == G.nez || ZS) {
-        if (lane == 29) {
+        if (lane == LANES - 1) {
 #pragma unroll
             for (int c = 0; c < 3; c++) sh.xtop[w][c] = kc[c];
         }
@@ -621,8 +668,8 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
         if (ez1 == G.nez) {
             if (own_x) {
                 Aux<T, LF> x;
-                load_aux<T, LF, CG>(F, G.np, (int64_t)iz * nx + ix, x);
-                finish_point<T, LF, TP, DEG>(F, G, k, ix, iz, u[N], kt, rinvN, wxi, k.winv[0], x, pfl);
+                load_aux<T, LF, CG>(F, np, iz * nx + ix, x);
+                finish_point<T, LF, TP, DEG>(F, G, k, ix, iz, u[N], kt, rinvN, wxi, k.winv[0], x, pfl, plain);
             }
         } else {
             if (own_x) {
@@ -643,8 +690,8 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
                     for (int c = 0; c < 3; c++)
                         K[c] = (lft[c] + __ldcg(hi + c)) + (kc[c] + __ldcg(hi + 3 + c));
                     Aux<T, LF> x;
-                    load_aux<T, LF, CG>(F, G.np, (int64_t)iz * nx + ix, x);
-                    finish_point<T, LF, TP, DEG>(F, G, k, ix, iz, u[N], K, rinvN, wxi, k.winv2, x, pfl);
+                    load_aux<T, LF, CG>(F, np, iz * nx + ix, x);
+                    finish_point<T, LF, TP, DEG>(F, G, k, ix, iz, u[N], K, rinvN, wxi, k.winv2, x, pfl, plain);
                 }
             }
         }
@@ -768,6 +815,8 @@ struct PipeCtl {
     int* claim;            // next (step, tile) index
     int* done;             // per tile: steps of the chunk it has finished
     int* error;            // set when a wait ran out
+    int spin_limit;        // polls before a wait gives up
+    int stall_tile;        // -1; for tests of the failure path, a tile that never marks a step finished
 };
 
 struct PipeChunk {
@@ -814,6 +863,7 @@ __device__ __forceinline__ void st_release(int* p, int v)
 }
 
 constexpr int PIPE_SPIN_LIMIT = 1 << 22;   // polls of one wait (with 128 ns sleeps: about a second)
+constexpr int PIPE_TEST_SPIN_LIMIT = 1 << 14;   // the failure-path tests' limit (a few ms)
 
 template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false, int DEG = N>
 __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
@@ -844,7 +894,7 @@ k_step_pipe(Field<T> F, Geo<T> G, Coef<T, DEG> k, PipeChunk C, PipeCtl ctl)
                     const int* f = ctl.done + z * G.ncx + x;
                     int spins = 0;
                     while (ld_acquire(f) < st) {
-                        if (++spins > PIPE_SPIN_LIMIT || ld_acquire(ctl.error)) { fail = 1; break; }
+                        if (++spins > ctl.spin_limit || ld_acquire(ctl.error)) { fail = 1; break; }
                         __nanosleep(128);
                     }
                 }
@@ -873,7 +923,7 @@ k_step_pipe(Field<T> F, Geo<T> G, Coef<T, DEG> k, PipeChunk C, PipeCtl ctl)
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
-            st_release(ctl.done + t, st + 1);
+            if (t != ctl.stall_tile) st_release(ctl.done + t, st + 1);
             s_claim = ld_acquire(ctl.error) ? total : s_next;
         }
         __syncthreads();
@@ -895,6 +945,8 @@ struct BatchPipeCtl {
     int* claim;            // next (step, tile) index
     int* error;            // set when a wait ran out
     int* done;             // per tile: steps of the chunk it has finished
+    int spin_limit;        // polls before a wait gives up
+    int stall_item;        // -1; for tests of the failure path, a tile that never marks a step finished
 };
 
 template <typename T, bool ANISO, bool LF, int NW, bool ZS, int CAP, bool TP = false, int DEG = N>
@@ -944,7 +996,7 @@ k_step_batch_pipe(const BatchMember<T>* __restrict__ mem, const BatchState* __re
                     const int* f = ctl.done + M->item0 + z * sG.ncx + x;
                     int spins = 0;
                     while (ld_acquire(f) < j) {
-                        if (++spins > PIPE_SPIN_LIMIT || ld_acquire(ctl.error)) { fail = 1; break; }
+                        if (++spins > ctl.spin_limit || ld_acquire(ctl.error)) { fail = 1; break; }
                         __nanosleep(128);
                     }
                 }
@@ -970,7 +1022,7 @@ k_step_batch_pipe(const BatchMember<T>* __restrict__ mem, const BatchState* __re
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();                // publishes the whole tile (see k_step_pipe)
-            if (s_go) st_release(ctl.done + i, j + 1);
+            if (s_go && i != ctl.stall_item) st_release(ctl.done + i, j + 1);
             s_claim = ld_acquire(ctl.error) ? total : s_next;
         }
         __syncthreads();
@@ -1043,6 +1095,20 @@ cudaError_t launch_step_f64_d5(const StepVariant& v, bool aniso, int blocks, cud
 int pipe_occupancy_f64_d5(const StepVariant& v, bool aniso);
 cudaError_t launch_pipe_f64_d5(const StepVariant& v, bool aniso, int blocks, cudaStream_t st, const Field<double>& F,
                                const Geo<double>& G, const Coef<double, 5>& k, const PipeChunk& C, const PipeCtl& ctl);
+// GLL degrees 3 and 6 (4 warps, register cap 0 or 1; single solves)
+#define SKS_DEG_DECL(F, T, D)                                                                                   \
+    int step_occupancy_##F##_d##D(const StepVariant& v, bool aniso);                                          \
+    cudaError_t launch_step_##F##_d##D(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,         \
+                                       const Field<T>& F_, const Geo<T>& G, const Coef<T, D>& k);             \
+    int pipe_occupancy_##F##_d##D(const StepVariant& v, bool aniso);                                          \
+    cudaError_t launch_pipe_##F##_d##D(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,         \
+                                       const Field<T>& F_, const Geo<T>& G, const Coef<T, D>& k,              \
+                                       const PipeChunk& C, const PipeCtl& ctl);
+SKS_DEG_DECL(f32, float, 3)
+SKS_DEG_DECL(f64, double, 3)
+SKS_DEG_DECL(f32, float, 6)
+SKS_DEG_DECL(f64, double, 6)
+#undef SKS_DEG_DECL
 // the same with the boundary taper compiled in (the entry points above call
 // these for a variant with taper set)
 int step_occupancy_f32_tp(const StepVariant& v, bool aniso);

@@ -179,6 +179,8 @@ static int mat_is_iso(const double *r)
            r[10] == 0 && r[11] == 0 && r[13] == 0 && r[0] == r[14] && r[5] == r[9] && r[9] == r[12];
 }
 
+int sks_material_is_isotropic(const double *r) { return mat_is_iso(r); }
+
 /* a SEM-model / ray-model layer: 13 constants (Cijkl_3D, sem2d_psvsh.c:1528-1563)
  * or, with semmodel_full=1, all 21 */
 typedef struct { double v[21]; double rho; int full; } LayerC;

@@ -80,6 +80,10 @@ __attribute__((visibility("hidden")))
 int  sks_model_from_par(sks_model *m, int argc, const char *const *argv, char *err, size_t errlen);
 __attribute__((visibility("hidden")))
 void sks_model_free(sks_model *m);
+/* 1 when a material row (the 15 stiffness entries, then rho) has the
+ * isotropic pattern exactly: zero coupling entries, C11 = C33, C44 = C55 = C66 */
+__attribute__((visibility("hidden")))
+int sks_material_is_isotropic(const double *r);
 __attribute__((visibility("hidden")))
 int  sks_mesh_spacing(const char *raymodel, int flat, int nfil, float eh_par, int hpn, int *nez, float *eh_f,
                       float *h_f, char *err, size_t errlen);

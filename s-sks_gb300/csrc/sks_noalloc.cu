@@ -28,8 +28,9 @@ extern "C" int sks_internal_set_error(int code, const char* msg, cudaError_t e);
 namespace {
 
 // Device address of the scratch, looked up once per device (with that device
-// current).  In host code the array's name is only a stand-in for the device
-// symbol, never a usable address.
+// current) in the device's primary context, which the CUDA runtime uses.  In
+// host code the array's name is only a stand-in for the device symbol, never
+// a usable address.
 std::mutex g_mu;
 double* g_addr[128] = {};
 
@@ -47,11 +48,13 @@ extern "C" int sks_line_increments_noalloc(const float* rec_psv, const float* re
     if (nx < 2 || nz < 2 || nbl < 0 || nbl >= nx - 1 || nbl >= nz - 1 || nsteps < 0)
         return fail(SKS_ERR_ARG, "bad sizes (nx, nz, nbl, nsteps)");
     if (nsteps == 0) return SKS_OK;
-    const int mtotal = 2 * (nx + nz), shtotal = nx + nz, L = mtotal + shtotal;
-    const size_t need = (size_t)(nsteps + 2) * (size_t)L;
-    if (need > kScratchDoubles)
+    // sizes in 64 bits, checked against the scratch before any narrowing
+    const int64_t L64 = 3 * ((int64_t)nx + nz);
+    const int64_t need = ((int64_t)nsteps + 2) * L64;
+    if (need > (int64_t)kScratchDoubles)
         return fail(SKS_ERR_ARG, "nsteps too large for the fixed scratch: (nsteps+2)*(3*(nx+nz)) must be "
                                  "at most 1048576");
+    const int mtotal = (int)(2 * ((int64_t)nx + nz)), shtotal = nx + nz, L = (int)L64;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(SKS_ERR_CUDA, "cudaGetDevice", e);

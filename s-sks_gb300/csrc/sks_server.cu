@@ -103,6 +103,9 @@ struct sks_server {
     // of all sharing the device
     int64_t max_points[2] = {(int64_t)8 << 20, (int64_t)24 << 20};
     int64_t active_points[2] = {0, 0};
+    // per form: the batch's tuning runs GLL degree 5 (4 warps per CTA,
+    // register cap 0 or 1); guarded by mu
+    bool deg5_ok[2] = {true, true};
     sks_batch* batch[2] = {nullptr, nullptr};      // by precision
     std::mutex mu;                                 // guards queue, reqs, next_id, in_use and the
                                                    // request fields other threads read
@@ -288,8 +291,29 @@ extern "C" int sks_server_set_tuning(sks_server* v, int precision, const sks_tun
 {
     if (!v || !t) return set_err(SKS_ERR_ARG, "NULL argument");
     if (precision != SKS_FP64 && precision != SKS_FP32C) return set_err(SKS_ERR_ARG, "unknown precision %d", precision);
+    const bool deg5 = t->warps_per_block == 4 && t->register_cap <= 1;
+    {
+        // a tuning that cannot run degree 5 is refused while the form has
+        // degree-5 requests queued or running
+        std::lock_guard<std::mutex> lk(v->mu);
+        if (!deg5) {
+            for (const Request* r : v->queue)
+                if (r->precision == precision && r->su && r->su->m.hpn == 5)
+                    return set_err(SKS_ERR_STATE, "request %lld is of GLL degree 5, which runs with 4 warps per CTA "
+                                                  "and register cap 0 or 1", (long long)r->id);
+            for (const Request* r : v->active[precision])
+                if (r->s && r->s->m.hpn == 5)
+                    return set_err(SKS_ERR_STATE, "request %lld is of GLL degree 5, which runs with 4 warps per CTA "
+                                                  "and register cap 0 or 1", (long long)r->id);
+        }
+    }
     if (batch_running(v->batch[precision])) batch_finish(v->batch[precision]);
-    return sks_batch_set_tuning(v->batch[precision], t);
+    const int rc = sks_batch_set_tuning(v->batch[precision], t);
+    if (!rc) {
+        std::lock_guard<std::mutex> lk(v->mu);
+        v->deg5_ok[precision] = deg5;
+    }
+    return rc;
 }
 
 extern "C" int sks_server_set_active_points(sks_server* v, int precision, int64_t max_points)
@@ -315,6 +339,20 @@ int submit(sks_server* v, sks_setup* su, int precision, const sks_plane_wave_t* 
     if (precision != SKS_FP64 && precision != SKS_FP32C) {
         sks_setup_close(su);
         return set_err(SKS_ERR_ARG, "unknown precision %d", precision);
+    }
+    if (su->m.hpn != 4 && su->m.hpn != 5) {
+        const int hpn = su->m.hpn;
+        sks_setup_close(su);
+        return set_err(SKS_ERR_UNSUPPORTED, "hpn=%d: served requests run GLL degrees 4 and 5 (other degrees run as "
+                                            "single solves)", hpn);
+    }
+    if (su->m.hpn == 5) {
+        std::lock_guard<std::mutex> lk(v->mu);
+        if (!v->deg5_ok[precision]) {
+            sks_setup_close(su);
+            return set_err(SKS_ERR_UNSUPPORTED, "GLL degree 5 requests need the form's tuning to be 4 warps per CTA "
+                                                "and register cap 0 or 1 (sks_server_set_tuning)");
+        }
     }
     if (!pw && !layers) {
         int rc = absolute_path(su->m.greenfile, sizeof su->m.greenfile);
@@ -398,13 +436,15 @@ extern "C" int sks_server_step(sks_server* v)
     cudaSetDevice(v->device);
     bool progressed = false;
     // finished quanta: move steps on, retire the requests that reached their
-    // end; a quantum that failed fails its form's running requests
+    // end; a quantum that failed fails its form's running requests, except
+    // that a request whose wavefield stopped being finite fails alone (its
+    // batch mates' results do not depend on it)
     for (int f = 0; f < 2; f++) {
         sks_batch* b = v->batch[f];
         if (!batch_running(b) || !batch_done(b)) continue;
         const int rc = batch_finish(b);
         progressed = true;
-        if (rc < 0) {
+        if (rc < 0 && rc != SKS_ERR_NONFINITE) {
             fail_form(v, f, rc);
             continue;
         }
@@ -414,7 +454,8 @@ extern "C" int sks_server_step(sks_server* v)
         }
         std::vector<Request*> keep;
         for (Request* r : v->active[f]) {
-            if (r->s->step >= r->s->m.nst) retire(v, r);
+            if (!sks_wavefield_finite(r->s)) finish_request(v, r, SKS_ERR_NONFINITE);
+            else if (r->s->step >= r->s->m.nst) retire(v, r);
             else keep.push_back(r);
         }
         v->active[f].swap(keep);

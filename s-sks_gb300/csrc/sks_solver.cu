@@ -139,7 +139,7 @@ void free_device(sks_solver* s)
     void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc, s->taper,
                   s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seisbuf[0], s->seisbuf[1], s->G, s->Dl, s->rec_psv, s->rec_sh,
                   s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt, s->items, s->seis_full,
-                  s->pipe_ctl, s->snaps, s->ser};
+                  s->pipe_ctl, s->snaps, s->ser, s->nonfinite, s->row_iso};
     for (void* p : ps)
         if (p) cudaFree(p);
     s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = s->taper = nullptr;
@@ -153,6 +153,8 @@ void free_device(sks_solver* s)
     s->pipe_ctl = nullptr;
     s->pipe_ctl_n = 0;
     s->snaps = nullptr;
+    s->nonfinite = nullptr;
+    s->row_iso = nullptr;
 }
 
 // per-kernel-class timing: an event pair around each launch when enabled
@@ -273,23 +275,119 @@ int upload_tables(sks_solver* s)
 // waves CTAs, each column split into bands of near-equal height, so every
 // SM carries the same work (no partly filled last wave).  The band-seam
 // buffers grow to fit and their counters restart at 0.
+// The compiled kernels of one GLL degree D (3..6) and form T: occupancy and
+// launch of the per-step and the pipelined step kernel.
+template <typename T, int D>
+struct DegKernels {
+    static constexpr bool F32 = sizeof(T) == 4;
+    static int step_occ(const StepVariant& v, bool a)
+    {
+        if constexpr (D == 3) return F32 ? step_occupancy_f32_d3(v, a) : step_occupancy_f64_d3(v, a);
+        else if constexpr (D == 5) return F32 ? step_occupancy_f32_d5(v, a) : step_occupancy_f64_d5(v, a);
+        else if constexpr (D == 6) return F32 ? step_occupancy_f32_d6(v, a) : step_occupancy_f64_d6(v, a);
+        else return F32 ? step_occupancy_f32(v, a) : step_occupancy_f64(v, a);
+    }
+    static int pipe_occ(const StepVariant& v, bool a)
+    {
+        if constexpr (D == 3) return F32 ? pipe_occupancy_f32_d3(v, a) : pipe_occupancy_f64_d3(v, a);
+        else if constexpr (D == 5) return F32 ? pipe_occupancy_f32_d5(v, a) : pipe_occupancy_f64_d5(v, a);
+        else if constexpr (D == 6) return F32 ? pipe_occupancy_f32_d6(v, a) : pipe_occupancy_f64_d6(v, a);
+        else return F32 ? pipe_occupancy_f32(v, a) : pipe_occupancy_f64(v, a);
+    }
+    static cudaError_t step(const StepVariant& v, bool a, int blocks, cudaStream_t st, const Field<T>& F,
+                            const Geo<T>& G, const Coef<T, D>& k)
+    {
+        if constexpr (F32) {
+            if constexpr (D == 3) return launch_step_f32_d3(v, a, blocks, st, F, G, k);
+            else if constexpr (D == 5) return launch_step_f32_d5(v, a, blocks, st, F, G, k);
+            else if constexpr (D == 6) return launch_step_f32_d6(v, a, blocks, st, F, G, k);
+            else return launch_step_f32(v, a, blocks, st, F, G, k);
+        } else {
+            if constexpr (D == 3) return launch_step_f64_d3(v, a, blocks, st, F, G, k);
+            else if constexpr (D == 5) return launch_step_f64_d5(v, a, blocks, st, F, G, k);
+            else if constexpr (D == 6) return launch_step_f64_d6(v, a, blocks, st, F, G, k);
+            else return launch_step_f64(v, a, blocks, st, F, G, k);
+        }
+    }
+    static cudaError_t pipe(const StepVariant& v, bool a, int blocks, cudaStream_t st, const Field<T>& F,
+                            const Geo<T>& G, const Coef<T, D>& k, const PipeChunk& C, const PipeCtl& ctl)
+    {
+        if constexpr (F32) {
+            if constexpr (D == 3) return launch_pipe_f32_d3(v, a, blocks, st, F, G, k, C, ctl);
+            else if constexpr (D == 5) return launch_pipe_f32_d5(v, a, blocks, st, F, G, k, C, ctl);
+            else if constexpr (D == 6) return launch_pipe_f32_d6(v, a, blocks, st, F, G, k, C, ctl);
+            else return launch_pipe_f32(v, a, blocks, st, F, G, k, C, ctl);
+        } else {
+            if constexpr (D == 3) return launch_pipe_f64_d3(v, a, blocks, st, F, G, k, C, ctl);
+            else if constexpr (D == 5) return launch_pipe_f64_d5(v, a, blocks, st, F, G, k, C, ctl);
+            else if constexpr (D == 6) return launch_pipe_f64_d6(v, a, blocks, st, F, G, k, C, ctl);
+            else return launch_pipe_f64(v, a, blocks, st, F, G, k, C, ctl);
+        }
+    }
+};
+
+// calls f.template run<D>() for the solver's degree D (3..6)
+template <typename Fn>
+auto with_degree(int hpn, Fn& f)
+{
+    switch (hpn) {
+    case 3: return f.template run<3>();
+    case 5: return f.template run<5>();
+    case 6: return f.template run<6>();
+    default: return f.template run<4>();
+    }
+}
+
+struct OccOf {
+    const sks_solver* s;
+    const StepVariant& v;
+    bool pipe;
+    template <int D>
+    int run()
+    {
+        const bool a = s->m.anisotropic != 0;
+        if (s->precision == SKS_FP64)
+            return pipe ? DegKernels<double, D>::pipe_occ(v, a) : DegKernels<double, D>::step_occ(v, a);
+        return pipe ? DegKernels<float, D>::pipe_occ(v, a) : DegKernels<float, D>::step_occ(v, a);
+    }
+};
+
 // resident CTAs per SM of the solver's step / pipelined variant (form and degree)
 int step_occ(const sks_solver* s, const StepVariant& v)
 {
-    const bool a = s->m.anisotropic != 0;
-    if (s->m.hpn == 5) return s->precision == SKS_FP64 ? step_occupancy_f64_d5(v, a) : step_occupancy_f32_d5(v, a);
-    return s->precision == SKS_FP64 ? step_occupancy_f64(v, a) : step_occupancy_f32(v, a);
+    OccOf o{s, v, false};
+    return with_degree(s->m.hpn, o);
 }
 
 int pipe_occ(const sks_solver* s, const StepVariant& v)
 {
-    const bool a = s->m.anisotropic != 0;
-    if (s->m.hpn == 5) return s->precision == SKS_FP64 ? pipe_occupancy_f64_d5(v, a) : pipe_occupancy_f32_d5(v, a);
-    return s->precision == SKS_FP64 ? pipe_occupancy_f64(v, a) : pipe_occupancy_f32(v, a);
+    OccOf o{s, v, true};
+    return with_degree(s->m.hpn, o);
 }
 
-// the tunings compiled for a degree: every one for 4; for 5, 4 warps per CTA
-// and register cap 0 or 1
+// one step launch (C == nullptr) or one pipelined chunk of the solver's form T
+// and degree
+template <typename T>
+struct StepOf {
+    const sks_solver* s;
+    const StepVariant& v;
+    const Field<T>& F;
+    const Geo<T>& G;
+    const PipeChunk* C;
+    const PipeCtl* ctl;
+    template <int D>
+    cudaError_t run()
+    {
+        static thread_local Coef<T, D> k;
+        k = make_coef<T, D>(s->m);
+        const bool a = s->m.anisotropic != 0;
+        if (C) return DegKernels<T, D>::pipe(v, a, s->pipe_blocks, s->stream, F, G, k, *C, *ctl);
+        return DegKernels<T, D>::step(v, a, s->nblocks, s->stream, F, G, k);
+    }
+};
+
+// the tunings compiled for a degree: every one for 4; for 3, 5 and 6, 4
+// warps per CTA and register cap 0 or 1
 bool tuning_compiled(int hpn, int NW, int CAP) { return hpn == 4 || (NW == 4 && CAP <= 1); }
 
 int set_grid(sks_solver* s, int NW, int HZ, int ZS, int CAP, int WAVES, int PIPE)
@@ -398,25 +496,8 @@ int step_impl(sks_solver* s, int it, const T* dline, float* seis_row)
     {
         KTimer t(s, SKS_KC_ELEMENT);
         const StepVariant v{s->NW, s->ZS, s->CAP, s->m.nh_att > 0};
-        if (m.hpn == 5) {
-            static thread_local Coef<T, 5> k5;
-            k5 = make_coef<T, 5>(m);
-            if (sizeof(T) == 4)
-                launch_step_f32_d5(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<float>*)&F,
-                                   *(const Geo<float>*)&G, *(const Coef<float, 5>*)&k5);
-            else
-                launch_step_f64_d5(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<double>*)&F,
-                                   *(const Geo<double>*)&G, *(const Coef<double, 5>*)&k5);
-        } else {
-            static thread_local Coef<T> k;
-            k = make_coef<T>(m);
-            if (sizeof(T) == 4)
-                launch_step_f32(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<float>*)&F,
-                                *(const Geo<float>*)&G, *(const Coef<float>*)&k);
-            else
-                launch_step_f64(v, m.anisotropic != 0, s->nblocks, s->stream, *(const Field<double>*)&F,
-                                *(const Geo<double>*)&G, *(const Coef<double>*)&k);
-        }
+        StepOf<T> f{s, v, F, G, nullptr, nullptr};
+        with_degree(m.hpn, f);
     }
     s->cur = 1 - s->cur;
     return SKS_OK;
@@ -483,34 +564,16 @@ int pipe_impl(sks_solver* s, int it1, int cnt, int i0)
     C.snap_incre = m.snap_incre;
     C.nsnap = s->nsnap;
     C.snap_size = s->snap_size;
-    const PipeCtl ctl{s->pipe_ctl, s->pipe_ctl + 2, s->pipe_ctl + 1};
+    const PipeCtl ctl{s->pipe_ctl, s->pipe_ctl + 2, s->pipe_ctl + 1, s->test_stall ? s->test_spins : PIPE_SPIN_LIMIT,
+                      s->test_stall - 1};
     const int ntiles = s->ncx * s->ncz;
     CK(cudaMemsetAsync(ctl.claim, 0, sizeof(int), s->stream));
     CK(cudaMemsetAsync(ctl.done, 0, sizeof(int) * (size_t)ntiles, s->stream));
     {
         KTimer t(s, SKS_KC_ELEMENT);
         const StepVariant v{s->NW, s->ZS, s->CAP, s->m.nh_att > 0};
-        cudaError_t e;
-        if (m.hpn == 5) {
-            static thread_local Coef<T, 5> k5;
-            k5 = make_coef<T, 5>(m);
-            if (sizeof(T) == 4)
-                e = launch_pipe_f32_d5(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<float>*)&F,
-                                       *(const Geo<float>*)&G, *(const Coef<float, 5>*)&k5, C, ctl);
-            else
-                e = launch_pipe_f64_d5(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<double>*)&F,
-                                       *(const Geo<double>*)&G, *(const Coef<double, 5>*)&k5, C, ctl);
-        } else {
-            static thread_local Coef<T> k;
-            k = make_coef<T>(m);
-            if (sizeof(T) == 4)
-                e = launch_pipe_f32(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<float>*)&F,
-                                    *(const Geo<float>*)&G, *(const Coef<float>*)&k, C, ctl);
-            else
-                e = launch_pipe_f64(v, m.anisotropic != 0, s->pipe_blocks, s->stream, *(const Field<double>*)&F,
-                                    *(const Geo<double>*)&G, *(const Coef<double>*)&k, C, ctl);
-        }
-        CK(e);
+        StepOf<T> f{s, v, F, G, &C, &ctl};
+        CK(with_degree(m.hpn, f));
     }
     s->cur = (it1 + cnt - 1) & 1;
     return SKS_OK;
@@ -589,7 +652,7 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
     delete su;
     int rc = SKS_OK;
     const sks_model& m = s->m;
-    if (m.hpn != 4 && m.hpn != 5) { sks_model_free(&s->m); delete s; return set_err(SKS_ERR_UNSUPPORTED, "hpn=%d: the kernels are built for GLL degrees 4 and 5", m.hpn); }
+    if (m.hpn < 3 || m.hpn > 6) { sks_model_free(&s->m); delete s; return set_err(SKS_ERR_UNSUPPORTED, "hpn=%d: the kernels are built for GLL degrees 3 to 6", m.hpn); }
     s->precision = precision;
     s->device = device;
     s->nbl = m.neh * m.hpn;
@@ -688,6 +751,26 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         }
         if (ce != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "copy stream/events: %s", cudaGetErrorString(ce));
     }
+    if (!rc) {
+        // element rows whose points are all of isotropic materials (the
+        // anisotropic step kernels take the isotropic stress there)
+        std::vector<uint8_t> iso((size_t)m.nez, 1);
+        std::vector<uint8_t> mat_iso((size_t)m.nmat);
+        for (int i = 0; i < m.nmat; i++) mat_iso[i] = (uint8_t)sks_material_is_isotropic(m.mat + (size_t)i * SKS_MAT_STRIDE);
+        for (int ez = 0; ez < m.nez; ez++)
+            for (int iz = ez * m.hpn; iz <= ez * m.hpn + m.hpn && iso[ez]; iz++)
+                for (int ix = 0; ix < m.nx; ix++)
+                    if (!mat_iso[m.mat_id[(size_t)iz * m.nx + ix]]) { iso[ez] = 0; break; }
+        rc = dmalloc(s, &s->row_iso, iso.size());
+        if (!rc && cudaMemcpy(s->row_iso, iso.data(), iso.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = set_err(SKS_ERR_CUDA, "upload of the isotropic element rows");
+    }
+    if (!rc) rc = dmalloc(s, &s->nonfinite, 1);
+    if (!rc && cudaMemset(s->nonfinite, 0, sizeof(int)) != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "wavefield flag");
+    if (!rc && cudaMallocHost((void**)&s->hflags, 2 * sizeof(int)) != cudaSuccess) {
+        s->hflags = nullptr;
+        rc = set_err(SKS_ERR_NOMEM, "pinned host flags");
+    }
     if (!rc) rc = dmalloc(s, &s->G, (size_t)(s->chunk + 2) * (m.mtotal + m.shtotal));
     if (!rc) {
         const size_t nline = (size_t)(m.nx - s->nbl) + (m.nz - s->nbl - 1);
@@ -724,7 +807,14 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
                 rc = set_err(SKS_ERR_CUDA, "snapshot buffers");
         }
     }
-    if (rc) { free_device(s); cudaStreamDestroy(s->stream); sks_model_free(&s->m); delete s; return rc; }
+    if (rc) {
+        free_device(s);
+        if (s->hflags) cudaFreeHost(s->hflags);
+        cudaStreamDestroy(s->stream);
+        sks_model_free(&s->m);
+        delete s;
+        return rc;
+    }
     s->boundary_ready = (m.nt_sem == 0);
     *out = s;
     return SKS_OK;
@@ -997,20 +1087,40 @@ extern "C" int sks_run(sks_solver* s, int32_t nsteps, float* su, float* sv, floa
         if (rc) return rc;
     }
     CK(cudaEventRecord(s->run_ev[1], s->stream));
+    // the run's flags, read with the final synchronisation
+    s->hflags[0] = s->hflags[1] = 0;
+    CK(cudaMemcpyAsync(s->hflags, s->nonfinite, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    if (s->PIPE) CK(cudaMemcpyAsync(s->hflags + 1, s->pipe_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     CK(cudaStreamSynchronize(s->copy_stream));
     s->slot_busy[0] = s->slot_busy[1] = false;
-    if (s->PIPE) {
-        int err = 0;
-        CK(cudaMemcpy(&err, s->pipe_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost));
-        if (err) return set_err(SKS_ERR_CUDA, "pipelined step: a wait for neighbouring tiles ran out");
-    }
+    s->test_stall = 0;
     {
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, s->run_ev[0], s->run_ev[1]));
         s->last_run_ms = ms;
     }
+    if (s->hflags[1]) return set_err(SKS_ERR_CUDA, "pipelined step: a wait for neighbouring tiles ran out");
+    if (s->hflags[0])
+        return set_err(SKS_ERR_NONFINITE, "the wavefield holds a non-finite displacement (steps up to %d)", s->step - 1);
     return total;
+}
+
+extern "C" int sks_wavefield_finite(const sks_solver* s)
+{
+    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    return s->hflags[0] ? 0 : 1;
+}
+
+extern "C" int sks_test_stall_pipeline(sks_solver* s, int32_t tile, int32_t spin_limit)
+{
+    if (!s) return set_err(SKS_ERR_ARG, "solver is NULL");
+    if (!s->PIPE) return set_err(SKS_ERR_STATE, "the solver does not run pipelined chunks (tuning pipeline=0)");
+    if (tile < 0 || tile >= s->ncx * s->ncz) return set_err(SKS_ERR_ARG, "tile %d: 0..%d", tile, s->ncx * s->ncz - 1);
+    if (spin_limit < 1 || spin_limit > PIPE_SPIN_LIMIT) return set_err(SKS_ERR_ARG, "spin_limit=%d: 1..%d", spin_limit, PIPE_SPIN_LIMIT);
+    s->test_stall = tile + 1;
+    s->test_spins = spin_limit;
+    return SKS_OK;
 }
 
 extern "C" int sks_reset(sks_solver* s)
@@ -1021,6 +1131,10 @@ extern "C" int sks_reset(sks_solver* s)
     s->cur = 0;
     s->g_last = 0;
     for (bool& t : s->snap_taken) t = false;
+    cudaSetDevice(s->device);
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemset(s->nonfinite, 0, sizeof(int)));
+    s->hflags[0] = 0;
     return SKS_OK;
 }
 
@@ -1122,6 +1236,8 @@ extern "C" int sks_state_load(sks_solver* s, const void* host, int64_t bytes)
     s->cur = h.cur;
     s->g_last = 0;
     for (int k = 0; k < SKS_NSNAP; k++) s->snap_taken[k] = h.snap_taken[k] != 0;
+    CK(cudaMemset(s->nonfinite, 0, sizeof(int)));
+    s->hflags[0] = 0;
     return SKS_OK;
 }
 
@@ -1171,6 +1287,7 @@ extern "C" void sks_destroy(sks_solver* s)
     if (s->copy_stream) { cudaStreamSynchronize(s->copy_stream); cudaStreamDestroy(s->copy_stream); }
     if (s->run_ev[0]) { cudaEventDestroy(s->run_ev[0]); cudaEventDestroy(s->run_ev[1]); }
     if (s->stream) cudaStreamDestroy(s->stream);
+    if (s->hflags) cudaFreeHost(s->hflags);
     sks_model_free(&s->m);
     delete s;
 }

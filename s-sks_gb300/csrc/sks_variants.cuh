@@ -32,10 +32,10 @@ auto visit_variant(const StepVariant& v, bool aniso, V& vis)
     return aniso ? visit_nw<true>(v, vis) : visit_nw<false>(v, vis);
 }
 
-// Degree 5 compiles the 4-warp variants with register cap 0 or 1 only (the
-// tunings the solver allows for it).
+// Degrees other than 4 (3, 5, 6) compile the 4-warp variants with register
+// cap 0 or 1 only (the tunings the solver allows for them).
 template <bool A, bool ZS, typename V>
-auto visit_deg5_cap(const StepVariant& v, V& vis)
+auto visit_deg_cap(const StepVariant& v, V& vis)
 {
     return v.cap ? vis.template run<A, 4, ZS, 1>() : vis.template run<A, 4, ZS, 0>();
 }
@@ -43,9 +43,9 @@ auto visit_deg5_cap(const StepVariant& v, V& vis)
 template <int DEG, typename V>
 auto visit_deg(const StepVariant& v, bool aniso, V& vis)
 {
-    if constexpr (DEG == 5) {
-        if (aniso) return v.zseam ? visit_deg5_cap<true, true>(v, vis) : visit_deg5_cap<true, false>(v, vis);
-        return v.zseam ? visit_deg5_cap<false, true>(v, vis) : visit_deg5_cap<false, false>(v, vis);
+    if constexpr (DEG != N) {
+        if (aniso) return v.zseam ? visit_deg_cap<true, true>(v, vis) : visit_deg_cap<true, false>(v, vis);
+        return v.zseam ? visit_deg_cap<false, true>(v, vis) : visit_deg_cap<false, false>(v, vis);
     } else {
         return visit_variant(v, aniso, vis);
     }

@@ -27,6 +27,7 @@ ERRORS = {0: "OK", -1: "ERR_ARG", -2: "ERR_IO", -3: "ERR_MODEL", -4: "ERR_UNSUPP
           -6: "ERR_NOMEM", -7: "ERR_BOUNDARY", -8: "ERR_STATE", -9: "ERR_NONFINITE"}
 
 EXPORTS = ["sks_open_par", "sks_load_boundary_files", "sks_set_boundary", "sks_run", "sks_reset",
+           "sks_wavefield_finite", "sks_test_stall_pipeline", "sks_batch_test_stall_pipeline",
            "sks_get_info", "sks_setup_open", "sks_setup_info", "sks_setup_material", "sks_setup_mass",
            "sks_setup_receivers", "sks_setup_schedule", "sks_setup_close", "sks_open_setup",
            "sks_kernel_launches", "sks_last_run_ms", "sks_enable_kernel_timing", "sks_kernel_timing",
@@ -140,6 +141,9 @@ def lib() -> C.CDLL:
         L.sks_set_boundary.argtypes = [vp, fp, C.c_int32, fp, C.c_int32]
         L.sks_run.argtypes = [vp, C.c_int32, fp, fp, fp]
         L.sks_reset.argtypes = [vp]
+        L.sks_wavefield_finite.argtypes = [vp]
+        L.sks_test_stall_pipeline.argtypes = [vp, C.c_int32, C.c_int32]
+        L.sks_batch_test_stall_pipeline.argtypes = [vp, C.c_int32, C.c_int32]
         L.sks_get_info.argtypes = [vp, C.POINTER(Info)]
         L.sks_setup_open.argtypes = [C.c_int, argv_t, C.POINTER(vp)]
         L.sks_setup_info.argtypes = [vp, C.POINTER(Info)]
@@ -358,6 +362,14 @@ class Solver:
     def reset(self):
         _check(lib().sks_reset(self.h))
 
+    def wavefield_finite(self) -> bool:
+        """False once a step produced a non-finite displacement (until reset)."""
+        return _check(lib().sks_wavefield_finite(self.h)) == 1
+
+    def test_stall_pipeline(self, tile: int, spin_limit: int):
+        """Failure-path tests only: the next run's pipelined wait on `tile` runs out."""
+        _check(lib().sks_test_stall_pipeline(self.h, tile, spin_limit))
+
     def save_state(self) -> np.ndarray:
         n = _check(lib().sks_state_bytes(self.h))
         buf = np.zeros(n, np.uint8)
@@ -454,8 +466,9 @@ class Batch:
     def __len__(self) -> int:
         return _check(lib().sks_batch_size(self.h))
 
-    def run(self, nsteps: int, want: bool = True):
-        """Advance every member; returns per member (u, v, w) of the rows it took."""
+    def run(self, nsteps: int, want: bool = True, status: bool = False):
+        """Advance every member; returns per member (u, v, w) of the rows it took
+        (with status=True: (that list, the call's status) instead of raising)."""
         infos = [m.info() for m in self.members]
         n = len(self.members)
         fpp = C.POINTER(C.c_float) * max(1, n)
@@ -466,8 +479,15 @@ class Batch:
             outs.append(o)
             for c in range(3):
                 arrs[c][i] = _f32(o[c]) if want and o[c].size else None
-        _check(lib().sks_batch_run(self.h, nsteps, arrs[0], arrs[1], arrs[2]))
+        rc = lib().sks_batch_run(self.h, nsteps, arrs[0], arrs[1], arrs[2])
+        if status:
+            return outs, rc
+        _check(rc)
         return outs
+
+    def test_stall_pipeline(self, tile: int, spin_limit: int):
+        """Failure-path tests only: the next run's pipelined wait on `tile` runs out."""
+        _check(lib().sks_batch_test_stall_pipeline(self.h, tile, spin_limit))
 
     def tuning(self) -> dict:
         t = Tuning()

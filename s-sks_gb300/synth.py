@@ -218,9 +218,12 @@ def ricker(t: np.ndarray, f0: float) -> np.ndarray:
     return (1.0 - 2.0 * a) * np.exp(-a)
 
 
+GLL3 = (-1.0, -0.4472135954999579, 0.4472135954999579, 1.0)         # GLL points of degree 3: +-1/sqrt(5)
 GLL4 = (-1.0, -0.6546536707079771, 0.0, 0.6546536707079771, 1.0)    # GLL points of degree 4
 GLL5 = (-1.0, -0.7650553239294647, -0.2852315164806451, 0.2852315164806451, 0.7650553239294647, 1.0)
-GLL_POINTS = {4: GLL4, 5: GLL5}
+# degree 6: 0 and +-sqrt((15 -+ 2 sqrt(15))/33)
+GLL6 = (-1.0, -0.8302238962785669, -0.46884879347071423, 0.0, 0.46884879347071423, 0.8302238962785669, 1.0)
+GLL_POINTS = {3: GLL3, 4: GLL4, 5: GLL5, 6: GLL6}
 
 
 def gll_positions(n: int, eh: float, deg: int = 4) -> np.ndarray:

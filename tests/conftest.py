@@ -21,7 +21,7 @@ def built():
     import sks_build
     from oracle import oracle as orc
     sks_build.build()
-    orc.build(None)
+    orc.build(with_reference=False)
     yield
 
 

@@ -77,6 +77,13 @@ CASES = {
     "psvsh_hpn5": dict(prog="sem2d_psvsh", case=lambda: synth.Case(
         nex=12, nez=7, eh=2.5, sdt=0.01, nst=640, layers=aniso_layers(17.5, 50.0), p=0.05, f0=1.0,
         sv_amp=1.0, sh_amp=0.6, hpn=5, ntrace=7, rec_x0=1.0, rec_dx=4.0)),
+    # GLL degrees 3 and 6, the ends of the range the reference accepts (lagrange.c:323-328)
+    "psvsh_hpn3": dict(prog="sem2d_psvsh", case=lambda: synth.Case(
+        nex=16, nez=9, eh=2.0, sdt=0.01, nst=700, layers=aniso_layers(18.0, 35.0), p=0.05, f0=1.0,
+        sv_amp=1.0, sh_amp=0.6, hpn=3, ntrace=7, rec_x0=1.0, rec_dx=4.0)),
+    "psvsh_hpn6": dict(prog="sem2d_psvsh", case=lambda: synth.Case(
+        nex=10, nez=6, eh=3.0, sdt=0.008, nst=800, layers=aniso_layers(18.0, 55.0), p=0.05, f0=1.0,
+        sv_amp=1.0, sh_amp=0.6, hpn=6, ntrace=7, rec_x0=1.0, rec_dx=4.0)),
     # snapshots (plot_snap): the reference's text files out1..outK
     "psvsh_snap": dict(prog="sem2d_psvsh", words=["plot_snap=1", "startsnap=40", "incresnap=60"],
                        case=lambda: synth.Case(

@@ -61,6 +61,13 @@ CASES = {
     "hpn5_aniso": lambda: synth.Case(nex=23, nez=8, eh=2.0, sdt=0.008, nst=900, layers=_aniso_layers(16.0),
                                      p=0.05, f0=1.0, sv_amp=1.0, sh_amp=0.5, hpn=5, ntrace=9, rec_x0=1.0,
                                      rec_dx=4.5, semmodel_full=True),
+    # GLL degrees 3 (7 elements per warp) and 6 (4 elements per warp)
+    "hpn3_aniso": lambda: synth.Case(nex=27, nez=9, eh=1.5, sdt=0.008, nst=900, layers=_aniso_layers(13.5),
+                                     p=0.05, f0=1.2, sv_amp=1.0, sh_amp=0.5, hpn=3, ntrace=9, rec_x0=1.0,
+                                     rec_dx=4.0, semmodel_full=True),
+    "hpn6_aniso": lambda: synth.Case(nex=17, nez=7, eh=2.5, sdt=0.006, nst=1100, layers=_aniso_layers(17.5),
+                                     p=0.05, f0=1.0, sv_amp=1.0, sh_amp=0.5, hpn=6, ntrace=9, rec_x0=1.0,
+                                     rec_dx=4.5, semmodel_full=True),
     "flat0_raymodel_xbeg": lambda: synth.Case(nex=20, nez=8, eh=2.0, sdt=0.01, nst=700,
                                               layers=synth.layered_two(16.0, 5.0), p=0.04, f0=1.0, flat=0,
                                               readpars=0, get_rec=0, ntrace=6, sh_amp=0.4,
@@ -153,12 +160,14 @@ def test_taper_under_every_grid_and_in_a_batch(casedirs, prec):
         assert np.array_equal(got[i], ref[i]), i
 
 
+@pytest.mark.parametrize("deg", [3, 5, 6])
 @pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])
-def test_degree5_tunings_bit_identical_and_refusals(casedirs, prec):
-    """Degree 5 compiles 4-warp CTAs with register cap 0 or 1: every such grid
-    (seams or halo rows, per-step or pipelined, balanced waves) gives the same
-    bits; other tunings are refused, and so is degree 6."""
-    d, c, _ = casedirs["hpn5_aniso"]
+def test_other_degrees_tunings_bit_identical_and_refusals(casedirs, prec, deg):
+    """Degrees 3, 5 and 6 compile 4-warp CTAs with register cap 0 or 1: every
+    such grid (seams or halo rows, per-step or pipelined, balanced waves)
+    gives the same bits; other tunings are refused; batches take degree 5 and
+    refuse 3 and 6."""
+    d, c, _ = casedirs[f"hpn{deg}_aniso"]
     ref = None
     with chdir(d):
         for t in ((4, 3, 0, 0, 0, 0), (4, 1, 1, 1, 0, 0), (4, 8, 0, 1, 0, 1), (4, 2, 1, 0, 0, 1), (4, 4, 0, 1, 2, 0)):
@@ -176,10 +185,15 @@ def test_degree5_tunings_bit_identical_and_refusals(casedirs, prec):
                     s.set_tuning(*bad)
             s.load_boundary_files()
             with sks.Batch(prec) as b:
-                b.add(s)                                # batches take degree 5 too
-                b.remove(s)
+                if deg == 5:
+                    b.add(s)                            # batches take degree 5 too
+                    b.remove(s)
+                else:
+                    with pytest.raises(sks.SksError) as e:
+                        b.add(s)
+                    assert e.value.code == -4
         with pytest.raises(sks.SksError):
-            sks.Solver(["par=run.par", "hpn=6"], precision=prec)
+            sks.Solver(["par=run.par", "hpn=7"], precision=prec)
 
 
 @pytest.mark.parametrize("prec", [sks.FP64, sks.FP32C])

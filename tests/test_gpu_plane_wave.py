@@ -22,7 +22,9 @@ def _case(tmp_path, psv_only=False, sh_amp=0.6, hpn=4):
     layers = [synth.SemLayer(H - 6, synth.iso_cij(8.1, 4.5, 3.4), 3.4),
               synth.SemLayer(H - 3, synth.hexagonal_cij(8.1, 4.5, 3.4, 0.05, 30.0, 15.0), 3.4),
               synth.SemLayer(H + 1, synth.iso_cij(6.4, 3.6, 2.8), 2.8)]
-    c = synth.Case(nex=29, nez=12, eh=1.0, sdt=0.005, nst=700, layers=layers, p=0.044, f0=1.3, sv_amp=1.0,
+    # degree 6's closest GLL nodes are 85 m apart in a 1 km element: a shorter step keeps it stable
+    sdt, nst = (0.0035, 900) if hpn == 6 else (0.005, 700)
+    c = synth.Case(nex=29, nez=12, eh=1.0, sdt=sdt, nst=nst, layers=layers, p=0.044, f0=1.3, sv_amp=1.0,
                    sh_amp=sh_amp, ntrace=13, rec_dx=2.0, semmodel_full=True, write_records=False,
                    psv_only=psv_only, hpn=hpn)
     d = str(tmp_path)
@@ -30,7 +32,7 @@ def _case(tmp_path, psv_only=False, sh_amp=0.6, hpn=4):
     return d, c, float(np.sqrt(layers[0].C[3, 3] / layers[0].rho))
 
 
-@pytest.mark.parametrize("psv_only,hpn", [(False, 4), (True, 4), (False, 5)])
+@pytest.mark.parametrize("psv_only,hpn", [(False, 4), (True, 4), (False, 5), (False, 3), (False, 6)])
 def test_device_records_match_host_generator(tmp_path, psv_only, hpn):
     d, c, vs = _case(tmp_path, psv_only, hpn=hpn)
     sh_amp = 0.0 if psv_only else c.sh_amp
