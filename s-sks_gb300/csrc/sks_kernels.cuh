@@ -219,10 +219,10 @@ struct MatRow<T, false> {
 
 // stress on the strain list (e11, e12=u_y,x, e13=u_z,x+u_x,z, e23=u_y,z, e33):
 // sigma_a = sum_b C[a][b] e_b in b order, as Stress_ij (sem2d_psvsh.c:1345-1380).
-// iso (anisotropic kernels, an element row of isotropic materials only): the
-// isotropic form, which gives the anisotropic sums' values for an isotropic
-// material (the zero entries' products add nothing; C33 = C11, C55 = C44 =
-// C66), with 7 operations instead of 25
+// iso (anisotropic FP64 kernels, an element row of isotropic materials only):
+// the isotropic form, which gives the anisotropic sums' values for an
+// isotropic material (the zero entries' products add nothing but the sign of
+// an exact zero; C33 = C11, C55 = C44 = C66), with 7 operations instead of 25
 template <typename T, bool ANISO>
 __device__ __forceinline__ void stress(const MatRow<T, ANISO>& M, const T e[5], T s[5], bool iso = false)
 {
@@ -532,7 +532,10 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
                 m[b] = F.mid[g];
             }
         }
-        const bool iso_row = ANISO && F.row_iso[ez];
+        // FP64 only: there it saves 36 of the ~276 flops of a point on the
+        // FP64 pipe the form is bound by (8 % of the step on the 3.8 M-point
+        // mesh); the FP32 form is issue-bound and measured 1 % slower with it
+        const bool iso_row = ANISO && sizeof(T) == 8 && F.row_iso[ez];
         Aux<T, LF> aux[N];
         if (!halo && own_x) {
 #pragma unroll
