@@ -63,6 +63,8 @@ typedef struct {
     int64_t seam_points;          /* points shared by warp tiles          */
     int32_t tile_rows;            /* element rows per CTA band            */
     int32_t neh;                  /* interface line offset in elements    */
+    int32_t iso_rows;             /* element rows whose points are all of
+                                     isotropic materials                  */
 } sks_info_t;
 
 /* Replaces main() of sem2d_psvsh up to its time loop (sem2d_psvsh.c:82-416):

@@ -42,9 +42,26 @@ extern "C" __attribute__((visibility("hidden"))) int sks_internal_set_error(int 
 }
 
 
+// per element row: 1 when every point of its grid rows has an isotropic material
+static std::vector<uint8_t> isotropic_rows(const sks_model& m)
+{
+    std::vector<uint8_t> iso((size_t)m.nez, 1);
+    std::vector<uint8_t> mat_iso((size_t)m.nmat);
+    for (int i = 0; i < m.nmat; i++) mat_iso[i] = (uint8_t)sks_material_is_isotropic(m.mat + (size_t)i * SKS_MAT_STRIDE);
+    for (int ez = 0; ez < m.nez; ez++)
+        for (int iz = ez * m.hpn; iz <= ez * m.hpn + m.hpn && iso[ez]; iz++)
+            for (int ix = 0; ix < m.nx; ix++)
+                if (!mat_iso[m.mat_id[(size_t)iz * m.nx + ix]]) { iso[ez] = 0; break; }
+    return iso;
+}
+
 static void fill_info(const sks_model& m, sks_info_t* info)
 {
     memset(info, 0, sizeof *info);
+    {
+        const std::vector<uint8_t> iso = isotropic_rows(m);
+        for (uint8_t v : iso) info->iso_rows += v;
+    }
     info->nex = m.nex; info->nez = m.nez; info->hpn = m.hpn;
     info->nx = m.nx; info->nz = m.nz; info->nst = m.nst; info->nt_inject = m.nt_sem;
     info->ntrace = m.ntrace; info->mtotal = m.mtotal; info->shtotal = m.shtotal;
@@ -753,14 +770,8 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
     }
     if (!rc) {
         // element rows whose points are all of isotropic materials (the
-        // anisotropic step kernels take the isotropic stress there)
-        std::vector<uint8_t> iso((size_t)m.nez, 1);
-        std::vector<uint8_t> mat_iso((size_t)m.nmat);
-        for (int i = 0; i < m.nmat; i++) mat_iso[i] = (uint8_t)sks_material_is_isotropic(m.mat + (size_t)i * SKS_MAT_STRIDE);
-        for (int ez = 0; ez < m.nez; ez++)
-            for (int iz = ez * m.hpn; iz <= ez * m.hpn + m.hpn && iso[ez]; iz++)
-                for (int ix = 0; ix < m.nx; ix++)
-                    if (!mat_iso[m.mat_id[(size_t)iz * m.nx + ix]]) { iso[ez] = 0; break; }
+        // anisotropic FP64 step kernels take the isotropic stress there)
+        const std::vector<uint8_t> iso = isotropic_rows(m);
         rc = dmalloc(s, &s->row_iso, iso.size());
         if (!rc && cudaMemcpy(s->row_iso, iso.data(), iso.size(), cudaMemcpyHostToDevice) != cudaSuccess)
             rc = set_err(SKS_ERR_CUDA, "upload of the isotropic element rows");

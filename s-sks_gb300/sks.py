@@ -62,7 +62,7 @@ class Info(C.Structure):
                                          "mtotal", "shtotal", "nrec_psv", "nrec_sh", "nmat", "anisotropic",
                                          "precision", "step")] + \
                [("eh", C.c_double), ("h", C.c_double), ("sdt", C.c_double), ("device_bytes", C.c_int64),
-                ("seam_points", C.c_int64), ("tile_rows", C.c_int32), ("neh", C.c_int32)]
+                ("seam_points", C.c_int64), ("tile_rows", C.c_int32), ("neh", C.c_int32), ("iso_rows", C.c_int32)]
 
     def asdict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
