@@ -111,8 +111,10 @@ struct sks_solver {
     // flag, [1] the pipelined chunks' wait-ran-out flag
     int* nonfinite;
     int* hflags;
-    // per element row: 1 when all its points are of isotropic materials
+    // per element row: 1 when all its points are of isotropic materials; the
+    // material all its points share, or -1
     uint8_t* row_iso;
+    int16_t* row_mat;
     // failure-path tests (sks_test_stall_pipeline): for the next run, tile
     // test_stall-1 of the pipelined chunks never marks a step finished and a
     // wait gives up after test_spins polls; 0 = off
@@ -186,6 +188,7 @@ Field<T> make_field(sks_solver* s)
     F.snap_nzs = (s->m.nz + 1) / 2;
     F.nonfinite = s->nonfinite;
     F.row_iso = s->row_iso;
+    F.row_mat = s->row_mat;
     return F;
 }
 

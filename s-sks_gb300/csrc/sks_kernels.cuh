@@ -133,6 +133,9 @@ struct Field {
     // per element row: 1 when every point of its grid rows has an isotropic
     // material (the anisotropic kernels take the isotropic stress there)
     const uint8_t* __restrict__ row_iso;
+    // per element row: the material of all its points when they share one
+    // (layered models: nearly every row), else -1 (read per point from mid)
+    const int16_t* __restrict__ row_mat;
 };
 
 // Displacement layout: the P-SV pair (u_x, u_z) of every point as one 2-vector
@@ -510,27 +513,41 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
 
     {
         const int o = ezs * N * nx + ix;
+        const int rm = F.row_mat[ezs];
 #pragma unroll
-        for (int b = 0; b < NP; b++) {
-            const int g = o + b * nx;
-            load_u<T, CG>(F.uc, np, g, u[b]);
-            m[b] = F.mid[g];
+        for (int b = 0; b < NP; b++) load_u<T, CG>(F.uc, np, o + b * nx, u[b]);
+        if (rm < 0) {
+#pragma unroll
+            for (int b = 0; b < NP; b++) m[b] = F.mid[o + b * nx];
+        } else {
+#pragma unroll
+            for (int b = 0; b < NP; b++) m[b] = (uint16_t)rm;
         }
     }
     int par = 0;
     for (int ez = ezs; ez < ez1; ++ez) {
         const bool halo = !ZS && ez < ez0;
+        // the element row's material when all its points share one: no
+        // per-point material index to read or compare
+        const int rm = F.row_mat[ez];
         if (ez > ezs) {
 #pragma unroll
             for (int c = 0; c < 3; c++) u[0][c] = u[N][c];
             m[0] = m[N];
             const int o = ez * N * nx + ix;
 #pragma unroll
-            for (int b = 1; b < NP; b++) {
-                const int g = o + b * nx;
-                load_u<T, CG>(F.uc, np, g, u[b]);
-                m[b] = F.mid[g];
+            for (int b = 1; b < NP; b++) load_u<T, CG>(F.uc, np, o + b * nx, u[b]);
+            if (rm < 0) {
+#pragma unroll
+                for (int b = 1; b < NP; b++) m[b] = F.mid[o + b * nx];
+            } else {
+#pragma unroll
+                for (int b = 1; b < NP; b++) m[b] = (uint16_t)rm;
             }
+        }
+        if (rm >= 0 && rm != mcur) {
+            M.load(F.mat + (size_t)rm * MAT_STRIDE);
+            mcur = rm;
         }
         // FP64 only: there it saves 36 of the ~276 flops of a point on the
         // FP64 pipe the form is bound by (8 % of the step on the 3.8 M-point
@@ -562,7 +579,7 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
                 dz[c] = z;
             }
             const T ee[5] = {dx[0], dx[1], dx[2] + dz[0], dz[1], dz[2]};
-            if ((int)m[bb] != mcur) {                // layered models: rarely taken
+            if (rm < 0 && (int)m[bb] != mcur) {      // rows across a material boundary
                 M.load(F.mat + (size_t)m[bb] * MAT_STRIDE);
                 mcur = m[bb];
             }

@@ -156,7 +156,7 @@ void free_device(sks_solver* s)
     void* ps[] = {s->U[0], s->U[1], s->Dv, s->Cc, s->mid, s->mat, s->stc, s->taper,
                   s->rec_off, s->recbits, s->rec_sorted, s->rec_idx, s->seisbuf[0], s->seisbuf[1], s->G, s->Dl, s->rec_psv, s->rec_sh,
                   s->tap_psv, s->tap_sh, s->w_psv, s->w_sh, s->seam_lo, s->seam_hi, s->seam_cnt, s->items, s->seis_full,
-                  s->pipe_ctl, s->snaps, s->ser, s->nonfinite, s->row_iso};
+                  s->pipe_ctl, s->snaps, s->ser, s->nonfinite, s->row_iso, s->row_mat};
     for (void* p : ps)
         if (p) cudaFree(p);
     s->U[0] = s->U[1] = s->Dv = s->Cc = s->mat = s->stc = s->taper = nullptr;
@@ -172,6 +172,7 @@ void free_device(sks_solver* s)
     s->snaps = nullptr;
     s->nonfinite = nullptr;
     s->row_iso = nullptr;
+    s->row_mat = nullptr;
 }
 
 // per-kernel-class timing: an event pair around each launch when enabled
@@ -775,6 +776,20 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         rc = dmalloc(s, &s->row_iso, iso.size());
         if (!rc && cudaMemcpy(s->row_iso, iso.data(), iso.size(), cudaMemcpyHostToDevice) != cudaSuccess)
             rc = set_err(SKS_ERR_CUDA, "upload of the isotropic element rows");
+        // element rows whose points share one material (-1: they do not)
+        std::vector<int16_t> rmat((size_t)m.nez);
+        for (int ez = 0; ez < m.nez; ez++) {
+            const uint16_t first = m.mat_id[(size_t)ez * m.hpn * m.nx];
+            int v = first < 32768 ? first : -1;
+            for (int iz = ez * m.hpn; iz <= ez * m.hpn + m.hpn && v >= 0; iz++)
+                for (int ix = 0; ix < m.nx; ix++)
+                    if (m.mat_id[(size_t)iz * m.nx + ix] != first) { v = -1; break; }
+            rmat[ez] = (int16_t)v;
+        }
+        if (!rc) rc = dmalloc(s, &s->row_mat, rmat.size());
+        if (!rc && cudaMemcpy(s->row_mat, rmat.data(), rmat.size() * sizeof(int16_t), cudaMemcpyHostToDevice) !=
+                       cudaSuccess)
+            rc = set_err(SKS_ERR_CUDA, "upload of the element rows' materials");
     }
     if (!rc) rc = dmalloc(s, &s->nonfinite, 1);
     if (!rc && cudaMemset(s->nonfinite, 0, sizeof(int)) != cudaSuccess) rc = set_err(SKS_ERR_CUDA, "wavefield flag");
