@@ -393,6 +393,7 @@ extern "C" int sks_batch_create(int precision, int device, sks_batch** out)
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev[0]);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev[1]);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&b->herr, sizeof(int));
+    if (e == cudaSuccess) *b->herr = 0;
     if (e != cudaSuccess) {
         if (b->stream) cudaStreamDestroy(b->stream);
         if (b->herr) cudaFreeHost(b->herr);

@@ -797,6 +797,7 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         s->hflags = nullptr;
         rc = set_err(SKS_ERR_NOMEM, "pinned host flags");
     }
+    if (!rc) s->hflags[0] = s->hflags[1] = 0;
     if (!rc) rc = dmalloc(s, &s->G, (size_t)(s->chunk + 2) * (m.mtotal + m.shtotal));
     if (!rc) {
         const size_t nline = (size_t)(m.nx - s->nbl) + (m.nz - s->nbl - 1);

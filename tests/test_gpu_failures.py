@@ -92,6 +92,7 @@ def test_nan_record_flags_the_solve_and_reset_clears_it(cases, prec):
     d, nst = cases[0]
     psv, sh = _records(d)
     with _open(d, prec) as s:
+        assert s.wavefield_finite()             # before any run
         ref = s.run(nst)
         assert s.wavefield_finite()
     assert max(np.abs(x).max() for x in ref) > 0.05
