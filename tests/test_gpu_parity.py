@@ -68,6 +68,14 @@ CASES = {
     "hpn6_aniso": lambda: synth.Case(nex=17, nez=7, eh=2.5, sdt=0.006, nst=1100, layers=_aniso_layers(17.5),
                                      p=0.05, f0=1.0, sv_amp=1.0, sh_amp=0.5, hpn=6, ntrace=9, rec_x0=1.0,
                                      rec_dx=4.5, semmodel_full=True),
+    # degree 3 with the boundary taper's bottom and left zones, degree 6 with the bottom, left and right
+    # ones (the top zone would hold the surface receivers)
+    "hpn3_atten2": lambda: synth.Case(nex=30, nez=12, eh=1.5, sdt=0.008, nst=900, layers=_aniso_layers(18.0),
+                                      p=0.05, f0=1.2, sv_amp=2.0, sh_amp=1.0, hpn=3, neh=2, ntrace=9, rec_x0=1.0,
+                                      rec_dx=4.0, semmodel_full=True, extra={"atten": 2, "ass": "0.9"}),
+    "hpn6_atten3": lambda: synth.Case(nex=18, nez=8, eh=2.5, sdt=0.006, nst=1100, layers=_aniso_layers(20.0),
+                                      p=0.05, f0=1.0, sv_amp=2.0, sh_amp=1.0, hpn=6, neh=2, ntrace=9, rec_x0=1.0,
+                                      rec_dx=4.5, semmodel_full=True, extra={"atten": 3, "ass": "0.85"}),
     "flat0_raymodel_xbeg": lambda: synth.Case(nex=20, nez=8, eh=2.0, sdt=0.01, nst=700,
                                               layers=synth.layered_two(16.0, 5.0), p=0.04, f0=1.0, flat=0,
                                               readpars=0, get_rec=0, ntrace=6, sh_amp=0.4,
