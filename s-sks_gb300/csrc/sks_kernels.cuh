@@ -328,7 +328,9 @@ __device__ __forceinline__ bool not_finite3(const double v[3])
 }
 
 // update one owned point, sample it if it is a receiver, then add the next
-// step's boundary increment if it lies on the interface line
+// step's boundary increment if it lies on the interface line.
+// M^-1 dt^2 = wxi * wzi * rinv: wxi is the column's inverse lumped-mass
+// weight times dt^2/Je, wzi the row's, rinv 1/rho.
 // plain: the CTA's tile holds no Stacey edge point, receiver, snapshot point,
 // interface-line point or taper zone (tile-uniform), so none of their tests runs
 template <typename T, bool LF, bool TP = false, int DEG = N>
@@ -341,7 +343,7 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
     T un[3], dn[3], cn[3];
     if (!LF) {
         if (!edge) {
-            const T mdt2 = G.dt2_Je * rinv * wxi * wzi;
+            const T mdt2 = (wxi * wzi) * rinv;   // wxi carries dt^2/Je
 #pragma unroll
             for (int c = 0; c < 3; c++) un[c] = (-mdt2 * K[c] + (T)2 * u[c]) - x.a[c];
         } else {
@@ -351,7 +353,7 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
         }
     } else {
         if (!edge) {
-            const T mdt2 = G.dt2_Je * rinv * wxi * wzi;
+            const T mdt2 = (wxi * wzi) * rinv;   // wxi carries dt^2/Je
 #pragma unroll
             for (int c = 0; c < 3; c++) dn[c] = fma(-mdt2, K[c], x.a[c]);
         } else {
@@ -502,7 +504,8 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
     const T wal = k.w[al];
     // lumped-mass weight of this lane's column: inside an element, on an
     // element edge shared by two elements, or on the box's left/right edge
-    const T wxi = (al > 0 && al < N) ? k.winv[al] : (pfl.edge_x ? k.winv[0] : k.winv2);
+    // times dt^2/Je: the lane's factor of the update's M^-1 dt^2
+    const T wxi = G.dt2_Je * ((al > 0 && al < N) ? k.winv[al] : (pfl.edge_x ? k.winv[0] : k.winv2));
 
     T u[NP][3];
     uint16_t m[NP];

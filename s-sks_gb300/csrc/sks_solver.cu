@@ -1426,7 +1426,7 @@ extern "C" int sks_autotune(sks_solver* s, int32_t steps, sks_tuning_t* best)
     const int old_timing = s->timing;
     s->timing = 0;
     const int nws[] = {2, 4};
-    const int hzs[] = {4, 6, 8, 12};
+    const int hzs[] = {4, 6, 8, 9, 12};
     sks_tuning_t b = {s->NW, s->HZ, s->ZS, s->CAP, s->WAVES, s->nblocks, 1e30f, s->PIPE};
     // fixed band heights, then balanced partitions of 1..3 waves; pipelined
     // chunks with fixed band heights
