@@ -45,8 +45,10 @@ FULL_STEPS = 24000
 # W x (3 u^n read + 3 u^(n-1) read + 3 u^(n+1) write + 1 inverse mass + 15 c_ij)
 # plus, for the compensated FP32 form, 4 B x 3 compensation words read and
 # written: 124 B (FP32C), 200 B (FP64).  The kernels move less than that (the
-# material is a 2-byte index into a table and the inverse mass is rebuilt from
-# GLL weights): 74 B per point in both forms (LAYOUT_BYTES_PER_POINT).
+# material is a 2-byte index into a table, read only on element rows of more
+# than one material, and the inverse mass is rebuilt from GLL weights): 72 B
+# per point in both forms on this mesh's one-material rows, 74 B on the few
+# others (LAYOUT_BYTES_PER_POINT: the former).
 BYTES_PER_POINT = {"fp32c": 124, "fp64": 200, "fp64_iso": 96}
 # algorithmic flops per grid-point update of the anisotropic step (an FMA is 2
 # flops, an n-term dot product 2n-1): per element row a GLL column does, for
@@ -57,7 +59,7 @@ BYTES_PER_POINT = {"fp32c": 124, "fp64": 200, "fp64_iso": 96}
 # (1.5) and the 3-level update (15)
 # isotropic: the 5x5 stress is 9 flops instead of 45, so 130 x 5 x 5 / 16 + 16.5
 FLOPS_PER_POINT = {"aniso": 276, "iso": 220}
-LAYOUT_BYTES_PER_POINT = {"fp32c": 74, "fp64": 74}
+LAYOUT_BYTES_PER_POINT = {"fp32c": 72, "fp64": 72}
 WORKLOAD = ("anisotropic 3-component SKS solve: 800x300 elements of 1 km, GLL degree 4, "
             "3,844,401 points, 100 km hexagonal layer (4 %, azimuth 45, tilt 20), dt 5 ms, 201 receivers")
 
@@ -933,7 +935,7 @@ def main() -> None:
     fma_peaks = {"fp64": sks.probe_fma_peak(sks.FP64, gpu), "fp32": sks.probe_fma_peak(sks.FP32C, gpu)}
     # roofline of the dominant kernel (the fused step kernel): algorithmic
     # bytes per launch = points it updates x 124 B over its mean event-timed
-    # duration; the same with the 74 B the layout actually moves beside it
+    # duration; the same with the 72 B the layout actually moves beside it
     # step-kernel time per step (a pipelined chunk is one launch of many steps)
     km, kc = r32["kernels"]["element"]
     main_pts = npts
