@@ -193,3 +193,38 @@ def test_materials_are_deduplicated(tmp_path):
     assert info["nmat"] <= 4
     assert len(np.unique(mat, axis=0)) <= info["nmat"]
     assert info["anisotropic"] == 0
+
+
+def _iso_rows_numpy(mat, info):
+    """Element rows whose points all carry an exactly isotropic material:
+    zero coupling entries, C11 = C33, C44 = C55 = C66 (the 15-entry row is
+    C11 C16 C15 C14 C13 | C66 C56 C46 C36 | C55 C45 C35 | C44 C34 | C33)."""
+    m = mat[:, :15]
+    iso = ((m[:, [1, 2, 3, 6, 7, 8, 10, 11, 13]] == 0).all(axis=1) & (m[:, 0] == m[:, 14]) &
+           (m[:, 5] == m[:, 9]) & (m[:, 9] == m[:, 12]))
+    iso = iso.reshape(info["nz"], info["nx"])
+    N = info["hpn"]
+    return sum(bool(iso[ez * N:ez * N + N + 1].all()) for ez in range(info["nez"]))
+
+
+@pytest.mark.parametrize("tilt", [0.0, 20.0])
+def test_isotropic_element_rows_are_counted_as_the_materials_say(tmp_path, tilt):
+    """sks_info_t.iso_rows (the rows the FP64 kernels give the isotropic
+    stress) equals a numpy classification of the per-point materials; an
+    anisotropic layer between isotropic ones leaves its rows and the rows
+    across its interfaces out."""
+    d = str(tmp_path)
+    H = 24.002
+    layers = [synth.SemLayer(H - 12, synth.iso_cij(8.1, 4.5, 3.4), 3.4),
+              synth.SemLayer(H - 5, synth.hexagonal_cij(8.1, 4.5, 3.4, 0.05, 40.0, tilt), 3.4),
+              synth.SemLayer(H + 1, synth.iso_cij(6.4, 3.6, 2.8), 2.8)]
+    c = synth.Case(nex=10, nez=12, eh=2.0, sdt=0.01, nst=10, layers=layers, p=0.05, f0=1.0, ntrace=3,
+                   rec_dx=4.0, semmodel_full=True)
+    synth.write_case(c, d)
+    with chdir(d), sks.Setup(["par=run.par"]) as su:
+        info = su.info()
+        mat = su.material()
+    want = _iso_rows_numpy(mat, info)
+    assert info["iso_rows"] == want
+    assert 0 < want < info["nez"]
+    assert info["anisotropic"] == 1
