@@ -696,19 +696,24 @@ extern "C" int sks_open_setup(sks_setup* su, int precision, int device, sks_solv
         // points: 1.26 ms against 1.43 pipelined).  One wave of tall bands is
         // not used on large meshes: with fewer CTA slots than twice the
         // element columns its bands differ in height by up to 2x (FP64, 64 M
-        // points: 30.5 ms against 21.1).
+        // points: 30.5 ms against 21.1).  Other GLL degrees, FP32C, pipelined
+        // on the 800 x 300 km box (3.84 M points): degree 5 with band seams
+        // (0.103 ms against 0.116 with halo rows), degree 3 in bands of 12
+        // (0.090 against 0.094), degree 6 without the register cap, which
+        // spills it (0.124 against 0.153).
         const int ncx4 = (m.nex + (tex_of(m.hpn) * 4 - 1) - 1) / (tex_of(m.hpn) * 4 - 1);
         const int64_t pts = (int64_t)m.nx * m.nz;
+        const int cap32 = m.hpn == 6 ? 0 : 1;
         int rcg;
         if (pts <= ((int64_t)2 << 20))
-            rcg = precision == SKS_FP32C ? set_grid(s, 4, pick_band(m, ncx4, sms, 10), 0, 1, 1)
+            rcg = precision == SKS_FP32C ? set_grid(s, 4, pick_band(m, ncx4, sms, 10), 0, cap32, 1)
                                          : set_grid(s, 4, pick_band(m, ncx4, sms, 5), 1, 0, 1);
         else if (precision == SKS_FP64)
             rcg = set_grid(s, 4, 6, 1, 1, 0, 1);
         else if (pts <= ((int64_t)16 << 20))
-            rcg = set_grid(s, 4, 8, 0, 1, 0, 1);
+            rcg = set_grid(s, 4, m.hpn == 3 ? 12 : 8, m.hpn == 5 ? 1 : 0, cap32, 0, 1);
         else
-            rcg = set_grid(s, 4, 12, 0, 1, 0, 0);
+            rcg = set_grid(s, 4, 12, 0, cap32, 0, 0);
         if (rcg) { free_device(s); cudaStreamDestroy(s->stream); sks_model_free(&s->m); delete s; return rcg; }
     }
     s->chunk = 64;
