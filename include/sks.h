@@ -76,8 +76,8 @@ typedef struct {
  * SKS_ERR_UNSUPPORTED: msource=1 (explosive source).  Every GLL degree the
  * reference accepts runs (hpn = 3..6, lagrange.c:323-328): degree 4 under
  * every tuning, degrees 3, 5 (the reference's default) and 6 with 4-warp
- * CTAs and register cap 0 or 1; batches and the serving loop run degrees 4
- * and 5 (a batch's members share one degree).  atten>0 (with ass) runs the
+ * CTAs and register cap 0 or 1, alone, in batches (a batch's members share
+ * one degree) and in the serving loop.  atten>0 (with ass) runs the
  * reference's boundary taper (atten_wave2, sem2d_psvsh.c:1780-1822). */
 int sks_open_par(int argc, const char *const *argv, int precision, int device,
                  sks_solver **out);
@@ -539,19 +539,19 @@ typedef struct {
  * steps per scheduling round (64 = one chunk). */
 int sks_server_create(int device, int64_t device_budget_bytes, int32_t quantum_steps, sks_server **out);
 /* A form's tuning (as sks_batch_set_tuning).  A tuning other than 4 warps
- * per CTA with register cap 0 or 1 cannot run GLL degree 5: it is refused
- * (SKS_ERR_STATE) while the form has degree-5 requests queued or running,
- * and afterwards degree-5 submissions of that form are refused. */
+ * per CTA with register cap 0 or 1 runs GLL degree 4 only: it is refused
+ * (SKS_ERR_STATE) while the form has requests of another degree queued or
+ * running, and afterwards such submissions of that form are refused. */
 int sks_server_set_tuning(sks_server *srv, int precision, const sks_tuning_t *t);
 int sks_server_set_active_points(sks_server *srv, int precision, int64_t max_points);
 /* Takes the set-up over (also on error).  pw: boundary records generated on
  * the device; NULL: read at admission from the files the par words name
  * (relative names resolved against the working directory at submission).
  * seis_u/v/w: nst*ntrace floats each, filled when the request is done (any
- * may be NULL); they must stay valid until then.  Served requests run GLL
- * degrees 4 and 5; other degrees are refused here (SKS_ERR_UNSUPPORTED), as
- * is degree 5 when the form's tuning cannot run it.  A request whose
- * wavefield stops being finite fails alone with SKS_ERR_NONFINITE. */
+ * may be NULL); they must stay valid until then.  A request of GLL degree 3,
+ * 5 or 6 is refused here (SKS_ERR_UNSUPPORTED) when the form's tuning cannot
+ * run it.  A request whose wavefield stops being finite fails alone with
+ * SKS_ERR_NONFINITE. */
 int sks_server_submit(sks_server *srv, sks_setup *su, int precision, const sks_plane_wave_t *pw,
                       float *seis_u, float *seis_v, float *seis_w, int64_t *id);
 /* Same with boundary records from a plane wave through a layered stack

@@ -73,8 +73,8 @@ bool member_aniso(const sks_solver* s) { return s->m.anisotropic != 0; }
 // the members' GLL degree (they share one; 4 while the batch is empty)
 int batch_deg(const sks_batch* b) { return b->mem.empty() ? N : b->mem[0]->m.hpn; }
 
-// the tunings compiled for a degree: every one for 4; for 5, 4 warps per CTA
-// and register cap 0 or 1
+// the tunings compiled for a degree: every one for 4; for 3, 5 and 6, 4 warps
+// per CTA and register cap 0 or 1
 bool batch_tuning_compiled(int deg, int NW, int CAP) { return deg == N || (NW == 4 && CAP <= 1); }
 
 int nline_of(const sks_solver* s) { return (s->m.nx - s->nbl) + (s->m.nz - s->nbl - 1); }
@@ -230,35 +230,105 @@ int build_tables(sks_batch* b)
     return SKS_OK;
 }
 
+// The compiled batch kernels of one GLL degree D (3..6) and form T
+template <typename T, int D>
+struct DegBatch {
+    static constexpr bool F32 = sizeof(T) == 4;
+    using M = BatchMember<T>;
+    static int occ(const StepVariant& v, bool a, bool pipe)
+    {
+        if constexpr (D == 3) {
+            if (pipe) return F32 ? batch_pipe_occupancy_f32_d3(v, a) : batch_pipe_occupancy_f64_d3(v, a);
+            return F32 ? batch_occupancy_f32_d3(v, a) : batch_occupancy_f64_d3(v, a);
+        } else if constexpr (D == 5) {
+            if (pipe) return F32 ? batch_pipe_occupancy_f32_d5(v, a) : batch_pipe_occupancy_f64_d5(v, a);
+            return F32 ? batch_occupancy_f32_d5(v, a) : batch_occupancy_f64_d5(v, a);
+        } else if constexpr (D == 6) {
+            if (pipe) return F32 ? batch_pipe_occupancy_f32_d6(v, a) : batch_pipe_occupancy_f64_d6(v, a);
+            return F32 ? batch_occupancy_f32_d6(v, a) : batch_occupancy_f64_d6(v, a);
+        } else {
+            if (pipe) return F32 ? batch_pipe_occupancy_f32(v, a) : batch_pipe_occupancy_f64(v, a);
+            return F32 ? batch_occupancy_f32(v, a) : batch_occupancy_f64(v, a);
+        }
+    }
+    static cudaError_t step(const StepVariant& v, bool a, int grid, cudaStream_t st, const M* mem,
+                            const BatchState* state, const int4* items, const BatchHeader* hdr, int j,
+                            const Coef<T, D>& k)
+    {
+        if constexpr (F32) {
+            if constexpr (D == 3) return launch_batch_f32_d3(v, a, grid, st, mem, state, items, hdr, j, k);
+            else if constexpr (D == 5) return launch_batch_f32_d5(v, a, grid, st, mem, state, items, hdr, j, k);
+            else if constexpr (D == 6) return launch_batch_f32_d6(v, a, grid, st, mem, state, items, hdr, j, k);
+            else return launch_batch_f32(v, a, grid, st, mem, state, items, hdr, j, k);
+        } else {
+            if constexpr (D == 3) return launch_batch_f64_d3(v, a, grid, st, mem, state, items, hdr, j, k);
+            else if constexpr (D == 5) return launch_batch_f64_d5(v, a, grid, st, mem, state, items, hdr, j, k);
+            else if constexpr (D == 6) return launch_batch_f64_d6(v, a, grid, st, mem, state, items, hdr, j, k);
+            else return launch_batch_f64(v, a, grid, st, mem, state, items, hdr, j, k);
+        }
+    }
+    static cudaError_t pipe(const StepVariant& v, bool a, int grid, cudaStream_t st, const M* mem,
+                            const BatchState* state, const int4* items, const BatchHeader* hdr, int nsteps,
+                            const BatchPipeCtl& ctl, const Coef<T, D>& k)
+    {
+        if constexpr (F32) {
+            if constexpr (D == 3) return launch_batch_pipe_f32_d3(v, a, grid, st, mem, state, items, hdr, nsteps, ctl, k);
+            else if constexpr (D == 5) return launch_batch_pipe_f32_d5(v, a, grid, st, mem, state, items, hdr, nsteps, ctl, k);
+            else if constexpr (D == 6) return launch_batch_pipe_f32_d6(v, a, grid, st, mem, state, items, hdr, nsteps, ctl, k);
+            else return launch_batch_pipe_f32(v, a, grid, st, mem, state, items, hdr, nsteps, ctl, k);
+        } else {
+            if constexpr (D == 3) return launch_batch_pipe_f64_d3(v, a, grid, st, mem, state, items, hdr, nsteps, ctl, k);
+            else if constexpr (D == 5) return launch_batch_pipe_f64_d5(v, a, grid, st, mem, state, items, hdr, nsteps, ctl, k);
+            else if constexpr (D == 6) return launch_batch_pipe_f64_d6(v, a, grid, st, mem, state, items, hdr, nsteps, ctl, k);
+            else return launch_batch_pipe_f64(v, a, grid, st, mem, state, items, hdr, nsteps, ctl, k);
+        }
+    }
+};
+
+// calls f.template run<D>() for the batch's degree D (3..6)
+template <typename Fn>
+auto with_batch_degree(int deg, Fn& f)
+{
+    switch (deg) {
+    case 3: return f.template run<3>();
+    case 5: return f.template run<5>();
+    case 6: return f.template run<6>();
+    default: return f.template run<4>();
+    }
+}
+
+// one step launch of every member (j = the launch within the chunk), or, with
+// nsteps > 0, one pipelined chunk of nsteps steps
+template <typename T>
+struct BatchLaunch {
+    sks_batch* b;
+    int j, nsteps;
+    const BatchPipeCtl* ctl;
+    template <int D>
+    cudaError_t run()
+    {
+        const StepVariant v{b->NW, b->ZS, b->CAP, b->taper};
+        static thread_local Coef<T, D> k;
+        k = make_coef<T, D>(b->mem[0]->m);     // GLL tables: the same for every member
+        const BatchMember<T>* mem = (const BatchMember<T>*)b->dmem;
+        if (ctl)
+            return DegBatch<T, D>::pipe(v, b->aniso, b->grid, b->stream, mem, b->dstate, b->ditems, b->dhdr, nsteps,
+                                        *ctl, k);
+        return DegBatch<T, D>::step(v, b->aniso, b->grid, b->stream, mem, b->dstate, b->ditems, b->dhdr, j, k);
+    }
+};
+
 template <typename T>
 cudaError_t launch_steps(sks_batch* b, int j)
 {
-    const StepVariant v{b->NW, b->ZS, b->CAP, b->taper};
-    if (batch_deg(b) == 5) {
-        static thread_local Coef<T, 5> k5;
-        k5 = make_coef<T, 5>(b->mem[0]->m);
-        if (sizeof(T) == 4)
-            return launch_batch_f32_d5(v, b->aniso, b->grid, b->stream, (const BatchMember<float>*)b->dmem, b->dstate,
-                                       b->ditems, b->dhdr, j, *(const Coef<float, 5>*)&k5);
-        return launch_batch_f64_d5(v, b->aniso, b->grid, b->stream, (const BatchMember<double>*)b->dmem, b->dstate,
-                                   b->ditems, b->dhdr, j, *(const Coef<double, 5>*)&k5);
-    }
-    static thread_local Coef<T> k;
-    k = make_coef<T>(b->mem[0]->m);     // GLL tables: the same for every member
-    if (sizeof(T) == 4)
-        return launch_batch_f32(v, b->aniso, b->grid, b->stream, (const BatchMember<float>*)b->dmem, b->dstate, b->ditems,
-                                b->dhdr, j, *(const Coef<float>*)&k);
-    return launch_batch_f64(v, b->aniso, b->grid, b->stream, (const BatchMember<double>*)b->dmem, b->dstate, b->ditems,
-                            b->dhdr, j, *(const Coef<double>*)&k);
+    BatchLaunch<T> l{b, j, 0, nullptr};
+    return with_batch_degree(batch_deg(b), l);
 }
 
 // a pipelined chunk of nsteps steps: the counters back to zero, then one launch
 template <typename T>
 cudaError_t launch_pipe_chunk(sks_batch* b, int nsteps)
 {
-    const StepVariant v{b->NW, b->ZS, b->CAP, b->taper};
-    static thread_local Coef<T> k;
-    k = make_coef<T>(b->mem[0]->m);
     // the claim counter and the done counters; the error flag stays set for
     // the rest of a run once a wait ran out (batch_launch clears it)
     cudaError_t e = cudaMemsetAsync(b->dpipe, 0, sizeof(int), b->stream);
@@ -266,36 +336,26 @@ cudaError_t launch_pipe_chunk(sks_batch* b, int nsteps)
     if (e != cudaSuccess) return e;
     const BatchPipeCtl ctl{b->dpipe, b->dpipe + 1, b->dpipe + 2, b->test_stall ? b->test_spins : PIPE_SPIN_LIMIT,
                            b->test_stall - 1};
-    if (batch_deg(b) == 5) {
-        static thread_local Coef<T, 5> k5;
-        k5 = make_coef<T, 5>(b->mem[0]->m);
-        if (sizeof(T) == 4)
-            return launch_batch_pipe_f32_d5(v, b->aniso, b->grid, b->stream, (const BatchMember<float>*)b->dmem,
-                                            b->dstate, b->ditems, b->dhdr, nsteps, ctl, *(const Coef<float, 5>*)&k5);
-        return launch_batch_pipe_f64_d5(v, b->aniso, b->grid, b->stream, (const BatchMember<double>*)b->dmem, b->dstate,
-                                        b->ditems, b->dhdr, nsteps, ctl, *(const Coef<double, 5>*)&k5);
-    }
-    if (sizeof(T) == 4)
-        return launch_batch_pipe_f32(v, b->aniso, b->grid, b->stream, (const BatchMember<float>*)b->dmem, b->dstate,
-                                     b->ditems, b->dhdr, nsteps, ctl, *(const Coef<float>*)&k);
-    return launch_batch_pipe_f64(v, b->aniso, b->grid, b->stream, (const BatchMember<double>*)b->dmem, b->dstate,
-                                 b->ditems, b->dhdr, nsteps, ctl, *(const Coef<double>*)&k);
+    BatchLaunch<T> l{b, 0, nsteps, &ctl};
+    return with_batch_degree(batch_deg(b), l);
 }
+
+struct BatchOcc {
+    const sks_batch* b;
+    template <int D>
+    int run()
+    {
+        const StepVariant v{b->NW, b->ZS, b->CAP, b->taper};
+        return b->precision == SKS_FP64 ? DegBatch<double, D>::occ(v, b->aniso, b->PIPE != 0)
+                                        : DegBatch<float, D>::occ(v, b->aniso, b->PIPE != 0);
+    }
+};
 
 // persistent grid: every SM full of resident CTAs of the step variant
 void set_persistent_grid(sks_batch* b)
 {
-    const StepVariant v{b->NW, b->ZS, b->CAP, b->taper};
-    int occ;
-    const bool f64 = b->precision == SKS_FP64;
-    if (batch_deg(b) == 5) {
-        if (b->PIPE) occ = f64 ? batch_pipe_occupancy_f64_d5(v, b->aniso) : batch_pipe_occupancy_f32_d5(v, b->aniso);
-        else occ = f64 ? batch_occupancy_f64_d5(v, b->aniso) : batch_occupancy_f32_d5(v, b->aniso);
-    } else {
-        if (b->PIPE) occ = f64 ? batch_pipe_occupancy_f64(v, b->aniso) : batch_pipe_occupancy_f32(v, b->aniso);
-        else occ = f64 ? batch_occupancy_f64(v, b->aniso) : batch_occupancy_f32(v, b->aniso);
-    }
-    b->grid = b->sms * occ;
+    BatchOcc o{b};
+    b->grid = b->sms * with_batch_degree(batch_deg(b), o);
 }
 
 template <typename T>
@@ -412,7 +472,7 @@ extern "C" int sks_batch_add(sks_batch* b, sks_solver* s)
     if (s->precision != b->precision) return set_err(SKS_ERR_ARG, "the solver's form differs from the batch's");
     if (s->device != b->device) return set_err(SKS_ERR_ARG, "the solver is on device %d, the batch on %d", s->device, b->device);
     if (s->snaps) return set_err(SKS_ERR_UNSUPPORTED, "snapshots (plot_snap=1) are taken by sks_run, not in batches");
-    if (s->m.hpn != 4 && s->m.hpn != 5) return set_err(SKS_ERR_UNSUPPORTED, "hpn=%d: batches run GLL degrees 4 and 5", s->m.hpn);
+    if (s->m.hpn < 3 || s->m.hpn > 6) return set_err(SKS_ERR_UNSUPPORTED, "hpn=%d: batches run GLL degrees 3 to 6", s->m.hpn);
     if (!b->mem.empty() && s->m.hpn != batch_deg(b))
         return set_err(SKS_ERR_ARG, "hpn=%d: the batch's members are of GLL degree %d", s->m.hpn, batch_deg(b));
     if (!batch_tuning_compiled(s->m.hpn, b->NW, b->CAP))

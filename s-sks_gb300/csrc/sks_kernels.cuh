@@ -1132,6 +1132,22 @@ SKS_DEG_DECL(f64, double, 3)
 SKS_DEG_DECL(f32, float, 6)
 SKS_DEG_DECL(f64, double, 6)
 #undef SKS_DEG_DECL
+// batches of GLL degrees 3 and 6 (4 warps, register cap 0 or 1)
+#define SKS_BATCH_DEG_DECL(F, T, D)                                                                             \
+    int batch_occupancy_##F##_d##D(const StepVariant& v, bool aniso);                                         \
+    cudaError_t launch_batch_##F##_d##D(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,        \
+                                        const BatchMember<T>* mem, const BatchState* state, const int4* items, \
+                                        const BatchHeader* hdr, int j, const Coef<T, D>& k);                  \
+    int batch_pipe_occupancy_##F##_d##D(const StepVariant& v, bool aniso);                                    \
+    cudaError_t launch_batch_pipe_##F##_d##D(const StepVariant& v, bool aniso, int blocks, cudaStream_t st,   \
+                                             const BatchMember<T>* mem, const BatchState* state,              \
+                                             const int4* items, const BatchHeader* hdr, int nsteps,           \
+                                             const BatchPipeCtl& ctl, const Coef<T, D>& k);
+SKS_BATCH_DEG_DECL(f32, float, 3)
+SKS_BATCH_DEG_DECL(f64, double, 3)
+SKS_BATCH_DEG_DECL(f32, float, 6)
+SKS_BATCH_DEG_DECL(f64, double, 6)
+#undef SKS_BATCH_DEG_DECL
 // the same with the boundary taper compiled in (the entry points above call
 // these for a variant with taper set)
 int step_occupancy_f32_tp(const StepVariant& v, bool aniso);

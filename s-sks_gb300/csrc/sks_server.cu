@@ -103,9 +103,9 @@ struct sks_server {
     // of all sharing the device
     int64_t max_points[2] = {(int64_t)8 << 20, (int64_t)24 << 20};
     int64_t active_points[2] = {0, 0};
-    // per form: the batch's tuning runs GLL degree 5 (4 warps per CTA,
-    // register cap 0 or 1); guarded by mu
-    bool deg5_ok[2] = {true, true};
+    // per form: the batch's tuning runs GLL degrees other than 4 (4 warps
+    // per CTA, register cap 0 or 1); guarded by mu
+    bool other_deg_ok[2] = {true, true};
     sks_batch* batch[2] = {nullptr, nullptr};      // by precision
     std::mutex mu;                                 // guards queue, reqs, next_id, in_use and the
                                                    // request fields other threads read
@@ -291,27 +291,27 @@ extern "C" int sks_server_set_tuning(sks_server* v, int precision, const sks_tun
 {
     if (!v || !t) return set_err(SKS_ERR_ARG, "NULL argument");
     if (precision != SKS_FP64 && precision != SKS_FP32C) return set_err(SKS_ERR_ARG, "unknown precision %d", precision);
-    const bool deg5 = t->warps_per_block == 4 && t->register_cap <= 1;
+    const bool other_deg = t->warps_per_block == 4 && t->register_cap <= 1;
     {
-        // a tuning that cannot run degree 5 is refused while the form has
-        // degree-5 requests queued or running
+        // a tuning that can run degree 4 only is refused while the form has
+        // requests of another degree queued or running
         std::lock_guard<std::mutex> lk(v->mu);
-        if (!deg5) {
+        if (!other_deg) {
             for (const Request* r : v->queue)
-                if (r->precision == precision && r->su && r->su->m.hpn == 5)
-                    return set_err(SKS_ERR_STATE, "request %lld is of GLL degree 5, which runs with 4 warps per CTA "
-                                                  "and register cap 0 or 1", (long long)r->id);
+                if (r->precision == precision && r->su && r->su->m.hpn != 4)
+                    return set_err(SKS_ERR_STATE, "request %lld is of GLL degree %d, which runs with 4 warps per CTA "
+                                                  "and register cap 0 or 1", (long long)r->id, r->su->m.hpn);
             for (const Request* r : v->active[precision])
-                if (r->s && r->s->m.hpn == 5)
-                    return set_err(SKS_ERR_STATE, "request %lld is of GLL degree 5, which runs with 4 warps per CTA "
-                                                  "and register cap 0 or 1", (long long)r->id);
+                if (r->s && r->s->m.hpn != 4)
+                    return set_err(SKS_ERR_STATE, "request %lld is of GLL degree %d, which runs with 4 warps per CTA "
+                                                  "and register cap 0 or 1", (long long)r->id, r->s->m.hpn);
         }
     }
     if (batch_running(v->batch[precision])) batch_finish(v->batch[precision]);
     const int rc = sks_batch_set_tuning(v->batch[precision], t);
     if (!rc) {
         std::lock_guard<std::mutex> lk(v->mu);
-        v->deg5_ok[precision] = deg5;
+        v->other_deg_ok[precision] = other_deg;
     }
     return rc;
 }
@@ -340,18 +340,13 @@ int submit(sks_server* v, sks_setup* su, int precision, const sks_plane_wave_t* 
         sks_setup_close(su);
         return set_err(SKS_ERR_ARG, "unknown precision %d", precision);
     }
-    if (su->m.hpn != 4 && su->m.hpn != 5) {
+    if (su->m.hpn != 4) {
         const int hpn = su->m.hpn;
-        sks_setup_close(su);
-        return set_err(SKS_ERR_UNSUPPORTED, "hpn=%d: served requests run GLL degrees 4 and 5 (other degrees run as "
-                                            "single solves)", hpn);
-    }
-    if (su->m.hpn == 5) {
         std::lock_guard<std::mutex> lk(v->mu);
-        if (!v->deg5_ok[precision]) {
+        if (!v->other_deg_ok[precision]) {
             sks_setup_close(su);
-            return set_err(SKS_ERR_UNSUPPORTED, "GLL degree 5 requests need the form's tuning to be 4 warps per CTA "
-                                                "and register cap 0 or 1 (sks_server_set_tuning)");
+            return set_err(SKS_ERR_UNSUPPORTED, "GLL degree %d requests need the form's tuning to be 4 warps per CTA "
+                                                "and register cap 0 or 1 (sks_server_set_tuning)", hpn);
         }
     }
     if (!pw && !layers) {

@@ -54,6 +54,7 @@ def build(verbose: bool = False) -> str:
                "sks_step_f32_tp", "sks_step_f64_tp", "sks_batch_f32_tp", "sks_batch_f64_tp",
                "sks_step_f32_d5", "sks_step_f64_d5", "sks_batch_f32_d5", "sks_batch_f64_d5",
                "sks_step_f32_d3", "sks_step_f64_d3", "sks_step_f32_d6", "sks_step_f64_d6",
+               "sks_batch_f32_d3", "sks_batch_f64_d3", "sks_batch_f32_d6", "sks_batch_f64_d6",
                "sks_noalloc", "sks_post", "sks_probe"):
         units.append((os.path.join(CSRC, cu + ".cu"), os.path.join(OUT, cu + ".o"),
                       [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC,

@@ -173,17 +173,25 @@ def test_batch_rejects_mixed_forms_and_double_membership(cases):
         s64.close()
 
 
+# per degree: the members' (nex, nez, eh, dt, steps)
+DEG_MEMBERS = {3: ((30, 9, 1.5, 0.008, 700), (20, 8, 2.0, 0.01, 560)),
+               5: ((23, 7, 2.0, 0.008, 700), (14, 6, 2.5, 0.01, 560)),
+               6: ((19, 6, 2.5, 0.006, 900), (12, 5, 3.0, 0.007, 720))}
+
+
+@pytest.mark.parametrize("deg", [5, 3, 6])
 @pytest.mark.parametrize("prec,tuning", [(sks.FP64, (4, 3, 1, 0, 0)), (sks.FP32C, (4, 3, 0, 1, 0)),
                                          (sks.FP32C, (4, 4, 1, 1, 1))])
-def test_degree5_batch_matches_members_alone(cases, tmp_path, prec, tuning):
-    """Members of GLL degree 5 (the reference's default hpn) in a batch equal
-    their solo runs; a batch holds one degree and degree 5's compiled tunings."""
+def test_other_degrees_batch_matches_members_alone(cases, tmp_path, prec, tuning, deg):
+    """Members of GLL degree 5 (the reference's default hpn), 3 or 6 in a
+    batch equal their solo runs; a batch holds one degree and that degree's
+    compiled tunings."""
     dirs, nst = [], []
-    for i, (nex, nez, eh, sdt, n) in enumerate(((23, 7, 2.0, 0.008, 700), (14, 6, 2.5, 0.01, 560))):
-        d = str(tmp_path / f"d5_{i}")
+    for i, (nex, nez, eh, sdt, n) in enumerate(DEG_MEMBERS[deg]):
+        d = str(tmp_path / f"d{deg}_{i}")
         H = nez * eh + 0.002
         c = synth.Case(nex=nex, nez=nez, eh=eh, sdt=sdt, nst=n, layers=_layers(H, True), p=0.045, f0=1.0,
-                       sv_amp=1.0, sh_amp=0.4, hpn=5, ntrace=7, rec_dx=3.0, semmodel_full=True)
+                       sv_amp=1.0, sh_amp=0.4, hpn=deg, ntrace=7, rec_dx=3.0, semmodel_full=True)
         synth.write_case(c, d)
         dirs.append(d)
         nst.append(n)
@@ -200,7 +208,7 @@ def test_degree5_batch_matches_members_alone(cases, tmp_path, prec, tuning):
             b.add(s)
         b.set_tuning(*tuning)
         with pytest.raises(sks.SksError):
-            b.set_tuning(2, 3, 0, 1, 0)                 # not compiled for degree 5
+            b.set_tuning(2, 3, 0, 1, 0)                 # not compiled for degrees other than 4
         other = _open(cases[0], prec)                    # degree 4
         with pytest.raises(sks.SksError):
             b.add(other)

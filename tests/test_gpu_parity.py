@@ -173,8 +173,7 @@ def test_taper_under_every_grid_and_in_a_batch(casedirs, prec):
 def test_other_degrees_tunings_bit_identical_and_refusals(casedirs, prec, deg):
     """Degrees 3, 5 and 6 compile 4-warp CTAs with register cap 0 or 1: every
     such grid (seams or halo rows, per-step or pipelined, balanced waves)
-    gives the same bits; other tunings are refused; batches take degree 5 and
-    refuse 3 and 6."""
+    gives the same bits; other tunings are refused; batches take them."""
     d, c, _ = casedirs[f"hpn{deg}_aniso"]
     ref = None
     with chdir(d):
@@ -193,13 +192,8 @@ def test_other_degrees_tunings_bit_identical_and_refusals(casedirs, prec, deg):
                     s.set_tuning(*bad)
             s.load_boundary_files()
             with sks.Batch(prec) as b:
-                if deg == 5:
-                    b.add(s)                            # batches take degree 5 too
-                    b.remove(s)
-                else:
-                    with pytest.raises(sks.SksError) as e:
-                        b.add(s)
-                    assert e.value.code == -4
+                b.add(s)                                # batches take these degrees too
+                b.remove(s)
         with pytest.raises(sks.SksError):
             sks.Solver(["par=run.par", "hpn=7"], precision=prec)
 

@@ -206,12 +206,13 @@ def test_layered_requests_are_the_same_alone_and_served(tmp_path):
     srv.close()
 
 
-def test_mixed_degrees_are_served_in_turn(tmp_path):
-    """A form's batch runs one GLL degree at a time: requests of degree 4 and
-    5 arriving mixed all complete, the other degree waiting for the batch to
-    drain, and each equals its solo run."""
+@pytest.mark.parametrize("degs", [(4, 5, 4, 5), (3, 6, 4, 3)], ids=["4-5", "3-6-4"])
+def test_mixed_degrees_are_served_in_turn(tmp_path, degs):
+    """A form's batch runs one GLL degree at a time: requests of several
+    degrees arriving mixed all complete, another degree waiting for the batch
+    to drain, and each equals its solo run."""
     reqs = []
-    for k, hpn in enumerate((4, 5, 4, 5)):
+    for k, hpn in enumerate(degs):
         d = str(tmp_path / f"deg{k}")
         nez, eh = 8, 2.0
         H = nez * eh + 0.002
@@ -232,24 +233,21 @@ def test_mixed_degrees_are_served_in_turn(tmp_path):
     srv.close()
 
 
-def test_unservable_degrees_and_tunings_are_refused_early(tmp_path):
-    """Degrees 3 and 6 run as single solves, not served: refused at
-    submission.  A tuning that cannot run degree 5 is refused while a degree-5
-    request waits, and degree-5 submissions are refused once it is set."""
+def test_tunings_that_cannot_run_a_degree_are_refused_early(tmp_path):
+    """Degrees 3, 5 and 6 run with 4-warp CTAs and register cap 0 or 1: a
+    form tuning outside that is refused while such a request waits, and such
+    requests are refused at submission once it is set."""
     dirs = {}
-    for hpn in (3, 5):
+    for hpn in (3, 6):
         d = str(tmp_path / f"deg{hpn}")
         H = 8 * 2.0 + 0.002
-        c = synth.Case(nex=20, nez=8, eh=2.0, sdt=0.008, nst=200, layers=_layers(H, True), p=0.045, f0=1.0,
-                       sv_amp=1.0, sh_amp=0.3, hpn=hpn, ntrace=5, rec_dx=4.0, semmodel_full=True,
+        c = synth.Case(nex=20, nez=8, eh=2.0, sdt=0.006 if hpn == 6 else 0.008, nst=200, layers=_layers(H, True),
+                       p=0.045, f0=1.0, sv_amp=1.0, sh_amp=0.3, hpn=hpn, ntrace=5, rec_dx=4.0, semmodel_full=True,
                        write_records=False)
         synth.write_case(c, d)
         dirs[hpn] = (d, (float(np.sqrt(c.layers[0].C[3, 3] / c.layers[0].rho)), c.p, c.f0, 1.0, 0.3))
     srv = sks.Server(0, 0, 64)
-    with pytest.raises(sks.SksError) as e:
-        srv.submit(_setup(dirs[3][0]), sks.FP32C, dirs[3][1])
-    assert e.value.code == -4
-    rid = srv.submit(_setup(dirs[5][0]), sks.FP32C, dirs[5][1])
+    rid = srv.submit(_setup(dirs[3][0]), sks.FP32C, dirs[3][1])
     with pytest.raises(sks.SksError) as e:
         srv.set_tuning(sks.FP32C, 2, 4, 0, 1)
     assert e.value.code == -8
@@ -257,10 +255,11 @@ def test_unservable_degrees_and_tunings_are_refused_early(tmp_path):
         pass
     assert srv.info(rid)["state"] == sks.REQ_DONE
     srv.set_tuning(sks.FP32C, 2, 4, 0, 1)
-    with pytest.raises(sks.SksError) as e:
-        srv.submit(_setup(dirs[5][0]), sks.FP32C, dirs[5][1])
-    assert e.value.code == -4
-    srv.submit(_setup(dirs[5][0]), sks.FP64, dirs[5][1])       # the other form's tuning still runs it
+    for hpn in (3, 6):
+        with pytest.raises(sks.SksError) as e:
+            srv.submit(_setup(dirs[hpn][0]), sks.FP32C, dirs[hpn][1])
+        assert e.value.code == -4
+    srv.submit(_setup(dirs[6][0]), sks.FP64, dirs[6][1])       # the other form's tuning still runs it
     while srv.step() > 0:
         pass
     srv.close()
