@@ -968,7 +968,8 @@ def main() -> None:
         "value_spread": r32["spread"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "k_step (element force + assembly + update + receivers + injection)",
+                     "kernel": ("k_step_pipe (pipelined chunk of steps: " if r32["tuning"].get("pipeline") else
+                                "k_step (one step: ") + "element force + assembly + update + receivers + injection)",
                      "kernel_ms_per_step": t_launch * 1e3, "kernel_share": km / max(total_k, 1e-12),
                      "bytes_per_point": BYTES_PER_POINT["fp32c"], "points_per_launch": main_pts,
                      "layout_bytes_per_point": LAYOUT_BYTES_PER_POINT["fp32c"],
