@@ -158,6 +158,20 @@ Coef<T, DEG> make_coef(const sks_model& m)
         }
     for (int i = 0; i < NP; i++) { k.w[i] = (T)m.gllw[i]; k.winv[i] = (T)(1.0 / m.gllw[i]); }
     k.winv2 = (T)(1.0 / (2.0 * m.gllw[0]));
+    // even-odd tables of the two in-lane z contractions: the gradient's
+    // A[a][t] = l'_t(xi_a), the divergence's A[a][t] = l'_a(xi_t) w_t
+    constexpr int H = NP / 2, NN = DEG;
+    for (int f = 0; f < 2; f++) {
+        auto A = [&](int a, int t) { return f == 0 ? m.dlagP[a * NP + t] : m.dlagP[t * NP + a] * m.gllw[t]; };
+        for (int a = 0; a < H; a++) {
+            for (int t = 0; t < H; t++) {
+                k.P[f][a * H + t] = (T)((A(a, t) - A(a, NN - t)) * 0.5);
+                k.Q[f][a * H + t] = (T)((A(a, t) + A(a, NN - t)) * 0.5);
+            }
+            k.R[f][a] = (T)((NP & 1) ? A(a, H) : 0.0);
+            k.Mid[f][a] = (T)((NP & 1) ? A(H, a) : 0.0);
+        }
+    }
     return k;
 }
 

@@ -55,13 +55,59 @@ constexpr int MAT_STRIDE = 16;
 // one kernel argument serves every instance of a batch.
 template <typename T, int DEG = N>
 struct Coef {
-    static constexpr int NP = DEG + 1;
+    static constexpr int NP = DEG + 1, H = NP / 2;
     T D[NP * NP];    // D[j*NP+i]  = l'_i(xi_j)
     T DWs[NP * NP];  // DWs[j*NP+i] = l'_i(xi_j) * w_j
     T w[NP];         // GLL weights
     T winv[NP];      // 1/w_a: inverse lumped-mass weight of a point inside an element edge
     T winv2;         // 1/(2 w_0): a point shared by two elements along x (or z)
+    // The FP64 kernels' in-lane z contractions in even-odd form (mirror_sum):
+    // [0] the gradient, A[a][t] = D[a][t]; [1] the divergence, A[a][t] = DWs[t][a]
+    T P[2][H * H];   // (A[a][t] - A[a][N-t]) / 2, a, t < H
+    T Q[2][H * H];   // (A[a][t] + A[a][N-t]) / 2
+    T R[2][H];       // A[a][H]   (odd NP: the middle column)
+    T Mid[2][H];     // A[H][t]   (odd NP: the middle row)
 };
+
+// y_a = sum_t A[a][t] v_t (a, t = 0..DEG) for a matrix with A[N-a][N-t] =
+// -A[a][t], as l'_t(xi_a) and l'_a(xi_t) w_t are on the mirror-symmetric GLL
+// points: from the mirrored sums e_t = v_t + v_{N-t} and differences
+// o_t = v_t - v_{N-t}, y_a + y_{N-a} = 2 sum_t P[a][t] o_t and
+// y_a - y_{N-a} = 2 (sum_t Q[a][t] e_t + R[a] v_H), and y_H = sum_t Mid[t] o_t.
+// Degree 4: 20 operations instead of 25 (a sum of the same terms in another
+// order, within FP64 rounding of the direct sum).  The sums and differences
+// are rounded adds that the compiler never fuses with a product (v may be a
+// product, e.g. an isotropic stress mu e): fused or not could then depend on
+// the kernel the code is inlined into, and every kernel must give the same bits.
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+
+template <typename T, int DEG>
+__device__ __forceinline__ void mirror_sum(const T v[DEG + 1], const T* P, const T* Q, const T* R, const T* Mid,
+                                           T y[DEG + 1])
+{
+    constexpr int N = DEG, NP = DEG + 1, H = NP / 2;
+    T e[H], o[H];
+#pragma unroll
+    for (int t = 0; t < H; t++) { e[t] = add_rn(v[t], v[N - t]); o[t] = sub_rn(v[t], v[N - t]); }
+#pragma unroll
+    for (int a = 0; a < H; a++) {
+        T sp = P[a * H] * o[0], sm = Q[a * H] * e[0];
+#pragma unroll
+        for (int t = 1; t < H; t++) { sp = fma(P[a * H + t], o[t], sp); sm = fma(Q[a * H + t], e[t], sm); }
+        if constexpr (NP & 1) sm = fma(R[a], v[H], sm);
+        y[a] = add_rn(sp, sm);
+        y[N - a] = sub_rn(sp, sm);
+    }
+    if constexpr (NP & 1) {
+        T m = Mid[0] * o[0];
+#pragma unroll
+        for (int t = 1; t < H; t++) m = fma(Mid[t], o[t], m);
+        y[H] = m;
+    }
+}
 
 template <typename T>
 struct Geo {
@@ -566,6 +612,23 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
         for (int b = 0; b < NP; b++)
 #pragma unroll
             for (int c = 0; c < 3; c++) kk[b][c] = (T)0;
+        // FP64 (bound by its FP64 operations): the z gradients of the element
+        // row's NP point rows at once and, after the rows, their z divergence
+        // in even-odd form; each row's z flux (sigma_13, sigma_23, sigma_33)
+        // waits in fz.  FP32 (bound by issue and registers): row by row.
+        constexpr bool EO = sizeof(T) == 8;
+        T dzr[EO ? NP : 1][3], fz[EO ? NP : 1][3];
+        if constexpr (EO) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                T v[NP], y[NP];
+#pragma unroll
+                for (int t = 0; t < NP; t++) v[t] = u[t][c];
+                mirror_sum<T, DEG>(v, k.P[0], k.Q[0], k.R[0], k.Mid[0], y);
+#pragma unroll
+                for (int t = 0; t < NP; t++) dzr[t][c] = y[t];
+            }
+        }
         T rinv[NP];
 #pragma unroll
         for (int bb = 0; bb < NP; bb++) {
@@ -576,10 +639,14 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
 #pragma unroll
                 for (int r = 1; r < NP; r++) s = fma(__shfl_sync(FULL, u[bb][c], src[r - 1]), Dx[r], s);
                 dx[c] = s;
-                T z = 0;
+                if constexpr (EO) {
+                    dz[c] = dzr[bb][c];
+                } else {
+                    T z = 0;
 #pragma unroll
-                for (int t = 0; t < NP; t++) z = fma(u[t][c], k.D[bb * NP + t], z);
-                dz[c] = z;
+                    for (int t = 0; t < NP; t++) z = fma(u[t][c], k.D[bb * NP + t], z);
+                    dz[c] = z;
+                }
             }
             const T ee[5] = {dx[0], dx[1], dx[2] + dz[0], dz[1], dz[2]};
             if (rm < 0 && (int)m[bb] != mcur) {      // rows across a material boundary
@@ -596,16 +663,34 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
                     T s = sg[c] * DWc[0];
 #pragma unroll
                     for (int r = 1; r < NP; r++) s = fma(__shfl_sync(FULL, sg[c], src[r - 1]), DWc[r], s);
-                    kk[bb][c] = fma(s, k.w[bb], kk[bb][c]);
+                    if constexpr (EO) kk[bb][c] = s * k.w[bb];
+                    else kk[bb][c] = fma(s, k.w[bb], kk[bb][c]);
                 }
             }
-            // z-divergence: row bb's stress feeds every row of the element
-            const T f2[3] = {sg[2] * wal, sg[3] * wal, sg[4] * wal};
+            if constexpr (EO) {
 #pragma unroll
-            for (int b = 0; b < NP; b++) {
-                if (halo && b < N) continue;
+                for (int c = 0; c < 3; c++) fz[bb][c] = sg[2 + c];
+            } else {
+                // z-divergence: row bb's stress feeds every row of the element
+                const T f2[3] = {sg[2] * wal, sg[3] * wal, sg[4] * wal};
 #pragma unroll
-                for (int c = 0; c < 3; c++) kk[b][c] = fma(f2[c], k.DWs[bb * NP + b], kk[b][c]);
+                for (int b = 0; b < NP; b++) {
+                    if (halo && b < N) continue;
+#pragma unroll
+                    for (int c = 0; c < 3; c++) kk[b][c] = fma(f2[c], k.DWs[bb * NP + b], kk[b][c]);
+                }
+            }
+        }
+        if constexpr (EO) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                T v[NP], y[NP];
+#pragma unroll
+                for (int t = 0; t < NP; t++) v[t] = fz[t][c];
+                mirror_sum<T, DEG>(v, k.P[1], k.Q[1], k.R[1], k.Mid[1], y);
+#pragma unroll
+                for (int b = 0; b < NP; b++)
+                    if (!halo || b == N) kk[b][c] = fma(wal, y[b], kk[b][c]);
             }
         }
         // the element row below contributed to row 0 first (the reference's order)
