@@ -390,8 +390,9 @@ __device__ __forceinline__ void finish_point(const Field<T>& F, const Geo<T>& G,
     if (!LF) {
         if (!edge) {
             const T mdt2 = (wxi * wzi) * rinv;   // wxi carries dt^2/Je
+            // two FMAs a component (2u - u_prev is one rounding)
 #pragma unroll
-            for (int c = 0; c < 3; c++) un[c] = (-mdt2 * K[c] + (T)2 * u[c]) - x.a[c];
+            for (int c = 0; c < 3; c++) un[c] = fma(-mdt2, K[c], fma((T)2, u[c], -x.a[c]));
         } else {
             const T* p = F.stc + stacey_index<DEG>(ix, iz, G.nx, G.nz) * 9;
 #pragma unroll
