@@ -52,14 +52,15 @@ FULL_STEPS = 24000
 BYTES_PER_POINT = {"fp32c": 124, "fp64": 200, "fp64_iso": 96}
 # flops per grid-point update of the FP64 step as the kernel computes it (an
 # FMA is 2 flops, an n-term dot product 2n-1): per element row a GLL column
-# does, for each of its 5 rows, the x derivatives of 3 components (27), their
-# z derivatives in even-odd form (16.2: 27 per component for all 5 rows), one
-# strain sum (1), the 5x5 stress (45), the x-divergence with its weight (30)
-# and the even-odd z-divergence scaled into the rows (22.2): 141.4 x 5 = 707,
-# an element's 5 columns 3535, over its 16 unique points 220.9; plus assembly
+# does, for each of its 5 rows, the x derivatives of 3 components with the
+# strain sum u_z,x + u_x,z folded into one of them (28), their z derivatives
+# in even-odd form (16.2: 27 per component for all 5 rows), the 5x5 stress
+# (45), the x-divergence with the row weight in its table (27) and the
+# even-odd z-divergence scaled into the rows (22.2): 138.4 x 5 = 692, an
+# element's 5 columns 3460, over its 16 unique points 216.25; plus assembly
 # (1.5) and the 3-level update (15).  (Direct 5-term sums: 276.)
-# isotropic: the 5x5 stress is 9 flops instead of 45: 105.4 x 25 / 16 + 16.5
-FLOPS_PER_POINT = {"aniso": 237.4, "iso": 181.2}
+# isotropic: the 5x5 stress is 9 flops instead of 45: 102.4 x 25 / 16 + 16.5
+FLOPS_PER_POINT = {"aniso": 232.75, "iso": 176.5}
 LAYOUT_BYTES_PER_POINT = {"fp32c": 72, "fp64": 72}
 WORKLOAD = ("anisotropic 3-component SKS solve: 800x300 elements of 1 km, GLL degree 4, "
             "3,844,401 points, 100 km hexagonal layer (4 %, azimuth 45, tilt 20), dt 5 ms, 201 receivers")

@@ -489,10 +489,32 @@ constexpr int cap_warps(int cap) { return cap == 0 ? 0 : (sizeof(T) == 4 ? (cap 
 // shared memory of one CTA tile
 template <typename T, int NW, int DEG = N>
 struct TileShared {
+    static constexpr int NP = DEG + 1, XW = sizeof(T) == 8 ? NP * (NP * NP + 1) : 1;
     T xch[2][NW][DEG][3];   // force of a warp's last column, for the next warp
     T xtop[NW][3];          // the same for the band's top row
+    // FP64: the x-divergence weights of each GLL column a and row b, in the
+    // rotated order the lanes read them, times the row weight:
+    // xw[a][b][r] = l'_a(xi_t) w_t w_b, t = (a + r) mod NP (a's stride
+    // NP*NP+1 keeps the 5-7 columns a warp reads in distinct banks)
+    T xw[XW];
     int second_arrival;
 };
+
+// a kernel's first act: the CTA's constant shared tables (FP64 forms), then a
+// barrier; nothing for the FP32 forms
+template <typename T, int NW, int DEG>
+__device__ __forceinline__ void init_tile_shared(TileShared<T, NW, DEG>& sh, const Coef<T, DEG>& k)
+{
+    if constexpr (sizeof(T) == 8) {
+        constexpr int NP = DEG + 1, SA = NP * NP + 1;
+        for (int i = threadIdx.x; i < NP * SA; i += blockDim.x) {
+            const int a = i / SA, q = i - a * SA, b = q / NP, r = q - b * NP;
+            const int t = a + r < NP ? a + r : a + r - NP;
+            sh.xw[i] = q < NP * NP ? k.DWs[t * NP + a] * k.w[b] : (T)0;
+        }
+        __syncthreads();
+    }
+}
 
 // One CTA tile: element column cx (S = 6*NW-1 owned elements), band cz of
 // element rows [ez0, ez1).
@@ -633,13 +655,10 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
         T rinv[NP];
 #pragma unroll
         for (int bb = 0; bb < NP; bb++) {
+            // dx[2] is the strain u_z,x + u_x,z: its x sum starts from u_x,z
             T dx[3], dz[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                T s = u[bb][c] * Dx[0];
-#pragma unroll
-                for (int r = 1; r < NP; r++) s = fma(__shfl_sync(FULL, u[bb][c], src[r - 1]), Dx[r], s);
-                dx[c] = s;
                 if constexpr (EO) {
                     dz[c] = dzr[bb][c];
                 } else {
@@ -648,8 +667,12 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
                     for (int t = 0; t < NP; t++) z = fma(u[t][c], k.D[bb * NP + t], z);
                     dz[c] = z;
                 }
+                T s = c == 2 ? fma(u[bb][c], Dx[0], dz[0]) : u[bb][c] * Dx[0];
+#pragma unroll
+                for (int r = 1; r < NP; r++) s = fma(__shfl_sync(FULL, u[bb][c], src[r - 1]), Dx[r], s);
+                dx[c] = s;
             }
-            const T ee[5] = {dx[0], dx[1], dx[2] + dz[0], dz[1], dz[2]};
+            const T ee[5] = {dx[0], dx[1], dx[2], dz[1], dz[2]};
             if (rm < 0 && (int)m[bb] != mcur) {      // rows across a material boundary
                 M.load(F.mat + (size_t)m[bb] * MAT_STRIDE);
                 mcur = m[bb];
@@ -661,11 +684,19 @@ __device__ __forceinline__ void step_tile(const Field<T>& F, const Geo<T>& G, co
             if (!halo || bb == N) {
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    T s = sg[c] * DWc[0];
+                    if constexpr (EO) {
+                        // the row weight w_bb is in the table (one product fewer)
+                        const T* xw = sh.xw + al * (NP * NP + 1) + bb * NP;
+                        T s = sg[c] * xw[0];
 #pragma unroll
-                    for (int r = 1; r < NP; r++) s = fma(__shfl_sync(FULL, sg[c], src[r - 1]), DWc[r], s);
-                    if constexpr (EO) kk[bb][c] = s * k.w[bb];
-                    else kk[bb][c] = fma(s, k.w[bb], kk[bb][c]);
+                        for (int r = 1; r < NP; r++) s = fma(__shfl_sync(FULL, sg[c], src[r - 1]), xw[r], s);
+                        kk[bb][c] = s;
+                    } else {
+                        T s = sg[c] * DWc[0];
+#pragma unroll
+                        for (int r = 1; r < NP; r++) s = fma(__shfl_sync(FULL, sg[c], src[r - 1]), DWc[r], s);
+                        kk[bb][c] = fma(s, k.w[bb], kk[bb][c]);
+                    }
                 }
             }
             if constexpr (EO) {
@@ -815,6 +846,7 @@ __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
 k_step(Field<T> F, Geo<T> G, Coef<T, DEG> k)
 {
     __shared__ TileShared<T, NW, DEG> sh;
+    init_tile_shared<T, NW, DEG>(sh, k);
     int cx, cz, ez0, ez1;
     if (G.items) {
         const int4 it = G.items[blockIdx.x];
@@ -866,6 +898,7 @@ k_step_batch(const BatchMember<T>* __restrict__ mem, const BatchState* __restric
              const int4* __restrict__ items, const BatchHeader* __restrict__ hdr, int j, Coef<T, DEG> k)
 {
     __shared__ TileShared<T, NW, DEG> sh;
+    init_tile_shared<T, NW, DEG>(sh, k);
     __shared__ __align__(16) Field<T> sF;
     __shared__ __align__(16) Geo<T> sG;
     __shared__ int s_go;
@@ -979,6 +1012,7 @@ __global__ void __launch_bounds__(NW * 32, CAP ? cap_warps<T>(CAP) / NW : 1)
 k_step_pipe(Field<T> F, Geo<T> G, Coef<T, DEG> k, PipeChunk C, PipeCtl ctl)
 {
     __shared__ TileShared<T, NW, DEG> sh;
+    init_tile_shared<T, NW, DEG>(sh, k);
     __shared__ __align__(16) Field<T> sF;
     __shared__ int s_claim, s_step, s_next, s_fail;
     const int ntiles = G.ncx * G.ncz;
@@ -1065,6 +1099,7 @@ k_step_batch_pipe(const BatchMember<T>* __restrict__ mem, const BatchState* __re
                   Coef<T, DEG> k)
 {
     __shared__ TileShared<T, NW, DEG> sh;
+    init_tile_shared<T, NW, DEG>(sh, k);
     __shared__ __align__(16) Field<T> sF;
     __shared__ __align__(16) Geo<T> sG;
     __shared__ int s_claim, s_next, s_fail, s_go, s_m, s_j;
