@@ -29,7 +29,11 @@
 // (u, d = u^n - u^{n-1}) with Kahan compensation of u += d; it is the same
 // recurrence as the 3-level form (d^{n+1} = d^n - dt^2 M^-1 K inside,
 // ((M-A) d^n - dt^2 K)/(M+A) on the Stacey edges, injection adds the
-// increment to both u and d).
+// increment to both u and d).  The FP64 kernels are bound by the FP64 pipe
+// and spend registers to save its operations: z contractions in even-odd
+// form (mirror_sum) and the x-divergence weights times the row weight from a
+// shared table; the FP32 kernels are bound by issue and registers and keep
+// row-by-row sums.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
