@@ -920,7 +920,8 @@ def main() -> None:
     if not a.no_serve:
         serve = run_serve(gpu, 2.0, a.serve_requests)
         # FP32C requests only, arriving faster than they are served: the
-        # served form at saturation (its roofline is the spec check)
+        # served form at saturation (its roofline fraction is the served
+        # form's target: 0.6 of the HBM bandwidth)
         serve_sat = run_serve(gpu, 20.0, 48, seed=11, fp64_frac=0.0)
     accuracy = None
     if not a.no_accuracy:
