@@ -1251,11 +1251,18 @@ extern "C" int sks_state_load(sks_solver* s, const void* host, int64_t bytes)
                        h.precision, h.nx, h.nz, h.nst);
     if (h.nsnap != (s->snaps ? s->nsnap : 0)) return set_err(SKS_ERR_ARG, "the state's snapshot set differs");
     if (bytes < sks_state_bytes(s)) return set_err(SKS_ERR_ARG, "state buffer too short");
-    if (s->batch && batch_running(s->batch)) return set_err(SKS_ERR_STATE, "the solver's batch is running");
-    cudaSetDevice(s->device);
     void* const* p[3];
     size_t sz[3];
     state_arrays(s, p, sz);
+    // the header's step and buffer index pick the device buffers the next run
+    // reads, so a damaged header is refused before anything is copied
+    if (h.step < 0 || h.step > h.nst || (h.cur != 0 && h.cur != 1))
+        return set_err(SKS_ERR_ARG, "the state's step %d or buffer index %d is out of range", h.step, h.cur);
+    if (h.field_bytes != (int64_t)(sz[0] + sz[1] + sz[2]) ||
+        h.snap_bytes != (int64_t)((size_t)h.nsnap * s->snap_size * sizeof(float)))
+        return set_err(SKS_ERR_ARG, "the state's array sizes differ from the solve's");
+    if (s->batch && batch_running(s->batch)) return set_err(SKS_ERR_STATE, "the solver's batch is running");
+    cudaSetDevice(s->device);
     const char* in = (const char*)host + sizeof h;
     CK(cudaStreamSynchronize(s->stream));
     for (int i = 0; i < 3; i++) {

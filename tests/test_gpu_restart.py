@@ -83,6 +83,17 @@ def test_state_of_another_solve_is_refused(case, tmp_path):
     bad[:8] = 0
     with pytest.raises(sks.SksError):
         a64.load_state(bad)                     # not a state
+    # damaged header words: step (int32 at byte 28), buffer index (byte 32),
+    # field bytes (int64 at byte 40)
+    for off, val, dt in ((28, -1, np.int32), (28, c.nst + 1, np.int32), (32, 2, np.int32), (40, 8, np.int64)):
+        bad = s64.copy()
+        bad[off:off + np.dtype(dt).itemsize] = np.frombuffer(np.array([val], dt).tobytes(), np.uint8)
+        with pytest.raises(sks.SksError):
+            a64.load_state(bad)
+    a64.load_state(s64)                         # the solver is unchanged and runs on
+    assert a64.info()["step"] == 10
+    more = a64.run(5)
+    assert more[0].shape[0] == 5 and all(np.isfinite(x).all() for x in more)
     d2 = str(tmp_path)
     c2 = synth.Case(nex=21, nez=11, eh=1.0, sdt=0.005, nst=900, layers=_layers(11.002), p=0.045, f0=1.5,
                     ntrace=5, rec_dx=3.0, semmodel_full=True)
