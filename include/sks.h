@@ -307,10 +307,11 @@ int sks_line_increments(sks_solver *s, int32_t it0, int32_t nsteps, double *out)
  * scratch array inside the library, so (nsteps+2)*3*(nx+nz) must not exceed
  * 1048576 or the call fails with SKS_ERR_ARG.  The first call on a device
  * looks the scratch's device address up (cudaGetSymbolAddress) and keeps it
- * for that device's primary context, the one the CUDA runtime uses; a program
- * that destroys that context (cudaDeviceReset) or calls from another driver
- * API context must not call this entry again in that process.  Make that
- * first call before any stream capture.  All calls on a device
+ * for the context current at that call (normally the device's primary
+ * context, the one the CUDA runtime uses); a call made in another context (a
+ * new primary context after cudaDeviceReset, or a driver-API context the
+ * caller made current) looks it up again for that context.  Make the first
+ * call in a context before any stream capture.  All calls on a device
  * share the scratch and it keeps the last call's contents (every value a call
  * reads is written by that call first); calls whose work overlaps on the GPU
  * (other streams, other host threads) race on it. */

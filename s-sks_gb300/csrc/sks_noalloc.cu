@@ -14,6 +14,7 @@
 #include "sks_kernels.cuh"
 #include "sks_aux_kernels.cuh"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdio>
 #include <mutex>
@@ -27,14 +28,50 @@ extern "C" int sks_internal_set_error(int code, const char* msg, cudaError_t e);
 
 namespace {
 
-// Device address of the scratch, looked up once per device (with that device
-// current) in the device's primary context, which the CUDA runtime uses.  In
-// host code the array's name is only a stand-in for the device symbol, never
-// a usable address.
+// Device address of the scratch.  In host code the array's name is only a
+// stand-in for the device symbol, never a usable address; the address itself
+// belongs to a CUDA context (normally the device's primary context, which
+// the runtime uses).  It is looked up with the device current on the first
+// call, and again whenever the calling thread's current context is another
+// one than the address was taken in (a context created after
+// cudaDeviceReset, or a driver-API context the caller made current): contexts
+// are told apart by their process-unique id (cuCtxGetId), reached through the
+// runtime's driver entry points so the library needs no link to libcuda.
 std::mutex g_mu;
-double* g_addr[128] = {};
+struct Cached {
+    unsigned long long ctx;   // id of the context the address is valid in (0: none yet)
+    double* addr;
+};
+Cached g_addr[128] = {};
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
 
 int fail(int code, const char* msg, cudaError_t e = cudaSuccess) { return sks_internal_set_error(code, msg, e); }
+
+// id of the calling thread's current context, 0 when none is current yet
+// (called with g_mu held)
+int current_context(unsigned long long* id)
+{
+    *id = 0;
+    if (!g_ctx_current || !g_ctx_id) {
+        void* p1 = nullptr;
+        void* p2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p1, 12000, cudaEnableDefault, &q1);
+        if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &p2, 12000, cudaEnableDefault, &q2);
+        if (e != cudaSuccess || q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess)
+            return fail(SKS_ERR_CUDA, "driver entry points cuCtxGetCurrent / cuCtxGetId", e);
+        g_ctx_current = (CtxGetCurrentFn)p1;
+        g_ctx_id = (CtxGetIdFn)p2;
+    }
+    CUcontext c = nullptr;
+    if (g_ctx_current(&c) != CUDA_SUCCESS) return fail(SKS_ERR_CUDA, "cuCtxGetCurrent");
+    if (c && g_ctx_id(c, id) != CUDA_SUCCESS) return fail(SKS_ERR_CUDA, "cuCtxGetId");
+    return SKS_OK;
+}
 
 }  // namespace
 
@@ -62,13 +99,19 @@ extern "C" int sks_line_increments_noalloc(const float* rec_psv, const float* re
     double* scratch;
     {
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_addr[dev]) {
+        unsigned long long ctx = 0;
+        int rc = current_context(&ctx);
+        if (rc) return rc;
+        if (!ctx || g_addr[dev].ctx != ctx) {
+            // the lookup makes the runtime's context current when none is
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess) return fail(SKS_ERR_CUDA, "cudaGetSymbolAddress of the scratch", e);
-            g_addr[dev] = (double*)p;
+            if ((rc = current_context(&ctx))) return rc;
+            if (!ctx) return fail(SKS_ERR_CUDA, "no CUDA context is current after the scratch lookup");
+            g_addr[dev] = Cached{ctx, (double*)p};
         }
-        scratch = g_addr[dev];
+        scratch = g_addr[dev].addr;
     }
     cudaStream_t st = (cudaStream_t)stream;
     // rows 1..nsteps+1 of the scratch hold g(step) for the nsteps+1 steps the

@@ -8,9 +8,11 @@ FP64 interpolation rows go to a fixed scratch array inside the library.  Here
 the caller's buffers are made with torch, the call is made twice in a row
 (different step ranges, so the second call runs over the first one's scratch
 contents), and each result is compared with sks_line_increments() on the same
-solve.  This file is collected last on purpose.
+solve.  A third call comes from a fresh host thread, in which no CUDA context
+is current yet when the call starts.  This file is collected last on purpose.
 """
 import ctypes as C
+import threading
 
 import numpy as np
 import pytest
@@ -47,7 +49,7 @@ def test_noalloc_matches_allocating_entry_point(tmp_path):
         psv = torch.from_numpy(np.fromfile("greenfile", np.float32)).to(dev)
         sh = torch.from_numpy(np.fromfile("shgreenfile", np.float32)).to(dev)
         stream = torch.cuda.current_stream(dev)
-        for it0, n in ((5, 60), (120, 37)):        # two calls in a row
+        for it0, n, fresh in ((5, 60, False), (120, 37, False), (5, 60, True)):   # calls in a row
             ref = s.line_increments(it0, n)
             assert np.abs(ref).max() > 0
             sl = slice(it0, it0 + n + 1)           # the schedule of steps it0..it0+n
@@ -56,10 +58,21 @@ def test_noalloc_matches_allocating_entry_point(tmp_path):
             tap_s = torch.from_numpy(np.ascontiguousarray(ts[sl])).to(dev)
             w_s = torch.from_numpy(np.ascontiguousarray(ws[sl])).to(dev)
             out = torch.full((n, ref.shape[1], 3), float("nan"), dtype=torch.float64, device=dev)
-            rc = sks.lib().sks_line_increments_noalloc(_ptr(psv), _ptr(sh), nx, nz, nbl, _ptr(tap_p), _ptr(w_p),
-                                                       _ptr(tap_s), _ptr(w_s), n, _ptr(out),
-                                                       C.c_void_p(stream.cuda_stream))
-            assert rc == 0, sks.lib().sks_last_error().decode()
+            res = {}
+
+            def call():
+                res["rc"] = sks.lib().sks_line_increments_noalloc(_ptr(psv), _ptr(sh), nx, nz, nbl, _ptr(tap_p),
+                                                                  _ptr(w_p), _ptr(tap_s), _ptr(w_s), n, _ptr(out),
+                                                                  C.c_void_p(stream.cuda_stream))
+                res["err"] = sks.lib().sks_last_error().decode()   # the error text is per host thread
+
+            if fresh:
+                t = threading.Thread(target=call)
+                t.start()
+                t.join()
+            else:
+                call()
+            assert res["rc"] == 0, res["err"]
             torch.cuda.synchronize(dev)
             got = out.cpu().numpy()
             assert np.allclose(got, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
