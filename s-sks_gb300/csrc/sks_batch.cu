@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <string>
 
 using namespace sks;
 using namespace sksi;
@@ -661,6 +662,7 @@ extern "C" int sks_batch_set_tuning(sks_batch* b, const sks_tuning_t* t)
     if (b->running) return set_err(SKS_ERR_STATE, "the batch is running");
     cudaSetDevice(b->device);
     cudaStreamSynchronize(b->stream);
+    const int old[5] = {b->NW, b->HZ, b->ZS, b->CAP, b->PIPE};
     b->NW = t->warps_per_block;
     b->HZ = t->band_rows;
     b->ZS = t->zseam ? 1 : 0;
@@ -668,7 +670,18 @@ extern "C" int sks_batch_set_tuning(sks_batch* b, const sks_tuning_t* t)
     b->PIPE = t->pipeline;
     for (sks_solver* s : b->mem) {
         int rc = apply_tuning(b, s);
-        if (rc) return rc;
+        if (rc) {
+            // a member's grid could not follow (e.g. no memory for its seam
+            // buffers): every member goes back to the previous tuning, so the
+            // batch never runs with members on different grids
+            const std::string msg = sks_last_error();
+            b->NW = old[0]; b->HZ = old[1]; b->ZS = old[2]; b->CAP = old[3]; b->PIPE = old[4];
+            for (sks_solver* r : b->mem) apply_tuning(b, r);
+            set_persistent_grid(b);
+            b->tables_dirty = true;
+            b->graph_dirty = true;
+            return set_err(rc, "%s", msg.c_str());
+        }
     }
     set_persistent_grid(b);
     b->tables_dirty = true;
