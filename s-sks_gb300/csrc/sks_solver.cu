@@ -1098,12 +1098,19 @@ extern "C" int sks_run(sks_solver* s, int32_t nsteps, float* su, float* sv, floa
             s->slot_busy[slot] = false;
         }
         s->seis = s->seisbuf[slot];
+        // a failed chunk returns only once the copies already queued into the
+        // caller's arrays have landed, so the caller may free them at once
+        auto bail = [&](int code) {
+            cudaStreamSynchronize(s->copy_stream);
+            s->slot_busy[0] = s->slot_busy[1] = false;
+            return code;
+        };
         int rc = run_chunk(s, s->step, n);
-        if (rc) return rc;
+        if (rc) return bail(rc);
         if (want) CK(cudaEventRecord(s->chunk_done[slot], s->stream));
         rc = collect_timing(s);
-        if (rc) return rc;
-        if (want && pend.slot >= 0 && (rc = issue_copy(pend))) return rc;
+        if (rc) return bail(rc);
+        if (want && pend.slot >= 0 && (rc = issue_copy(pend))) return bail(rc);
         pend = want ? Pending{slot, n, done} : Pending{-1, 0, 0};
         if (s->snaps)
             for (int it = s->step; it < s->step + n; it++) {
