@@ -16,9 +16,10 @@ at full size, so the chain GPU -> oracle -> reference holds there too:
       field of every second point is compared as well as the seismograms.
 
 c0_short and c1_short are the same meshes over 300 and 8 steps with
-snapshots inside the window; `--record` writes their input and output
-digests to tests/golden/config_pins.json, which the CPU tests compare the
-float oracle with (tests/test_oracle_pin_configs.py).
+snapshots inside the window.  `--record` writes each case's input and
+output digests to tests/golden/config_pins.json; the CPU tests compare the
+float oracle with the short cases' digests (tests/test_oracle_pin_configs.py),
+and the long cases' digests are kept there as the record of those runs.
 
 Each program runs on the same input files in a directory of its own, both at
 once; seis.u / seis.v / seis.w and the snapshot files out1.. must be equal
@@ -155,7 +156,7 @@ def main():
         r = pin(n)
         print(json.dumps(r), flush=True)
         ok = ok and r["bit_exact"]
-        if record and n.endswith("_short"):
+        if record:
             case, prog, oracle_words, words = CASES[n]()
             rec[n] = {"program": prog, "steps": case.nst, "points": r["points"], "words": oracle_words + words,
                       "inputs_sha256": r["inputs_sha256"],

@@ -36,7 +36,8 @@ RECORD = os.path.join(HERE, "golden", "config_pins.json")
 ORACLE32 = os.path.join(orc.BUILD, "oracle_sem2d_psvsh32")
 
 with open(RECORD) as _f:
-    PINS = json.load(_f)
+    # the short windows; the whole-solve records take minutes of CPU each
+    PINS = {k: v for k, v in json.load(_f).items() if k.endswith("_short")}
 
 
 def _sha(path):
