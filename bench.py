@@ -814,6 +814,7 @@ def main() -> None:
     ap.add_argument("--serve-tuning", default="4,12,0,1,1",
                     help="with --serve-rates: W,B,Z,C,P of the FP32C batch (P: pipelined chunks)")
     a = ap.parse_args()
+    warmup_requested = a.warmup
     a.warmup = max(3, a.warmup)
     dist, rank, world, local = _dist()
 
@@ -841,7 +842,7 @@ def main() -> None:
                 "config": {"workload": WORKLOAD, "form": "reference float arithmetic",
                            "step": f"one time step of the 3,844,401-point mesh in each of {ncpu} independent "
                                    "single-threaded solves running at once",
-                           "steps_requested": a.steps, "warmup_requested": a.warmup},
+                           "steps_requested": a.steps, "warmup_requested": warmup_requested},
                 "cpu_baseline": {"value": v, "unit": "GLL-pt updates/s", "cores": ncpu, "kind": "port",
                                  "sample": f"{kwarm} untimed then {ksteps} timed time steps of the full mesh in "
                                            f"each of {ncpu} independent single-threaded processes (oracle float "
